@@ -1,0 +1,668 @@
+// C ABI (include/sbec.h) and the host-side drivers that loop over the device
+// operators: split_step!, the leapfrog / standard run_simulation! loops, the
+// adaptive Strang and Yoshida loops and the find_ground_state ITP loop.  Each
+// driver restates the control flow of the reference file:line it cites; the
+// per-step arithmetic runs in the device kernels (sbec_kernels.cuh).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "sbec.h"
+#include "sbec_engine.h"
+#include "sbec_setup.h"
+
+namespace sbec {
+
+void cuda_check(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return;
+  cudaGetLastError();
+  const sbec_status st = (e == cudaErrorMemoryAllocation) ? SBEC_ERR_OOM : SBEC_ERR_DEVICE;
+  throw SbecError{st, std::string(what) + ": " + cudaGetErrorString(e)};
+}
+
+}  // namespace sbec
+
+using namespace sbec;
+
+struct sbec_ws {
+  std::unique_ptr<EngineBase> eng;
+  double kin_dt = 0.0;    // parameters of the current kinetic phase (the batched kinetic cache)
+  bool kin_itp = false;
+  std::vector<double> host_psi;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+#define SBEC_API_BEGIN try {
+#define SBEC_API_END                                      \
+  }                                                       \
+  catch (const SbecError& e) {                            \
+    g_err = e.msg;                                        \
+    return e.status;                                      \
+  }                                                       \
+  catch (const std::bad_alloc&) {                         \
+    g_err = "host allocation failed";                     \
+    return SBEC_ERR_OOM;                                  \
+  }                                                       \
+  catch (const std::exception& e) {                       \
+    g_err = e.what();                                     \
+    return SBEC_ERR_DEVICE;                               \
+  }                                                       \
+  return SBEC_OK;
+
+void need(const void* p, const char* what) {
+  if (!p) fail(SBEC_ERR_INVALID, std::string(what) + " must not be NULL");
+}
+
+EngineBase& E(sbec_ws* ws) {
+  need(ws, "workspace");
+  return *ws->eng;
+}
+
+// ---- operator sequences shared by the drivers -----------------------------
+
+void kinetic(sbec_ws* ws, double dt, bool itp) {
+  ws->kin_dt = dt;
+  ws->kin_itp = itp;
+  ws->eng->kinetic(dt, itp);
+}
+
+// split_step! (src/split_step.jl:10-35)
+void split_step_once(sbec_ws* ws) {
+  EngineBase& e = *ws->eng;
+  const double dt = e.dt;
+  const bool it = e.itp;
+  e.half_potential(dt / 2, it);
+  e.kinetic(ws->kin_dt, ws->kin_itp);
+  e.half_potential(dt / 2, it);
+  e.t += it ? 0.0 : dt;
+  e.step += 1;
+  if (it && e.normalize_every > 0 && e.step % e.normalize_every == 0) e.normalize();
+}
+
+// _strang_core! (src/split_step.jl:146-152)
+void strang_core(sbec_ws* ws, double dt) {
+  ws->eng->half_potential(dt / 2, false);
+  kinetic(ws, dt, false);
+  ws->eng->half_potential(dt / 2, false);
+}
+
+const double kW1 = 1.0 / (2.0 - std::pow(2.0, 1.0 / 3.0));
+const double kW0 = 1.0 - 2.0 * kW1;
+
+// _yoshida_core! (src/split_step.jl:161-183)
+void yoshida_core(sbec_ws* ws, double dt) {
+  const double w1 = kW1, w0 = kW0, wm = (w1 + w0) / 2;
+  EngineBase& e = *ws->eng;
+  e.half_potential(w1 * dt / 2, false);
+  kinetic(ws, w1 * dt, false);
+  e.half_potential(wm * dt, false);
+  kinetic(ws, w0 * dt, false);
+  e.half_potential(wm * dt, false);
+  kinetic(ws, w1 * dt, false);
+  e.half_potential(w1 * dt / 2, false);
+}
+
+double total_energy(EngineBase& e) {
+  const sbec_energy_terms t = e.energy_terms();
+  return t.kinetic + t.trap + t.zeeman + t.c0 + t.c1 + t.ddi + t.lhy + t.tensor;
+}
+
+void norm_and_mz(EngineBase& e, double* norm, double* mz) {
+  const Setup& s = e.setup();
+  std::vector<double> sums(s.D);
+  double nan = 0;
+  e.comp_norms(sums.data(), &nan);
+  double n = 0.0, m = 0.0;
+  for (int c = 0; c < s.D; ++c) {
+    n += sums[c];
+    m += (double)(s.F - c) * sums[c] * s.dV;
+  }
+  *norm = n * s.dV;
+  *mz = m;
+}
+
+// _record_snapshot! (src/simulation_utils.jl:9-15) delivered to the callback.
+int snapshot(sbec_ws* ws, sbec_callback cb, void* user) {
+  if (!cb) return 0;
+  EngineBase& e = *ws->eng;
+  sbec_snapshot sn{};
+  sn.t = e.t;
+  sn.step = e.step;
+  sn.energy = total_energy(e);
+  norm_and_mz(e, &sn.norm, &sn.magnetization);
+  const Setup& s = e.setup();
+  ws->host_psi.resize((size_t)2 * s.N * s.D);
+  e.get_psi(ws->host_psi.data());
+  sn.psi = ws->host_psi.data();
+  return cb(user, &sn);
+}
+
+void check_cb(int rc) {
+  if (rc != 0) fail(SBEC_ERR_CALLBACK, "callback requested stop");
+}
+
+// _normalize_psi_constrained! (src/ground_state.jl:279-320)
+void normalize_constrained(EngineBase& e, double target) {
+  const Setup& s = e.setup();
+  const int D = s.D, F = s.F;
+  e.normalize();
+  std::vector<double> raw(D);
+  double nan = 0;
+  e.comp_norms(raw.data(), &nan);
+  double lambda = 0.0;
+  std::vector<double> norms(D);
+  for (int it = 0; it < 20; ++it) {
+    for (int c = 0; c < D; ++c) {
+      const int m = F - c;
+      const double w = std::exp(lambda * m);
+      norms[c] = raw[c] * s.dV * (w * w);
+    }
+    double total = 0.0;
+    for (int c = 0; c < D; ++c) total += norms[c];
+    if (total < 1e-30) break;
+    double Mz = 0.0;
+    for (int c = 0; c < D; ++c) Mz += (double)(F - c) * norms[c];
+    Mz /= total;
+    if (std::fabs(Mz - target) < 1e-12) break;
+    double dMz = 0.0;
+    for (int c = 0; c < D; ++c) {
+      const double m = (double)(F - c);
+      dMz += 2 * m * (m - Mz) * norms[c] / total;
+    }
+    if (std::fabs(dMz) < 1e-30) break;
+    lambda -= (Mz - target) / dMz;
+    lambda = std::min(10.0, std::max(-10.0, lambda));
+  }
+  std::vector<double> w(D);
+  for (int c = 0; c < D; ++c) w[c] = std::exp(lambda * (double)(F - c));
+  e.scale_components(w.data());
+  e.normalize();
+}
+
+// _check_itp_overflow (src/ground_state.jl:4-29)
+void check_itp_overflow(EngineBase& e, long long step) {
+  const Setup& s = e.setup();
+  std::vector<double> sums(s.D);
+  double nan = 0;
+  e.comp_norms(sums.data(), &nan);
+  if (nan > 0)
+    fail(SBEC_ERR_NUMERIC, "NaN detected in ITP at step " + std::to_string(step) +
+                               ". Likely DDI potential overflow. Reduce dt.");
+  if (!s.ddi) return;
+  const double phi_max = e.ddi_phi_max();
+  const double exponent = phi_max * e.dt / 2;
+  if (exponent > 50.0)
+    fail(SBEC_ERR_NUMERIC, "DDI potential overflow in ITP at step " + std::to_string(step) + ": exponent=" +
+                               std::to_string(exponent) + " > 50. Reduce dt.");
+}
+
+}  // namespace
+
+// ============================================================================
+extern "C" {
+
+const char* sbec_last_error(void) { return g_err.c_str(); }
+
+const char* sbec_version(void) { return "sbec-gb300 0.1 (sm_103a)"; }
+
+int sbec_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+sbec_status sbec_ws_create(const sbec_config* cfg, const double* psi, const double* V, sbec_ws** out) {
+  SBEC_API_BEGIN
+  need(cfg, "config");
+  need(psi, "psi");
+  need(out, "out");
+  *out = nullptr;
+  Setup s = build_setup(*cfg);
+  if (sbec_device_count() < 1) fail(SBEC_ERR_DEVICE, "no CUDA device available (the GPU path has no CPU fallback)");
+  auto ws = std::make_unique<sbec_ws>();
+  ws->eng = cfg->precision == SBEC_FP32_BULK ? make_engine_f32(s) : make_engine_f64(s);
+  EngineBase& e = *ws->eng;
+  e.zeeman_p = cfg->zeeman_p;
+  e.zeeman_q = cfg->zeeman_q;
+  e.dt = cfg->dt;
+  e.itp = cfg->imaginary_time != 0;
+  e.normalize_every = cfg->normalize_every;
+  ws->kin_dt = cfg->dt;
+  ws->kin_itp = e.itp;
+  e.set_psi(psi);
+  if (V) e.set_potential(V);
+  e.sync();
+  *out = ws.release();
+  SBEC_API_END
+}
+
+sbec_status sbec_ws_destroy(sbec_ws* ws) {
+  SBEC_API_BEGIN
+  delete ws;
+  SBEC_API_END
+}
+
+sbec_status sbec_set_psi(sbec_ws* ws, const double* psi) {
+  SBEC_API_BEGIN
+  need(psi, "psi");
+  E(ws).set_psi(psi);
+  E(ws).sync();
+  SBEC_API_END
+}
+
+sbec_status sbec_get_psi(sbec_ws* ws, double* psi) {
+  SBEC_API_BEGIN
+  need(psi, "psi");
+  E(ws).get_psi(psi);
+  SBEC_API_END
+}
+
+sbec_status sbec_set_time(sbec_ws* ws, double t, int64_t step) {
+  SBEC_API_BEGIN
+  E(ws).t = t;
+  E(ws).step = step;
+  SBEC_API_END
+}
+
+sbec_status sbec_get_time(sbec_ws* ws, double* t, int64_t* step) {
+  SBEC_API_BEGIN
+  if (t) *t = E(ws).t;
+  if (step) *step = E(ws).step;
+  SBEC_API_END
+}
+
+sbec_status sbec_set_zeeman(sbec_ws* ws, double p, double q) {
+  SBEC_API_BEGIN
+  E(ws).zeeman_p = p;
+  E(ws).zeeman_q = q;
+  SBEC_API_END
+}
+
+sbec_status sbec_set_potential(sbec_ws* ws, const double* V) {
+  SBEC_API_BEGIN
+  need(V, "V");
+  E(ws).set_potential(V);
+  SBEC_API_END
+}
+
+sbec_status sbec_set_dt(sbec_ws* ws, double dt) {
+  SBEC_API_BEGIN
+  if (!(dt > 0)) fail(SBEC_ERR_INVALID, "dt must be positive");
+  E(ws).dt = dt;
+  ws->kin_dt = dt;
+  ws->kin_itp = E(ws).itp;
+  SBEC_API_END
+}
+
+sbec_status sbec_tensor_channels(sbec_ws* ws, int32_t* active, int32_t* n_channels, int32_t* S, double* gS) {
+  SBEC_API_BEGIN
+  const Setup& s = E(ws).setup();
+  if (active) *active = s.tensor ? 1 : 0;
+  if (n_channels) *n_channels = (int32_t)s.chS.size();
+  for (size_t i = 0; i < s.chS.size(); ++i) {
+    if (S) S[i] = s.chS[i];
+    if (gS) gS[i] = s.chG[i];
+  }
+  SBEC_API_END
+}
+
+sbec_status sbec_half_potential(sbec_ws* ws, double dt_half, int32_t imaginary_time) {
+  SBEC_API_BEGIN
+  E(ws).half_potential(dt_half, imaginary_time != 0);
+  E(ws).sync();
+  SBEC_API_END
+}
+
+sbec_status sbec_kinetic(sbec_ws* ws, double dt, int32_t imaginary_time) {
+  SBEC_API_BEGIN
+  E(ws);
+  kinetic(ws, dt, imaginary_time != 0);
+  ws->eng->sync();
+  SBEC_API_END
+}
+
+sbec_status sbec_normalize(sbec_ws* ws) {
+  SBEC_API_BEGIN
+  E(ws).normalize();
+  E(ws).sync();
+  SBEC_API_END
+}
+
+sbec_status sbec_normalize_constrained(sbec_ws* ws, double target_Mz) {
+  SBEC_API_BEGIN
+  normalize_constrained(E(ws), target_Mz);
+  E(ws).sync();
+  SBEC_API_END
+}
+
+sbec_status sbec_split_step(sbec_ws* ws, int64_t n) {
+  SBEC_API_BEGIN
+  E(ws);
+  for (int64_t i = 0; i < n; ++i) split_step_once(ws);
+  ws->eng->sync();
+  SBEC_API_END
+}
+
+sbec_status sbec_strang_core(sbec_ws* ws, double dt) {
+  SBEC_API_BEGIN
+  E(ws);
+  strang_core(ws, dt);
+  ws->eng->sync();
+  SBEC_API_END
+}
+
+sbec_status sbec_yoshida_core(sbec_ws* ws, double dt) {
+  SBEC_API_BEGIN
+  E(ws);
+  yoshida_core(ws, dt);
+  ws->eng->sync();
+  SBEC_API_END
+}
+
+// run_simulation! (src/simulation.jl:1-94)
+sbec_status sbec_run_simulation(sbec_ws* ws, int64_t n_steps, int64_t save_every, sbec_callback cb, void* user) {
+  SBEC_API_BEGIN
+  EngineBase& e = E(ws);
+  if (n_steps <= 0) fail(SBEC_ERR_INVALID, "n_steps must be positive");
+  if (save_every <= 0) fail(SBEC_ERR_INVALID, "save_every must be positive");
+  check_cb(snapshot(ws, cb, user));
+  if (e.itp) {
+    for (int64_t step = 1; step <= n_steps; ++step) {
+      split_step_once(ws);
+      if (step % save_every == 0) check_cb(snapshot(ws, cb, user));
+    }
+  } else {
+    const double dt = e.dt;
+    e.half_potential(dt / 2, false);
+    for (int64_t step = 1; step <= n_steps; ++step) {
+      e.kinetic(ws->kin_dt, ws->kin_itp);
+      const bool is_save = step % save_every == 0;
+      const bool is_last = step == n_steps;
+      const bool need_split = is_save || is_last;
+      e.half_potential(need_split ? dt / 2 : dt, false);
+      e.t += dt;
+      e.step += 1;
+      if (is_save) check_cb(snapshot(ws, cb, user));
+      if (need_split && !is_last) e.half_potential(dt / 2, false);
+    }
+  }
+  e.sync();
+  SBEC_API_END
+}
+
+// run_simulation_adaptive! (src/adaptive.jl:57-296)
+sbec_status sbec_run_adaptive(sbec_ws* ws, const sbec_adaptive_params* p, double t_end, double save_interval,
+                              sbec_callback cb, void* user, sbec_adaptive_result* out) {
+  SBEC_API_BEGIN
+  EngineBase& e = E(ws);
+  need(p, "params");
+  if (!(p->dt_init > 0) || !(p->dt_min > 0) || !(p->dt_max >= p->dt_min) || !(p->tol > 0))
+    fail(SBEC_ERR_INVALID, "invalid AdaptiveDtParams");
+  double dt = std::min(std::max(p->dt_init, p->dt_min), p->dt_max);
+  long long n_acc = 0, n_rej = 0;
+  check_cb(snapshot(ws, cb, user));
+  double next_save = e.t + save_interval;
+  if (p->error_mode == 0) {
+    // _adaptive_step_change_loop! (src/adaptive.jl:69-195)
+    double current_kinetic_dt = NAN;
+    bool fsal_deferred = false;
+    double fsal_dt = 0.0;
+    while (e.t < t_end - 1e-14) {
+      double dt_step = std::min(dt, t_end - e.t);
+      const double rem = next_save - e.t;
+      if (rem > 1e-14 && rem < dt_step) dt_step = rem;
+      dt_step = std::max(dt_step, p->dt_min);
+      const bool is_clamped = dt_step < dt * 0.99;
+      const bool may_reject = !is_clamped && dt_step > p->dt_min * 1.01;
+      if (dt_step != current_kinetic_dt) current_kinetic_dt = dt_step;
+      if (!is_clamped) e.copy_slot(kSlotA, kPsi);
+      const bool prev_fd = fsal_deferred;
+      const double prev_fdt = fsal_dt;
+      if (fsal_deferred && std::fabs(fsal_dt - dt_step) < 1e-14) {
+        e.half_potential(dt_step, false);
+      } else if (fsal_deferred) {
+        e.half_potential(fsal_dt / 2, false);
+        e.half_potential(dt_step / 2, false);
+      } else {
+        e.half_potential(dt_step / 2, false);
+      }
+      fsal_deferred = false;
+      kinetic(ws, current_kinetic_dt, false);
+      double rel = 0.0;
+      if (may_reject) {
+        rel = e.l2_change(kPsi, kSlotA);
+        if (rel > p->tol) {
+          e.copy_slot(kPsi, kSlotA);
+          fsal_deferred = prev_fd;
+          fsal_dt = prev_fdt;
+          const double factor = std::max(0.5, 0.9 * std::sqrt(p->tol / rel));
+          dt = std::max(dt_step * factor, p->dt_min);
+          current_kinetic_dt = NAN;
+          ++n_rej;
+          continue;
+        }
+      }
+      fsal_deferred = true;
+      fsal_dt = dt_step;
+      e.t += dt_step;
+      e.step += 1;
+      ++n_acc;
+      if (!is_clamped) {
+        if (!may_reject) rel = e.l2_change(kPsi, kSlotA);
+        const double factor = rel > 1e-300 ? std::min(2.0, 0.9 * std::sqrt(p->tol / rel)) : 2.0;
+        dt = std::min(std::max(dt * factor, p->dt_min), p->dt_max);
+      }
+      if (e.t >= next_save - 1e-14) {
+        e.half_potential(fsal_dt / 2, false);
+        fsal_deferred = false;
+        check_cb(snapshot(ws, cb, user));
+        next_save += save_interval;
+      }
+    }
+    if (fsal_deferred) e.half_potential(fsal_dt / 2, false);
+  } else {
+    // _adaptive_richardson_loop! (src/adaptive.jl:204-296)
+    while (e.t < t_end - 1e-14) {
+      double dt_step = std::min(dt, t_end - e.t);
+      const double rem = next_save - e.t;
+      if (rem > 1e-14 && rem < dt_step) dt_step = rem;
+      dt_step = std::max(dt_step, p->dt_min);
+      const bool is_clamped = dt_step < dt * 0.99;
+      const bool may_reject = !is_clamped && dt_step > p->dt_min * 1.01;
+      e.copy_slot(kSlotA, kPsi);
+      e.half_potential(dt_step / 2, false);
+      kinetic(ws, dt_step, false);
+      e.half_potential(dt_step / 2, false);
+      e.copy_slot(kSlotB, kPsi);
+      e.copy_slot(kPsi, kSlotA);
+      const double dt_half = dt_step / 2;
+      for (int r = 0; r < 2; ++r) {
+        e.half_potential(dt_half / 2, false);
+        kinetic(ws, dt_half, false);
+        e.half_potential(dt_half / 2, false);
+      }
+      const double err = e.l2_change(kSlotB, kPsi);
+      if (may_reject && err > p->tol) {
+        e.copy_slot(kPsi, kSlotA);
+        const double factor = std::max(0.5, 0.9 * std::cbrt(p->tol / err));
+        dt = std::max(dt_step * factor, p->dt_min);
+        ++n_rej;
+        continue;
+      }
+      e.t += dt_step;
+      e.step += 1;
+      ++n_acc;
+      if (!is_clamped) {
+        const double factor = err > 1e-300 ? std::min(2.0, 0.9 * std::cbrt(p->tol / err)) : 2.0;
+        dt = std::min(std::max(dt * factor, p->dt_min), p->dt_max);
+      }
+      if (e.t >= next_save - 1e-14) {
+        check_cb(snapshot(ws, cb, user));
+        next_save += save_interval;
+      }
+    }
+  }
+  e.sync();
+  if (out) {
+    out->n_accepted = n_acc;
+    out->n_rejected = n_rej;
+    out->final_dt = dt;
+  }
+  SBEC_API_END
+}
+
+// run_simulation_yoshida! (src/yoshida.jl:11-98)
+sbec_status sbec_run_yoshida(sbec_ws* ws, const sbec_adaptive_params* p, double t_end, double save_interval,
+                             int64_t max_accepted, sbec_callback cb, void* user, sbec_adaptive_result* out) {
+  SBEC_API_BEGIN
+  EngineBase& e = E(ws);
+  need(p, "params");
+  if (!(p->dt_init > 0) || !(p->dt_min > 0) || !(p->dt_max >= p->dt_min) || !(p->tol > 0))
+    fail(SBEC_ERR_INVALID, "invalid AdaptiveDtParams");
+  double dt = std::min(std::max(p->dt_init, p->dt_min), p->dt_max);
+  long long n_acc = 0, n_rej = 0;
+  check_cb(snapshot(ws, cb, user));
+  double next_save = e.t + save_interval;
+  while (e.t < t_end - 1e-14) {
+    if (max_accepted > 0 && n_acc >= max_accepted) break;
+    double dt_step = std::min(dt, t_end - e.t);
+    const double rem = next_save - e.t;
+    if (rem > 1e-14 && rem < dt_step) dt_step = rem;
+    dt_step = std::max(dt_step, p->dt_min);
+    const bool is_clamped = dt_step < dt * 0.99;
+    e.copy_slot(kSlotA, kPsi);
+    strang_core(ws, dt_step);
+    e.copy_slot(kSlotB, kPsi);
+    e.copy_slot(kPsi, kSlotA);
+    yoshida_core(ws, dt_step);
+    const double err = e.l2_change(kPsi, kSlotB);
+    if (!is_clamped && err > p->tol && dt_step > p->dt_min * 1.01) {
+      e.copy_slot(kPsi, kSlotA);
+      const double factor = std::max(0.3, 0.9 * std::pow(p->tol / err, 0.2));
+      dt = std::max(dt_step * factor, p->dt_min);
+      ++n_rej;
+      continue;
+    }
+    e.t += dt_step;
+    e.step += 1;
+    ++n_acc;
+    if (!is_clamped) {
+      const double factor = err > 1e-300 ? std::min(3.0, 0.9 * std::pow(p->tol / err, 0.2)) : 3.0;
+      dt = std::min(std::max(dt * factor, p->dt_min), p->dt_max);
+    }
+    if (e.t >= next_save - 1e-14) {
+      check_cb(snapshot(ws, cb, user));
+      next_save += save_interval;
+    }
+  }
+  e.sync();
+  if (out) {
+    out->n_accepted = n_acc;
+    out->n_rejected = n_rej;
+    out->final_dt = dt;
+  }
+  SBEC_API_END
+}
+
+// find_ground_state ITP loop (src/ground_state.jl:116-169)
+sbec_status sbec_ground_state(sbec_ws* ws, int64_t n_steps, double tol, int64_t check_every, double target_Mz,
+                              sbec_gs_result* out) {
+  SBEC_API_BEGIN
+  EngineBase& e = E(ws);
+  if (!e.itp) fail(SBEC_ERR_INVALID, "sbec_ground_state needs an imaginary-time workspace");
+  if (n_steps <= 0 || check_every <= 0) fail(SBEC_ERR_INVALID, "n_steps and check_every must be positive");
+  const bool use_c = !std::isnan(target_Mz);
+  if (use_c) normalize_constrained(e, target_Mz);
+  double E_prev = total_energy(e);
+  bool converged = false;
+  e.copy_slot(kSlotA, kPsi);
+  double final_dE = NAN, final_dpsi = NAN;
+  int64_t steps = 0;
+  for (int64_t step = 1; step <= n_steps; ++step) {
+    split_step_once(ws);
+    steps = step;
+    if (step <= 10) check_itp_overflow(e, step);
+    if (use_c) normalize_constrained(e, target_Mz);
+    if (step % check_every == 0) {
+      const double En = total_energy(e);
+      const double dE = std::fabs(En - E_prev);
+      double pmax = 0, dmax = 0;
+      e.max_abs(kPsi, kSlotA, &pmax, &dmax);
+      const double dpsi = pmax > 0 ? dmax / pmax : 0.0;
+      final_dE = dE;
+      final_dpsi = dpsi;
+      if (dE < tol && dpsi < tol) {
+        converged = true;
+        break;
+      }
+      E_prev = En;
+      e.copy_slot(kSlotA, kPsi);
+    }
+  }
+  const double Efin = total_energy(e);
+  if (out) {
+    out->converged = converged ? 1 : 0;
+    out->energy = Efin;
+    out->dE = final_dE;
+    out->dpsi = final_dpsi;
+    out->steps = steps;
+  }
+  SBEC_API_END
+}
+
+sbec_status sbec_total_energy(sbec_ws* ws, double* Eout) {
+  SBEC_API_BEGIN
+  need(Eout, "E");
+  *Eout = total_energy(E(ws));
+  SBEC_API_END
+}
+
+sbec_status sbec_energy_breakdown(sbec_ws* ws, sbec_energy_terms* out) {
+  SBEC_API_BEGIN
+  need(out, "out");
+  *out = E(ws).energy_terms();
+  SBEC_API_END
+}
+
+sbec_status sbec_total_norm(sbec_ws* ws, double* norm) {
+  SBEC_API_BEGIN
+  need(norm, "norm");
+  double mz;
+  norm_and_mz(E(ws), norm, &mz);
+  SBEC_API_END
+}
+
+sbec_status sbec_magnetization(sbec_ws* ws, double* Mz) {
+  SBEC_API_BEGIN
+  need(Mz, "Mz");
+  double n;
+  norm_and_mz(E(ws), &n, Mz);
+  SBEC_API_END
+}
+
+sbec_status sbec_spin_density(sbec_ws* ws, double* out) {
+  SBEC_API_BEGIN
+  need(out, "out");
+  E(ws).spin_density(out);
+  SBEC_API_END
+}
+
+sbec_status sbec_ddi_potential(sbec_ws* ws, int32_t padded, double* out) {
+  SBEC_API_BEGIN
+  need(out, "out");
+  E(ws).ddi_potential(padded != 0, out);
+  SBEC_API_END
+}
+
+}  // extern "C"

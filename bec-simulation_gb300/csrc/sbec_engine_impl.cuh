@@ -1,0 +1,815 @@
+// Engine<R>: device buffers of one workspace and the launch sequences of the
+// split-step operators.  Included once per precision (sbec_engine_f64.cu,
+// sbec_engine_f32.cu).
+#pragma once
+
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "sbec_engine.h"
+#include "sbec_kernels.cuh"
+
+namespace sbec {
+
+// ---------------------------------------------------------------------------
+// Tile shapes
+// ---------------------------------------------------------------------------
+template <typename R, int N>
+constexpr int x_lines_per_block() {
+  constexpr int tpl = N / FftPlan<N>::E;
+  constexpr int target = (sizeof(R) == 8 ? 2048 : 4096) / N;
+  constexpr int lpb = target < 1 ? 1 : target;
+  return lpb * tpl > 1024 ? 1024 / tpl : lpb;
+}
+
+template <typename R, int N>
+constexpr int strided_width() {
+  constexpr int tpl = N / FftPlan<N>::E;
+  constexpr int smem_budget = 96 * 1024;
+  int w = sizeof(R) == 8 ? 16 : 32;
+  while (w > 1 && (w * tpl > 1024 || (long)w * N * (int)sizeof(cplx<R>) > smem_budget)) w /= 2;
+  return w;
+}
+
+template <typename R, int MH>
+constexpr int ddi_x_rows_per_block() {
+  constexpr int tpl = MH / FftPlan<MH>::E;
+  constexpr int smem_budget = 96 * 1024;
+  int lpb = 8;
+  while (lpb > 1 && (3 * lpb * tpl > 1024 || (long)3 * lpb * (2 * MH + 1) * (int)sizeof(cplx<R>) > smem_budget))
+    lpb /= 2;
+  return lpb;
+}
+
+template <typename R, int M>
+constexpr int ddi_last_width() {
+  constexpr int tpl = M / FftPlan<M>::E;
+  constexpr int smem_budget = 100 * 1024;
+  int w = sizeof(R) == 8 ? 8 : 16;
+  while (w > 1 && (3 * w * tpl > 1024 || (long)3 * w * M * (int)sizeof(cplx<R>) > smem_budget)) w /= 2;
+  return w;
+}
+
+template <typename K>
+inline void set_smem(K kernel, size_t bytes) {
+  if (bytes > 48 * 1024) cuda_check(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes),
+                                    "cudaFuncSetAttribute");
+}
+
+#define SBEC_SWITCH_POW2(n, FN, ...)                                 \
+  switch (n) {                                                       \
+    case 2: FN<2>(__VA_ARGS__); break;                               \
+    case 4: FN<4>(__VA_ARGS__); break;                               \
+    case 8: FN<8>(__VA_ARGS__); break;                               \
+    case 16: FN<16>(__VA_ARGS__); break;                             \
+    case 32: FN<32>(__VA_ARGS__); break;                             \
+    case 64: FN<64>(__VA_ARGS__); break;                             \
+    case 128: FN<128>(__VA_ARGS__); break;                           \
+    case 256: FN<256>(__VA_ARGS__); break;                           \
+    case 512: FN<512>(__VA_ARGS__); break;                           \
+    case 1024: FN<1024>(__VA_ARGS__); break;                         \
+    case 2048: FN<2048>(__VA_ARGS__); break;                         \
+    case 4096: FN<4096>(__VA_ARGS__); break;                         \
+    default: fail(SBEC_ERR_UNSUPPORTED, "unsupported FFT length " + std::to_string(n)); \
+  }
+
+#define SBEC_SWITCH_POW2_STRIDED(n, FN, ...)                         \
+  switch (n) {                                                       \
+    case 2: FN<2>(__VA_ARGS__); break;                               \
+    case 4: FN<4>(__VA_ARGS__); break;                               \
+    case 8: FN<8>(__VA_ARGS__); break;                               \
+    case 16: FN<16>(__VA_ARGS__); break;                             \
+    case 32: FN<32>(__VA_ARGS__); break;                             \
+    case 64: FN<64>(__VA_ARGS__); break;                             \
+    case 128: FN<128>(__VA_ARGS__); break;                           \
+    case 256: FN<256>(__VA_ARGS__); break;                           \
+    case 512: FN<512>(__VA_ARGS__); break;                           \
+    case 1024: FN<1024>(__VA_ARGS__); break;                         \
+    default: fail(SBEC_ERR_UNSUPPORTED, "unsupported FFT length " + std::to_string(n)); \
+  }
+
+#define SBEC_SWITCH_D(D, FN, ...)                                    \
+  switch (D) {                                                       \
+    case 1: FN<1>(__VA_ARGS__); break;                               \
+    case 3: FN<3>(__VA_ARGS__); break;                               \
+    case 5: FN<5>(__VA_ARGS__); break;                               \
+    case 7: FN<7>(__VA_ARGS__); break;                               \
+    case 9: FN<9>(__VA_ARGS__); break;                               \
+    case 11: FN<11>(__VA_ARGS__); break;                             \
+    case 13: FN<13>(__VA_ARGS__); break;                             \
+    default: fail(SBEC_ERR_UNSUPPORTED, "unsupported component count"); \
+  }
+
+// ---------------------------------------------------------------------------
+template <typename R>
+class Engine final : public EngineBase {
+ public:
+  explicit Engine(const Setup& s) : EngineBase(s) {
+    cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+    const int D = s_.D;
+    N_ = s_.N;
+    nc_ = N_ * D;
+    psi_[kPsi] = alloc<cplx<R>>(nc_);
+    V_ = alloc<R>(N_);
+    cuda_check(cudaMemsetAsync(V_, 0, sizeof(R) * N_, stream_), "memset V");
+    for (int a = 0; a < s_.ndim; ++a) ptab_[a] = alloc<cplx<R>>(s_.n[a]);
+    for (int a = s_.ndim; a < 3; ++a) ptab_[a] = nullptr;
+    for (int a = 0; a < s_.ndim; ++a) twiddle(s_.n[a]);
+    partials_ = alloc<double>((size_t)kMaxBlocks * 16);
+    results_ = alloc<double>(64);
+    cuda_check(cudaMallocHost(&host_res_, 64 * sizeof(double)), "cudaMallocHost");
+    cuda_check(cudaMallocHost(&host_psi_, sizeof(double) * 2 * nc_), "cudaMallocHost psi");
+    if (sizeof(R) != 8) stage_ = alloc<double2>(nc_);
+    // spin tables
+    std::memset(&st_, 0, sizeof(st_));
+    for (int i = 0; i < D; ++i)
+      for (int j = 0; j < D; ++j) {
+        const auto v = s_.FyV[(size_t)i * D + j], vt = s_.FyVt[(size_t)i * D + j];
+        st_.V[i * D + j] = mk<R>((R)v.real(), (R)v.imag());
+        st_.Vt[i * D + j] = mk<R>((R)vt.real(), (R)vt.imag());
+      }
+    for (int c = 0; c < D; ++c) {
+      st_.fp[c] = (R)s_.fp[c];
+      st_.m[c] = (R)s_.m[c];
+    }
+    if (s_.tensor) {
+      G_ = alloc<double>(s_.G.size());
+      upload(G_, s_.G.data(), s_.G.size());
+      const int np = (int)s_.pair_a.size();
+      std::vector<int4> pairs(np);
+      for (int q = 0; q < np; ++q) pairs[q] = make_int4(s_.pair_a[q], s_.pair_c1[q], s_.pair_c2[q], 0);
+      pairs_ = alloc<int4>(std::max(np, 1));
+      pcg_ = alloc<double>(std::max(np, 1));
+      gA_ = alloc<double>(std::max((int)s_.gA.size(), 1));
+      upload(pairs_, pairs.data(), np);
+      upload(pcg_, s_.pair_cg.data(), np);
+      upload(gA_, s_.gA.data(), s_.gA.size());
+    }
+    if (s_.ddi) {
+      spin3_ = alloc<R>(3 * N_);
+      phi3_ = alloc<R>(3 * N_);
+      phi_per_ = alloc<R>(3 * N_);
+      for (int kind = 0; kind < (s_.padded ? 2 : 1); ++kind) {
+        DdiGeom g = geom(kind);
+        spec_[kind] = alloc<cplx<R>>((size_t)3 * g.field_stride);
+        twiddle(g.Mx / 2);
+        twiddle(g.Mx);
+        if (s_.ndim >= 2) twiddle(g.My);
+        if (s_.ndim >= 3) twiddle(g.Mz);
+      }
+    }
+    sync();
+  }
+
+  ~Engine() override {
+    cudaStreamSynchronize(stream_);
+    for (void* p : allocs_) cudaFree(p);
+    if (host_res_) cudaFreeHost(host_res_);
+    if (host_psi_) cudaFreeHost(host_psi_);
+    cudaStreamDestroy(stream_);
+  }
+
+  // ---------------- state ----------------
+  void set_psi(const double* host) override {
+    std::memcpy(host_psi_, host, sizeof(double) * 2 * nc_);
+    upload_psi_from_pinned();
+  }
+
+  void get_psi(double* host) override {
+    download_psi_to_pinned();
+    sync();
+    std::memcpy(host, host_psi_, sizeof(double) * 2 * nc_);
+  }
+
+  void set_potential(const double* host) override {
+    if (sizeof(R) == 8) {
+      cuda_check(cudaMemcpyAsync(V_, host, sizeof(double) * N_, cudaMemcpyHostToDevice, stream_), "V upload");
+    } else {
+      double* tmp = reinterpret_cast<double*>(stage_);
+      cuda_check(cudaMemcpyAsync(tmp, host, sizeof(double) * N_, cudaMemcpyHostToDevice, stream_), "V upload");
+      k_real_from_f64<R><<<grid_for(N_), 256, 0, stream_>>>(tmp, V_, N_);
+      launch_check("k_real_from_f64");
+    }
+    sync();
+  }
+
+  // ---------------- operators ----------------
+  void half_potential(double dt_half, bool imaginary_time) override {
+    const double tau_d = dt_half / 2;
+    const double tau_s = dt_half / 2;
+    const bool sm = !s_.tensor && std::fabs(s_.c1) >= 1e-30 && s_.D > 1;
+    PotArgs<R> a = pot_args(tau_d, imaginary_time);
+    a.tau_s = (R)tau_s;
+    a.tau_ddi = (R)dt_half;
+    if (s_.tensor) {
+      TensorArgs<R> ta = tensor_args(tau_d, tau_s, imaginary_time);
+      ta.pre_diag = 1;
+      ta.post_diag = s_.ddi ? 0 : 1;
+      ta.n_apply = s_.ddi ? 1 : 2;
+      launch_tensor(ta);
+      if (s_.ddi) {
+        SBEC_SWITCH_D(s_.D, launch_spin_density_d, spin3_);
+        ddi_conv(s_.padded ? 1 : 0, spin3_, phi3_);
+        PotArgs<R> b = a;
+        b.pre_diag = 0;
+        b.rot_a = 0;
+        b.rot_b = 0;
+        b.post_diag = 0;
+        b.ddi_rot = 1;
+        b.phi = phi3_;
+        launch_potential(b);
+        ta.pre_diag = 0;
+        ta.post_diag = 1;
+        ta.n_apply = 1;
+        launch_tensor(ta);
+      }
+      return;
+    }
+    if (!s_.ddi) {
+      a.pre_diag = 1;
+      a.rot_a = sm;
+      a.rot_b = sm;
+      a.post_diag = 1;
+      launch_potential(a);
+      return;
+    }
+    PotArgs<R> first = a;
+    first.pre_diag = 1;
+    first.rot_a = sm;
+    first.spin_out = spin3_;
+    launch_potential(first);
+    ddi_conv(s_.padded ? 1 : 0, spin3_, phi3_);
+    PotArgs<R> second = a;
+    second.ddi_rot = 1;
+    second.phi = phi3_;
+    second.rot_b = sm;
+    second.post_diag = 1;
+    launch_potential(second);
+  }
+
+  void kinetic(double dt_k, bool imaginary_time) override {
+    update_phase(dt_k, imaginary_time);
+    fft_full(psi_[kPsi], /*kinetic=*/true);
+  }
+
+  void normalize() override {
+    comp_norms_async(psi_[kPsi]);
+    k_normalize_apply<R><<<grid_for(nc_), 256, 0, stream_>>>(psi_[kPsi], N_, s_.D, results_ + 1, s_.dV);
+    launch_check("k_normalize_apply");
+  }
+
+  void scale_components(const double* w) override {
+    std::memcpy(host_res_, w, sizeof(double) * s_.D);
+    cuda_check(cudaMemcpyAsync(results_ + 32, host_res_, sizeof(double) * s_.D, cudaMemcpyHostToDevice, stream_),
+               "weights");
+    k_scale_comp<R><<<grid_for(nc_), 256, 0, stream_>>>(psi_[kPsi], N_, s_.D, results_ + 32);
+    launch_check("k_scale_comp");
+    sync();
+  }
+
+  void copy_slot(int dst, int src) override {
+    cuda_check(cudaMemcpyAsync(slot(dst), slot(src), sizeof(cplx<R>) * nc_, cudaMemcpyDeviceToDevice, stream_),
+               "slot copy");
+  }
+
+  // ---------------- reductions ----------------
+  void comp_norms(double* sums, double* nan_count) override {
+    comp_norms_async(psi_[kPsi]);
+    fetch(s_.D + 2);
+    for (int c = 0; c < s_.D; ++c) sums[c] = host_res_[1 + c];
+    if (nan_count) *nan_count = host_res_[1 + s_.D];
+  }
+
+  sbec_energy_terms energy_terms() override {
+    sbec_energy_terms e{};
+    const double dV = s_.dV;
+    // kinetic: forward FFT of a copy, sum k^2 |psi_hat|^2 dV / N (src/energy.jl:56-65)
+    cplx<R>* scr = slot_scratch();
+    cuda_check(cudaMemcpyAsync(scr, psi_[kPsi], sizeof(cplx<R>) * nc_, cudaMemcpyDeviceToDevice, stream_), "copy");
+    fft_full(scr, false);
+    {
+      PhaseTableArgs g = phase_geom(0.0, false);
+      const int nb = red_blocks(nc_);
+      k_kinetic_sum<R><<<nb, kRedThreads, 0, stream_>>>(scr, N_, s_.D, g, partials_);
+      launch_check("k_kinetic_sum");
+      finish<1>(nb, false, 0);
+    }
+    comp_norms_async(psi_[kPsi]);  // -> results_[1 .. D+1]
+    {
+      const int nb = red_blocks(N_);
+      SBEC_SWITCH_D(s_.D, launch_energy_local_d, nb);
+      finish<4>(nb, false, 20);
+    }
+    if (s_.tensor) {
+      const int nb = red_blocks(N_);
+      SBEC_SWITCH_D(s_.D, launch_tensor_energy_d, nb);
+      finish<1>(nb, false, 30);
+    }
+    if (s_.ddi) {
+      SBEC_SWITCH_D(s_.D, launch_spin_density_d, spin3_);
+      ddi_conv(0, spin3_, phi_per_);
+      const int nb = red_blocks(N_);
+      k_dot3<R><<<nb, kRedThreads, 0, stream_>>>(phi_per_, spin3_, N_, partials_);
+      launch_check("k_dot3");
+      finish<1>(nb, false, 31);
+    }
+    fetch(32);
+    const double N = (double)N_;
+    e.kinetic = 0.5 * (host_res_[0] * dV / N);
+    e.trap = host_res_[20] * dV;
+    double ez = 0.0;
+    for (int c = 0; c < s_.D; ++c) {
+      const double mc = (double)(s_.F - c);
+      const double Ec = -zeeman_p * mc + zeeman_q * mc * mc;
+      ez += Ec * host_res_[1 + c] * dV;
+    }
+    e.zeeman = ez;
+    if (!s_.tensor) {
+      e.c0 = 0.5 * s_.c0 * host_res_[21] * dV;
+      e.c1 = 0.5 * s_.c1 * host_res_[22] * dV;
+    }
+    if (s_.ddi) e.ddi = 0.5 * host_res_[31] * dV;
+    if (s_.c_lhy != 0.0) e.lhy = (2.0 / 5.0) * s_.c_lhy * host_res_[23] * dV;
+    if (s_.tensor) e.tensor = host_res_[30] * dV;
+    return e;
+  }
+
+  double l2_change(int a, int b) override {
+    const int nb = red_blocks(nc_);
+    k_l2_change<R><<<nb, kRedThreads, 0, stream_>>>(slot(a), slot(b), nc_, partials_);
+    launch_check("k_l2_change");
+    finish<2>(nb, false, 0);
+    fetch(2);
+    return host_res_[0] / std::max(host_res_[1], 1e-300);
+  }
+
+  void max_abs(int a, int b, double* max_a, double* max_diff) override {
+    const int nb = red_blocks(nc_);
+    k_max_abs<R><<<nb, kRedThreads, 0, stream_>>>(slot(a), b >= 0 ? slot(b) : nullptr, nc_, partials_);
+    launch_check("k_max_abs");
+    finish<2>(nb, true, 0);
+    fetch(2);
+    *max_a = host_res_[0];
+    *max_diff = host_res_[1];
+  }
+
+  double ddi_phi_max() override {
+    if (!s_.ddi) return 0.0;
+    const int nb = red_blocks(3 * N_);
+    k_max_abs_real<R><<<nb, kRedThreads, 0, stream_>>>(s_.padded ? phi_per_ : phi3_, 3 * N_, partials_);
+    launch_check("k_max_abs_real");
+    finish<1>(nb, true, 0);
+    fetch(1);
+    return host_res_[0];
+  }
+
+  void spin_density(double* host3N) override {
+    R* out = s_.ddi ? spin3_ : alloc_tmp_real3();
+    SBEC_SWITCH_D(s_.D, launch_spin_density_d, out);
+    download_real3(out, host3N);
+  }
+
+  void ddi_potential(bool padded, double* host3N) override {
+    if (!s_.ddi) fail(SBEC_ERR_INVALID, "DDI is not enabled on this workspace");
+    if (padded && !s_.padded) fail(SBEC_ERR_INVALID, "zero-padded DDI is not enabled on this workspace");
+    SBEC_SWITCH_D(s_.D, launch_spin_density_d, spin3_);
+    ddi_conv(padded ? 1 : 0, spin3_, phi_per_);
+    download_real3(phi_per_, host3N);
+  }
+
+  void sync() override { cuda_check(cudaStreamSynchronize(stream_), "stream sync"); }
+
+ private:
+  static constexpr int kMaxBlocks = 2048;
+
+  template <typename T>
+  T* alloc(size_t n) {
+    void* p = nullptr;
+    const cudaError_t e = cudaMalloc(&p, sizeof(T) * std::max<size_t>(n, 1));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      fail(SBEC_ERR_OOM, std::string("device allocation failed: ") + cudaGetErrorString(e));
+    }
+    allocs_.push_back(p);
+    return static_cast<T*>(p);
+  }
+
+  template <typename T>
+  void upload(T* dst, const T* src, size_t n) {
+    if (n == 0) return;
+    cuda_check(cudaMemcpy(dst, src, sizeof(T) * n, cudaMemcpyHostToDevice), "upload");
+  }
+
+  void launch_check(const char* what) { cuda_check(cudaGetLastError(), what); }
+
+  int grid_for(int64_t n) const {
+    const int64_t b = (n + 255) / 256;
+    return (int)std::min<int64_t>(std::max<int64_t>(b, 1), 152 * 16);
+  }
+  int red_blocks(int64_t n) const {
+    const int64_t b = (n + kRedThreads - 1) / kRedThreads;
+    return (int)std::min<int64_t>(std::max<int64_t>(b, 1), kMaxBlocks);
+  }
+
+  template <int K>
+  void finish(int nb, bool is_max, int out_off) {
+    k_reduce_finish<K><<<1, 32, 0, stream_>>>(partials_, nb, is_max ? 1 : 0, results_ + out_off);
+    launch_check("k_reduce_finish");
+  }
+
+  void fetch(int n) {
+    cuda_check(cudaMemcpyAsync(host_res_, results_, sizeof(double) * n, cudaMemcpyDeviceToHost, stream_), "fetch");
+    sync();
+  }
+
+  cplx<R>* slot(int i) {
+    if (i < 0 || i >= kNumSlots) fail(SBEC_ERR_INVALID, "bad slot");
+    if (!psi_[i]) psi_[i] = alloc<cplx<R>>(nc_);
+    return psi_[i];
+  }
+  cplx<R>* slot_scratch() {
+    if (!scratch_) scratch_ = alloc<cplx<R>>(nc_);
+    return scratch_;
+  }
+  R* alloc_tmp_real3() {
+    if (!tmp3_) tmp3_ = alloc<R>(3 * N_);
+    return tmp3_;
+  }
+
+  void upload_psi_from_pinned() {
+    if (sizeof(R) == 8) {
+      cuda_check(cudaMemcpyAsync(psi_[kPsi], host_psi_, sizeof(double) * 2 * nc_, cudaMemcpyHostToDevice, stream_),
+                 "psi upload");
+    } else {
+      cuda_check(cudaMemcpyAsync(stage_, host_psi_, sizeof(double) * 2 * nc_, cudaMemcpyHostToDevice, stream_),
+                 "psi upload");
+      k_from_f64<R><<<grid_for(nc_), 256, 0, stream_>>>(stage_, psi_[kPsi], nc_);
+      launch_check("k_from_f64");
+    }
+  }
+
+  void download_psi_to_pinned() {
+    if (sizeof(R) == 8) {
+      cuda_check(cudaMemcpyAsync(host_psi_, psi_[kPsi], sizeof(double) * 2 * nc_, cudaMemcpyDeviceToHost, stream_),
+                 "psi download");
+    } else {
+      k_to_f64<R><<<grid_for(nc_), 256, 0, stream_>>>(psi_[kPsi], stage_, nc_);
+      launch_check("k_to_f64");
+      cuda_check(cudaMemcpyAsync(host_psi_, stage_, sizeof(double) * 2 * nc_, cudaMemcpyDeviceToHost, stream_),
+                 "psi download");
+    }
+  }
+
+  void download_real3(const R* src, double* host) {
+    double* tmp = alloc_host_tmp(3 * N_);
+    if (sizeof(R) == 8) {
+      cuda_check(cudaMemcpyAsync(tmp, src, sizeof(double) * 3 * N_, cudaMemcpyDeviceToHost, stream_), "download");
+    } else {
+      double* dtmp = reinterpret_cast<double*>(stage_);
+      if (3 * N_ > 2 * nc_) fail(SBEC_ERR_INVALID, "staging buffer too small");
+      k_real_to_f64<R><<<grid_for(3 * N_), 256, 0, stream_>>>(src, dtmp, 3 * N_);
+      launch_check("k_real_to_f64");
+      cuda_check(cudaMemcpyAsync(tmp, dtmp, sizeof(double) * 3 * N_, cudaMemcpyDeviceToHost, stream_), "download");
+    }
+    sync();
+    std::memcpy(host, tmp, sizeof(double) * 3 * N_);
+  }
+
+  double* alloc_host_tmp(int64_t n) {
+    if (host_tmp_n_ < n) {
+      if (host_tmp_) cudaFreeHost(host_tmp_);
+      cuda_check(cudaMallocHost(&host_tmp_, sizeof(double) * n), "cudaMallocHost");
+      host_tmp_n_ = n;
+    }
+    return host_tmp_;
+  }
+
+  // twiddle table W_n^e = exp(-2 pi i e/n), e = 0..n-1 (computed in long double).
+  const cplx<R>* twiddle(int n) {
+    auto it = tw_.find(n);
+    if (it != tw_.end()) return it->second;
+    std::vector<cplx<R>> h(n);
+    for (int e = 0; e < n; ++e) {
+      const long double ang = -2.0L * 3.141592653589793238462643383279502884L * (long double)e / (long double)n;
+      h[e] = mk<R>((R)std::cos(ang), (R)std::sin(ang));
+    }
+    cplx<R>* d = alloc<cplx<R>>(n);
+    upload(d, h.data(), n);
+    tw_[n] = d;
+    return d;
+  }
+
+  PhaseTableArgs phase_geom(double dtv, bool it) const {
+    PhaseTableArgs g{};
+    g.ndim = s_.ndim;
+    for (int a = 0; a < 3; ++a) {
+      g.n[a] = s_.n[a];
+      g.kmult[a] = s_.kmult[a];
+    }
+    g.dt = dtv;
+    g.itp = it ? 1 : 0;
+    g.scale = 1.0 / (double)N_;
+    return g;
+  }
+
+  void update_phase(double dtv, bool it) {
+    if (dtv == phase_dt_ && (it ? 1 : 0) == phase_itp_) return;
+    PhaseTableArgs g = phase_geom(dtv, it);
+    dim3 grid(8, s_.ndim);
+    k_phase_tables<R><<<grid, 256, 0, stream_>>>(ptab_[0], ptab_[1], ptab_[2], g);
+    launch_check("k_phase_tables");
+    phase_dt_ = dtv;
+    phase_itp_ = it ? 1 : 0;
+  }
+
+  PhaseRef<R> phase_ref() const {
+    PhaseRef<R> p{};
+    p.ndim = s_.ndim;
+    for (int a = 0; a < 3; ++a) {
+      p.tab[a] = ptab_[a];
+      p.n[a] = s_.n[a];
+    }
+    return p;
+  }
+
+  // ---- FFT launchers
+  template <int NN>
+  void launch_fft_x(cplx<R>* data, int64_t n_lines, int mode) {
+    constexpr int LPB = x_lines_per_block<R, NN>();
+    constexpr int TPL = NN / FftPlan<NN>::E;
+    const size_t smem = sizeof(cplx<R>) * LPB * NN;
+    auto kern = k_fft_x<R, NN, LPB>;
+    static const bool once = (set_smem(kern, smem), true);
+    (void)once;
+    const int64_t blocks = (n_lines + LPB - 1) / LPB;
+    kern<<<(unsigned)blocks, LPB * TPL, smem, stream_>>>(data, n_lines, mode, phase_ref(), twiddle(NN));
+    launch_check("k_fft_x");
+  }
+
+  template <int NN>
+  void launch_fft_strided(cplx<R>* data, int64_t S, int64_t inner, int64_t outer, int64_t outer_stride, int n_in,
+                          int n_out, int mode) {
+    constexpr int W = strided_width<R, NN>();
+    constexpr int TPL = NN / FftPlan<NN>::E;
+    const size_t smem = sizeof(cplx<R>) * W * NN;
+    auto kern = k_fft_strided<R, NN, W>;
+    static const bool once = (set_smem(kern, smem), true);
+    (void)once;
+    dim3 grid((unsigned)((inner + W - 1) / W), (unsigned)outer);
+    kern<<<grid, W * TPL, smem, stream_>>>(data, S, inner, outer_stride, n_in, n_out, mode, phase_ref(),
+                                           twiddle(NN));
+    launch_check("k_fft_strided");
+  }
+
+  // Full spatial FFT of a D-component buffer: forward only (kinetic=false), or the
+  // kinetic step fwd -> phase -> inv (kinetic=true).
+  void fft_full(cplx<R>* buf, bool kinetic) {
+    const int nd = s_.ndim;
+    const int nx = s_.n[0], ny = s_.n[1], nz = s_.n[2];
+    const int64_t D = s_.D;
+    if (nd == 1) {
+      SBEC_SWITCH_POW2(nx, launch_fft_x, buf, D, kinetic ? 2 : 0);
+      return;
+    }
+    SBEC_SWITCH_POW2(nx, launch_fft_x, buf, (int64_t)ny * nz * D, 0);
+    if (nd == 2) {
+      SBEC_SWITCH_POW2_STRIDED(ny, launch_fft_strided, buf, (int64_t)nx, (int64_t)nx, D, N_, ny, ny, kinetic ? 2 : 0);
+    } else {
+      SBEC_SWITCH_POW2_STRIDED(ny, launch_fft_strided, buf, (int64_t)nx, (int64_t)nx, (int64_t)nz * D,
+                               (int64_t)nx * ny, ny, ny, 0);
+      SBEC_SWITCH_POW2_STRIDED(nz, launch_fft_strided, buf, (int64_t)nx * ny, (int64_t)nx * ny, D, N_, nz, nz,
+                               kinetic ? 2 : 0);
+      if (kinetic)
+        SBEC_SWITCH_POW2_STRIDED(ny, launch_fft_strided, buf, (int64_t)nx, (int64_t)nx, (int64_t)nz * D,
+                                 (int64_t)nx * ny, ny, ny, 1);
+    }
+    if (kinetic) SBEC_SWITCH_POW2(nx, launch_fft_x, buf, (int64_t)ny * nz * D, 1);
+  }
+
+  // ---- DDI
+  DdiGeom geom(int kind) const {
+    DdiGeom g{};
+    g.ndim = s_.ndim;
+    g.nx = s_.n[0];
+    g.ny = s_.ndim >= 2 ? s_.n[1] : 1;
+    g.nz = s_.ndim >= 3 ? s_.n[2] : 1;
+    g.Mx = s_.conv_M[kind][0];
+    g.My = s_.conv_M[kind][1];
+    g.Mz = s_.conv_M[kind][2];
+    g.Hx = g.Mx / 2 + 1;
+    g.field_stride = (int64_t)g.Hx * g.My * g.nz;
+    g.kmx = s_.conv_kmult[kind][0];
+    g.kmy = s_.conv_kmult[kind][1];
+    g.kmz = s_.conv_kmult[kind][2];
+    g.C = s_.c_dd / ((double)g.Mx * g.My * g.Mz);
+    g.secular = s_.secular ? 1 : 0;
+    return g;
+  }
+
+  template <int MH>
+  void launch_ddi_r2c(const R* f3, cplx<R>* spec, const DdiGeom& g, R* phi3) {
+    constexpr int LPB = ddi_x_rows_per_block<R, MH>();
+    constexpr int TPL = MH / FftPlan<MH>::E;
+    const size_t smem = sizeof(cplx<R>) * 3 * LPB * (2 * MH + 1);
+    auto kern = k_ddi_r2c_x<R, MH, LPB>;
+    static const bool once = (set_smem(kern, smem), true);
+    (void)once;
+    const int64_t rows = (int64_t)g.ny * g.nz;
+    kern<<<(unsigned)((rows + LPB - 1) / LPB), 3 * LPB * TPL, smem, stream_>>>(f3, N_, spec, g, phi3, twiddle(MH),
+                                                                               twiddle(2 * MH));
+    launch_check("k_ddi_r2c_x");
+  }
+
+  template <int MH>
+  void launch_ddi_c2r(const cplx<R>* spec, const DdiGeom& g, R* phi3) {
+    constexpr int LPB = ddi_x_rows_per_block<R, MH>();
+    constexpr int TPL = MH / FftPlan<MH>::E;
+    const size_t smem = sizeof(cplx<R>) * 3 * LPB * (2 * MH + 1);
+    auto kern = k_ddi_c2r_x<R, MH, LPB>;
+    static const bool once = (set_smem(kern, smem), true);
+    (void)once;
+    const int64_t rows = (int64_t)g.ny * g.nz;
+    kern<<<(unsigned)((rows + LPB - 1) / LPB), 3 * LPB * TPL, smem, stream_>>>(spec, g, phi3, N_, twiddle(MH),
+                                                                               twiddle(2 * MH));
+    launch_check("k_ddi_c2r_x");
+  }
+
+  template <int M>
+  void launch_ddi_last(cplx<R>* spec, const DdiGeom& g, int64_t S, int64_t inner, int n_in, int n_out) {
+    constexpr int W = ddi_last_width<R, M>();
+    constexpr int TPL = M / FftPlan<M>::E;
+    const size_t smem = sizeof(cplx<R>) * 3 * W * M;
+    auto kern = k_ddi_last<R, M, W>;
+    static const bool once = (set_smem(kern, smem), true);
+    (void)once;
+    kern<<<(unsigned)((inner + W - 1) / W), 3 * W * TPL, smem, stream_>>>(spec, g, S, inner, n_in, n_out,
+                                                                         twiddle(M));
+    launch_check("k_ddi_last");
+  }
+
+  // Φ = C_dd Q * F on convolution grid `kind` (0 periodic, 1 zero padded).
+  void ddi_conv(int kind, const R* f3, R* phi3) {
+    const DdiGeom g = geom(kind);
+    cplx<R>* spec = spec_[kind];
+    if (!spec) fail(SBEC_ERR_INVALID, "DDI convolution buffers missing");
+    const int MH = g.Mx / 2;
+    if (MH < 2) fail(SBEC_ERR_UNSUPPORTED, "DDI needs at least 4 points along x");
+    SBEC_SWITCH_POW2(MH, launch_ddi_r2c, f3, spec, g, phi3);
+    if (g.ndim == 1) return;
+    if (g.ndim == 2) {
+      SBEC_SWITCH_POW2_STRIDED(g.My, launch_ddi_last, spec, g, (int64_t)g.Hx, (int64_t)g.Hx, g.ny, g.ny);
+    } else {
+      const int64_t plane = (int64_t)g.Hx * g.My;
+      SBEC_SWITCH_POW2_STRIDED(g.My, launch_fft_strided, spec, (int64_t)g.Hx, (int64_t)g.Hx, (int64_t)3 * g.nz,
+                               plane, g.ny, g.My, 0);
+      SBEC_SWITCH_POW2_STRIDED(g.Mz, launch_ddi_last, spec, g, plane, plane, g.nz, g.nz);
+      SBEC_SWITCH_POW2_STRIDED(g.My, launch_fft_strided, spec, (int64_t)g.Hx, (int64_t)g.Hx, (int64_t)3 * g.nz,
+                               plane, g.My, g.ny, 1);
+    }
+    SBEC_SWITCH_POW2(MH, launch_ddi_c2r, spec, g, phi3);
+  }
+
+  // ---- pointwise launchers
+  PotArgs<R> pot_args(double tau_d, bool it) const {
+    PotArgs<R> a{};
+    a.psi = psi_[kPsi];
+    a.N = N_;
+    a.V = V_;
+    a.itp = it ? 1 : 0;
+    a.tau_d = (R)tau_d;
+    a.c0 = (R)s_.c0;
+    a.c1 = (R)s_.c1;
+    a.c_lhy = (R)s_.c_lhy;
+    zeeman_factors(tau_d, it, a.zee);
+    return a;
+  }
+
+  // Zeeman factors (src/propagators.jl:95-116): cis(-E_c tau) or exp(-(E_c - min E) tau).
+  void zeeman_factors(double tau, bool it, cplx<R>* out) const {
+    const int D = s_.D, F = s_.F;
+    double E[kMaxD];
+    double emin = INFINITY;
+    for (int c = 0; c < D; ++c) {
+      const double m = (double)(F - c);
+      E[c] = -zeeman_p * m + zeeman_q * (m * m);
+      emin = std::min(emin, E[c]);
+    }
+    for (int c = 0; c < D; ++c) {
+      if (it) {
+        out[c] = mk<R>((R)std::exp(-((E[c] - emin) * tau)), (R)0);
+      } else {
+        const double arg = -(E[c] * tau);
+        out[c] = mk<R>((R)std::cos(arg), (R)std::sin(arg));
+      }
+    }
+  }
+
+  TensorArgs<R> tensor_args(double tau_d, double tau_t, bool it) const {
+    TensorArgs<R> a{};
+    a.psi = psi_[kPsi];
+    a.N = N_;
+    a.V = V_;
+    a.G = G_;
+    a.bound_coef = s_.bound_coef;
+    a.itp = it ? 1 : 0;
+    a.tau = (R)tau_t;
+    a.tau_d = (R)tau_d;
+    a.c0 = (R)s_.c0;
+    a.c_lhy = (R)s_.c_lhy;
+    a.eps = sizeof(R) == 8 ? 1e-17 : 1e-8;
+    zeeman_factors(tau_d, it, a.zee);
+    return a;
+  }
+
+  template <int D>
+  void launch_potential_d(const PotArgs<R>& a) {
+    k_potential<R, D><<<(unsigned)((N_ + 255) / 256), 256, 0, stream_>>>(a, st_);
+    launch_check("k_potential");
+  }
+  void launch_potential(const PotArgs<R>& a) { SBEC_SWITCH_D(s_.D, launch_potential_d, a); }
+
+  template <int D>
+  void launch_tensor_d(const TensorArgs<R>& a) {
+    constexpr int T = 64;
+    const size_t smem = sizeof(cplx<R>) * T * (D * (D + 1) / 2);
+    auto kern = k_tensor<R, D>;
+    static const bool once = (set_smem(kern, smem), true);
+    (void)once;
+    kern<<<(unsigned)((N_ + T - 1) / T), T, smem, stream_>>>(a);
+    launch_check("k_tensor");
+  }
+  void launch_tensor(const TensorArgs<R>& a) { SBEC_SWITCH_D(s_.D, launch_tensor_d, a); }
+
+  template <int D>
+  void launch_spin_density_d(R* out) {
+    k_spin_density<R, D><<<(unsigned)((N_ + 255) / 256), 256, 0, stream_>>>(psi_[kPsi], N_, st_, out);
+    launch_check("k_spin_density");
+  }
+
+  template <int D>
+  void launch_energy_local_d(int nb) {
+    k_energy_local<R, D><<<nb, kRedThreads, 0, stream_>>>(psi_[kPsi], N_, V_, st_, partials_);
+    launch_check("k_energy_local");
+  }
+
+  template <int D>
+  void launch_tensor_energy_d(int nb) {
+    k_tensor_energy<R, D><<<nb, kRedThreads, 0, stream_>>>(psi_[kPsi], N_, pairs_, pcg_, (int)s_.pair_a.size(), gA_,
+                                                          (int)s_.gA.size(), partials_);
+    launch_check("k_tensor_energy");
+  }
+
+  template <int D>
+  void launch_comp_norms_d(const cplx<R>* buf, int nb) {
+    k_comp_norms<R, D><<<nb, kRedThreads, 0, stream_>>>(buf, N_, partials_);
+    launch_check("k_comp_norms");
+  }
+
+  // per-component sums into results_[1..D], NaN count into results_[D+1]
+  void comp_norms_async(const cplx<R>* buf) {
+    const int nb = red_blocks(N_);
+    SBEC_SWITCH_D(s_.D, launch_comp_norms_d, buf, nb);
+    switch (s_.D) {
+      case 1: finish<2>(nb, false, 1); break;
+      case 3: finish<4>(nb, false, 1); break;
+      case 5: finish<6>(nb, false, 1); break;
+      case 7: finish<8>(nb, false, 1); break;
+      case 9: finish<10>(nb, false, 1); break;
+      case 11: finish<12>(nb, false, 1); break;
+      case 13: finish<14>(nb, false, 1); break;
+    }
+  }
+
+  int64_t N_ = 0, nc_ = 0;
+  cplx<R>* psi_[kNumSlots] = {nullptr, nullptr, nullptr, nullptr};
+  cplx<R>* scratch_ = nullptr;
+  R* V_ = nullptr;
+  R* tmp3_ = nullptr;
+  cplx<R>* ptab_[3] = {nullptr, nullptr, nullptr};
+  std::map<int, cplx<R>*> tw_;
+  double* partials_ = nullptr;
+  double* results_ = nullptr;
+  double* host_res_ = nullptr;
+  double* host_psi_ = nullptr;
+  double* host_tmp_ = nullptr;
+  int64_t host_tmp_n_ = 0;
+  double2* stage_ = nullptr;
+  SpinTabs<R> st_;
+  double* G_ = nullptr;
+  int4* pairs_ = nullptr;
+  double* pcg_ = nullptr;
+  double* gA_ = nullptr;
+  R* spin3_ = nullptr;
+  R* phi3_ = nullptr;
+  R* phi_per_ = nullptr;
+  cplx<R>* spec_[2] = {nullptr, nullptr};
+  double phase_dt_ = NAN;
+  int phase_itp_ = -1;
+  std::vector<void*> allocs_;
+};
+
+}  // namespace sbec

@@ -1,0 +1,162 @@
+// Shared-memory Stockham FFT for power-of-two line lengths 2..4096.
+//
+// A tile of lines sits in shared memory; element (line l, index i) lives at
+// s[i*SI + l*SL].  Each line is transformed by TPL = N/E threads, E being the
+// largest radix of the line's plan, so every thread holds E values in registers
+// per stage.  A stage of radix RAD reads its inputs at stride N/RAD, applies the
+// Stockham twiddles W_N^{r*(j mod Ns)*N/(Ns*RAD)}, runs a register DFT of size
+// RAD and writes to the autosorted positions (j div Ns)*Ns*RAD + (j mod Ns) + r*Ns.
+// Output is in natural order; forward is unnormalised (FFTW's fft!), the inverse
+// is the unnormalised conjugate transform (normalisation is folded elsewhere).
+#pragma once
+
+#include "sbec_common.cuh"
+
+namespace sbec {
+
+// cos and sin of 2*pi*j/16, j = 0..7 (constants of the unit circle).
+__device__ __forceinline__ double cos16(int j) {
+  constexpr double c[8] = {1.0,
+                           0.92387953251128675613,
+                           0.70710678118654752440,
+                           0.38268343236508977173,
+                           0.0,
+                           -0.38268343236508977173,
+                           -0.70710678118654752440,
+                           -0.92387953251128675613};
+  return c[j];
+}
+__device__ __forceinline__ double sin16(int j) {
+  constexpr double s[8] = {0.0,
+                           0.38268343236508977173,
+                           0.70710678118654752440,
+                           0.92387953251128675613,
+                           1.0,
+                           0.92387953251128675613,
+                           0.70710678118654752440,
+                           0.38268343236508977173};
+  return s[j];
+}
+
+// x * exp(SIGN * 2*pi*i*k/N) for compile-time N <= 16 and (after unrolling) constant k < N/2.
+template <typename R, int N, int SIGN>
+__device__ __forceinline__ cplx<R> twmul(cplx<R> x, int k) {
+  const int j = k * (16 / N);
+  if (j == 0) return x;
+  if (j == 4) return SIGN < 0 ? mul_mi(x) : mul_i(x);
+  if (j == 2) {
+    const R h = (R)0.70710678118654752440;
+    return SIGN < 0 ? mk<R>(h * (x.x + x.y), h * (x.y - x.x)) : mk<R>(h * (x.x - x.y), h * (x.y + x.x));
+  }
+  if (j == 6) {
+    const R h = (R)0.70710678118654752440;
+    return SIGN < 0 ? mk<R>(h * (x.y - x.x), -h * (x.x + x.y)) : mk<R>(-h * (x.x + x.y), h * (x.x - x.y));
+  }
+  const cplx<R> w = mk<R>((R)cos16(j), (R)(SIGN * sin16(j)));
+  return x * w;
+}
+
+// In-register DFT of compile-time size N (1, 2, 4, 8, 16) by radix-2 decimation in time.
+template <typename R, int N, int SIGN>
+__device__ __forceinline__ void dft(cplx<R>* v) {
+  if constexpr (N == 1) {
+    return;
+  } else if constexpr (N == 2) {
+    const cplx<R> a = v[0], b = v[1];
+    v[0] = a + b;
+    v[1] = a - b;
+  } else {
+    cplx<R> e[N / 2], o[N / 2];
+#pragma unroll
+    for (int k = 0; k < N / 2; ++k) {
+      e[k] = v[2 * k];
+      o[k] = v[2 * k + 1];
+    }
+    dft<R, N / 2, SIGN>(e);
+    dft<R, N / 2, SIGN>(o);
+#pragma unroll
+    for (int k = 0; k < N / 2; ++k) {
+      const cplx<R> t = twmul<R, N, SIGN>(o[k], k);
+      v[k] = e[k] + t;
+      v[k + N / 2] = e[k] - t;
+    }
+  }
+}
+
+// One Stockham stage.  tw holds W_N^e = exp(-2*pi*i*e/N), e = 0..N-1 (forward sign).
+template <typename R, int N, int E, int RAD, int SIGN>
+__device__ __forceinline__ void fft_stage(cplx<R>* s, int SI, int SL, int l, int t, int Ns,
+                                          const cplx<R>* __restrict__ tw) {
+  constexpr int TPL = N / E;
+  constexpr int NBT = E / RAD;
+  constexpr int STRIDE = N / RAD;
+  cplx<R> v[E];
+#pragma unroll
+  for (int b = 0; b < NBT; ++b) {
+    const int j = t + b * TPL;
+#pragma unroll
+    for (int r = 0; r < RAD; ++r) v[b * RAD + r] = s[(j + r * STRIDE) * SI + l * SL];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int b = 0; b < NBT; ++b) {
+    const int j = t + b * TPL;
+    const int jm = j & (Ns - 1);
+    if (Ns > 1) {
+      const int step = jm * (N / (Ns * RAD));
+#pragma unroll
+      for (int r = 1; r < RAD; ++r) {
+        cplx<R> w = __ldg(tw + r * step);
+        if (SIGN > 0) w.y = -w.y;
+        v[b * RAD + r] = v[b * RAD + r] * w;
+      }
+    }
+    dft<R, RAD, SIGN>(&v[b * RAD]);
+    const int base = (j - jm) * RAD + jm;
+#pragma unroll
+    for (int r = 0; r < RAD; ++r) s[(base + r * Ns) * SI + l * SL] = v[b * RAD + r];
+  }
+  __syncthreads();
+}
+
+template <typename R, int N, int E, int SIGN, int RAD, int... REST>
+__device__ __forceinline__ void run_stages(cplx<R>* s, int SI, int SL, int l, int t, int Ns,
+                                           const cplx<R>* __restrict__ tw) {
+  fft_stage<R, N, E, RAD, SIGN>(s, SI, SL, l, t, Ns, tw);
+  if constexpr (sizeof...(REST) > 0) run_stages<R, N, E, SIGN, REST...>(s, SI, SL, l, t, Ns * RAD, tw);
+}
+
+// Radix plan per line length: E = largest radix; stages run in the listed order.
+template <int N> struct FftPlan;
+#define SBEC_PLAN(NN, EE, ...)                                                                   \
+  template <> struct FftPlan<NN> {                                                               \
+    static constexpr int E = EE;                                                                 \
+    template <typename R, int SIGN>                                                              \
+    static __device__ __forceinline__ void run(cplx<R>* s, int SI, int SL, int l, int t,        \
+                                               const cplx<R>* __restrict__ tw) {                 \
+      run_stages<R, NN, EE, SIGN, __VA_ARGS__>(s, SI, SL, l, t, 1, tw);                          \
+    }                                                                                            \
+  };
+SBEC_PLAN(2, 2, 2)
+SBEC_PLAN(4, 4, 4)
+SBEC_PLAN(8, 8, 8)
+SBEC_PLAN(16, 16, 16)
+SBEC_PLAN(32, 8, 8, 4)
+SBEC_PLAN(64, 8, 8, 8)
+SBEC_PLAN(128, 16, 16, 8)
+SBEC_PLAN(256, 16, 16, 16)
+SBEC_PLAN(512, 8, 8, 8, 8)
+SBEC_PLAN(1024, 16, 16, 8, 8)
+SBEC_PLAN(2048, 16, 16, 16, 8)
+SBEC_PLAN(4096, 16, 16, 16, 16)
+#undef SBEC_PLAN
+
+// Transform every line of a shared-memory tile (all threads of the block participate).
+// Caller must __syncthreads() after filling the tile; the function ends synchronised.
+template <typename R, int N, int SIGN>
+__device__ __forceinline__ void fft_tile(cplx<R>* s, int SI, int SL, int l, int t,
+                                         const cplx<R>* __restrict__ tw) {
+  FftPlan<N>::template run<R, SIGN>(s, SI, SL, l, t, tw);
+}
+
+}  // namespace sbec

@@ -1,0 +1,993 @@
+// Device kernels of the split-step engine, templated on the working real type R
+// (double: the plain FP64 form; float: the FP32-bulk form).  Reductions always
+// accumulate in double.
+#pragma once
+
+#include "sbec_common.cuh"
+#include "sbec_fft.cuh"
+
+namespace sbec {
+
+// ---------------------------------------------------------------------------
+// Kinetic phase tables
+// ---------------------------------------------------------------------------
+// exp(-i k^2 dt/2) (or exp(-k^2 dt/2) in imaginary time) factorises over axes:
+// tab_a[m] = exp(-i k_a(m)^2 dt/2) with k_a(m) = fftfreq index * kmult_a
+// (src/propagators.jl:1-7, 137-145).  The 1/prod(n) normalisation of the inverse
+// FFT (FFTW ifft!) is folded into the axis-0 table.
+struct PhaseTableArgs {
+  int n[3];
+  double kmult[3];
+  double dt;
+  double scale;
+  int ndim;
+  int itp;
+};
+
+template <typename R>
+__global__ void k_phase_tables(cplx<R>* tab0, cplx<R>* tab1, cplx<R>* tab2, PhaseTableArgs a) {
+  const int axis = blockIdx.y;
+  if (axis >= a.ndim) return;
+  cplx<R>* tab = axis == 0 ? tab0 : (axis == 1 ? tab1 : tab2);
+  const int n = a.n[axis];
+  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x) {
+    const int idx = m < (n + 1) / 2 ? m : m - n;
+    const double k = (double)idx * a.kmult[axis];
+    const double arg = -0.5 * (k * k) * a.dt;
+    double re, im;
+    if (a.itp) {
+      re = exp(arg);
+      im = 0.0;
+    } else {
+      sincos(arg, &im, &re);
+    }
+    if (axis == 0) {
+      re *= a.scale;
+      im *= a.scale;
+    }
+    tab[m] = mk<R>((R)re, (R)im);
+  }
+}
+
+template <typename R>
+struct PhaseRef {
+  const cplx<R>* tab[3];
+  int n[3];
+  int ndim;
+};
+
+// ---------------------------------------------------------------------------
+// FFT along x (contiguous lines).  mode 0: forward, 1: inverse,
+// 2: forward, x phase (1-D kinetic step), inverse.
+// ---------------------------------------------------------------------------
+template <typename R, int N, int LPB>
+__global__ void __launch_bounds__(LPB * (N / FftPlan<N>::E))
+k_fft_x(cplx<R>* __restrict__ data, int64_t n_lines, int mode, PhaseRef<R> ph,
+        const cplx<R>* __restrict__ tw) {
+  constexpr int TPL = N / FftPlan<N>::E;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);
+  const int tid = threadIdx.x;
+  const int64_t line0 = (int64_t)blockIdx.x * LPB;
+  const int nl = (int)min((int64_t)LPB, n_lines - line0);
+  cplx<R>* g = data + line0 * N;
+  for (int f = tid; f < LPB * N; f += blockDim.x) s[f] = (f < nl * N) ? g[f] : mk<R>(0, 0);
+  __syncthreads();
+  const int t = tid % TPL, l = tid / TPL;
+  if (mode == 1) {
+    fft_tile<R, N, +1>(s, 1, N, l, t, tw);
+  } else {
+    fft_tile<R, N, -1>(s, 1, N, l, t, tw);
+    if (mode == 2) {
+      for (int f = tid; f < LPB * N; f += blockDim.x) s[f] = s[f] * __ldg(ph.tab[0] + (f % N));
+      __syncthreads();
+      fft_tile<R, N, +1>(s, 1, N, l, t, tw);
+    }
+  }
+  for (int f = tid; f < nl * N; f += blockDim.x) g[f] = s[f];
+}
+
+// ---------------------------------------------------------------------------
+// FFT along a strided axis.  Line (o, w) starts at o*outer_stride + i0 + w and
+// has elements at stride S.  Loads only i < n_in (zero beyond), stores only
+// i < n_out (pruned transforms of the zero-padded DDI grid).
+// mode 0 forward, 1 inverse, 2 forward, x phase, inverse (last axis of the
+// kinetic step; the line's lower-axis coordinates come from i0 + w).
+// ---------------------------------------------------------------------------
+template <typename R, int N, int W>
+__global__ void __launch_bounds__(W * (N / FftPlan<N>::E))
+k_fft_strided(cplx<R>* __restrict__ data, int64_t S, int64_t inner, int64_t outer_stride, int n_in,
+              int n_out, int mode, PhaseRef<R> ph, const cplx<R>* __restrict__ tw) {
+  constexpr int TPL = N / FftPlan<N>::E;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);
+  __shared__ cplx<R> inner_ph[W];
+  const int tid = threadIdx.x;
+  const int64_t i0 = (int64_t)blockIdx.x * W;
+  const int nw = (int)min((int64_t)W, inner - i0);
+  cplx<R>* g = data + (int64_t)blockIdx.y * outer_stride + i0;
+  for (int f = tid; f < W * N; f += blockDim.x) {
+    const int i = f / W, w = f % W;
+    s[f] = (i < n_in && w < nw) ? g[(int64_t)i * S + w] : mk<R>(0, 0);
+  }
+  if (mode == 2 && tid < W) {
+    // lower-axis factors of the kinetic phase for this line
+    int64_t pos = i0 + tid;
+    cplx<R> f = mk<R>(1, 0);
+    for (int a = 0; a < ph.ndim - 1; ++a) {
+      const int ia = (int)(pos % ph.n[a]);
+      pos /= ph.n[a];
+      f = f * __ldg(ph.tab[a] + ia);
+    }
+    inner_ph[tid] = f;
+  }
+  __syncthreads();
+  const int w = tid % W, t = tid / W;
+  if (mode == 1) {
+    fft_tile<R, N, +1>(s, W, 1, w, t, tw);
+  } else {
+    fft_tile<R, N, -1>(s, W, 1, w, t, tw);
+    if (mode == 2) {
+      const cplx<R>* last = ph.tab[ph.ndim - 1];
+      for (int f = tid; f < W * N; f += blockDim.x) {
+        const int i = f / W, ww = f % W;
+        s[f] = s[f] * (inner_ph[ww] * __ldg(last + i));
+      }
+      __syncthreads();
+      fft_tile<R, N, +1>(s, W, 1, w, t, tw);
+    }
+  }
+  for (int f = tid; f < W * N; f += blockDim.x) {
+    const int i = f / W, ww = f % W;
+    if (i < n_out && ww < nw) g[(int64_t)i * S + ww] = s[f];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Dipolar convolution (src/ddi.jl:108-136, src/ddi_padded.jl:55-85).
+// Real spin-density fields live on the simulation grid (nx, ny, nz); the
+// convolution grid has (Mx, My, Mz) = n (periodic) or 2n (zero padded).  The
+// half spectrum (Mx/2+1, My, nz) of each of the 3 fields is stored with the
+// z-extent pruned to nz: z >= nz is zero before the z transform and never read
+// after it.  Φ̂ = C' (k (k·F̂)/k² - F̂/3), Q(0) = 0, computed on the fly from k
+// (src/ddi.jl:7-40); the secular variant keeps only the zz part.
+// ---------------------------------------------------------------------------
+struct DdiGeom {
+  int nx, ny, nz;      // simulation grid (active corner)
+  int Mx, My, Mz;      // convolution grid
+  int Hx;              // Mx/2 + 1
+  int64_t field_stride;  // complex elements per field in the spectrum buffer (Hx*My*nz)
+  double kmx, kmy, kmz;  // k multipliers of the convolution grid
+  double C;            // C_dd / (Mx*My*Mz): contraction scale incl. inverse normalisation
+  int secular;
+  int ndim;
+};
+
+template <typename R>
+__device__ __forceinline__ void ddi_contract(cplx<R>& fx, cplx<R>& fy, cplx<R>& fz, double kx, double ky,
+                                             double kz, const DdiGeom& g) {
+  const double k2 = kx * kx + ky * ky + kz * kz;
+  if (k2 == 0.0) {
+    fx = fy = fz = mk<R>(0, 0);
+    return;
+  }
+  const double inv = 1.0 / k2;
+  if (g.secular) {
+    const R qzz = (R)(kz * kz * inv - 1.0 / 3.0);
+    const R qxx = -qzz / (R)2;
+    const R C = (R)g.C;
+    fx = (C * qxx) * fx;
+    fy = (C * qxx) * fy;
+    fz = (C * qzz) * fz;
+    return;
+  }
+  const R qxx = (R)(kx * kx * inv - 1.0 / 3.0), qyy = (R)(ky * ky * inv - 1.0 / 3.0),
+          qzz = (R)(kz * kz * inv - 1.0 / 3.0);
+  const R qxy = (R)(kx * ky * inv), qxz = (R)(kx * kz * inv), qyz = (R)(ky * kz * inv);
+  const R C = (R)g.C;
+  const cplx<R> px = C * (qxx * fx + qxy * fy + qxz * fz);
+  const cplx<R> py = C * (qxy * fx + qyy * fy + qyz * fz);
+  const cplx<R> pz = C * (qxz * fx + qyz * fy + qzz * fz);
+  fx = px;
+  fy = py;
+  fz = pz;
+}
+
+__device__ __forceinline__ int freq_index(int m, int M) { return m < (M + 1) / 2 ? m : m - M; }
+
+// R2C along x of the 3 real fields, via a complex FFT of length MH = Mx/2 on
+// z[j] = f[2j] + i f[2j+1] followed by the split X[k] = E_k + W_Mx^k O_k.
+// Rows (y < ny, z < nz) only; output row (y, z) at spectrum row y + My*z.
+// tw_half: W_MH table; tw_full: W_Mx table.  For 1-D (ndim == 1) the kernel
+// also contracts and returns to real space (the x axis is the last axis).
+template <typename R, int MH, int LPB>
+__global__ void __launch_bounds__(3 * LPB * (MH / FftPlan<MH>::E))
+k_ddi_r2c_x(const R* __restrict__ f3, int64_t field_n, cplx<R>* __restrict__ spec, DdiGeom g,
+            R* __restrict__ phi3, const cplx<R>* __restrict__ tw_half,
+            const cplx<R>* __restrict__ tw_full) {
+  constexpr int TPL = MH / FftPlan<MH>::E;
+  constexpr int NL = 3 * LPB;  // lines in the tile: field-major
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);   // NL * MH
+  cplx<R>* xs = s + NL * MH;                            // NL * (MH + 1) split output
+  const int tid = threadIdx.x;
+  const int64_t n_rows = (int64_t)g.ny * g.nz;
+  const int64_t row0 = (int64_t)blockIdx.x * LPB;
+  const int nr = (int)min((int64_t)LPB, n_rows - row0);
+  for (int f = tid; f < NL * MH; f += blockDim.x) {
+    const int line = f / MH, j = f % MH;
+    const int fld = line / LPB, r = line % LPB;
+    cplx<R> v = mk<R>(0, 0);
+    if (r < nr) {
+      const R* src = f3 + fld * field_n + (row0 + r) * g.nx;
+      const int x0 = 2 * j, x1 = 2 * j + 1;
+      v.x = x0 < g.nx ? src[x0] : (R)0;
+      v.y = x1 < g.nx ? src[x1] : (R)0;
+    }
+    s[f] = v;
+  }
+  __syncthreads();
+  const int t = tid % TPL, l = tid / TPL;
+  fft_tile<R, MH, -1>(s, 1, MH, l, t, tw_half);
+  // split into the half spectrum X[0..MH]
+  for (int f = tid; f < NL * (MH + 1); f += blockDim.x) {
+    const int line = f / (MH + 1), k = f % (MH + 1);
+    const cplx<R> Zk = s[line * MH + (k % MH)];
+    const cplx<R> Zc = conj(s[line * MH + ((MH - k) % MH)]);
+    const cplx<R> E = (R)0.5 * (Zk + Zc);
+    const cplx<R> O = (R)0.5 * mul_mi(Zk - Zc);
+    const cplx<R> w = __ldg(tw_full + (k % (2 * MH)));
+    xs[f] = (k == MH) ? (E - O) : E + w * O;
+  }
+  __syncthreads();
+  if (g.ndim > 1) {
+    for (int f = tid; f < NL * (MH + 1); f += blockDim.x) {
+      const int line = f / (MH + 1), k = f % (MH + 1);
+      const int fld = line / LPB, r = line % LPB;
+      if (r >= nr) continue;
+      const int64_t row = row0 + r;
+      const int64_t y = row % g.ny, z = row / g.ny;
+      spec[fld * g.field_stride + (y + (int64_t)g.My * z) * g.Hx + k] = xs[f];
+    }
+    return;
+  }
+  // 1-D: contract at kx and go back to real space in the same tile.
+  for (int f = tid; f < LPB * (MH + 1); f += blockDim.x) {
+    const int r = f / (MH + 1), k = f % (MH + 1);
+    cplx<R>& ax = xs[(0 * LPB + r) * (MH + 1) + k];
+    cplx<R>& ay = xs[(1 * LPB + r) * (MH + 1) + k];
+    cplx<R>& az = xs[(2 * LPB + r) * (MH + 1) + k];
+    ddi_contract<R>(ax, ay, az, (double)k * g.kmx, 0.0, 0.0, g);
+  }
+  __syncthreads();
+  // C2R: Z_k = (X_k + conj X_{MH-k}) + i (X_k - conj X_{MH-k}) W_Mx^{-k}, k < MH
+  for (int f = tid; f < NL * MH; f += blockDim.x) {
+    const int line = f / MH, k = f % MH;
+    const cplx<R> Xk = xs[line * (MH + 1) + k];
+    const cplx<R> Xc = conj(xs[line * (MH + 1) + (MH - k)]);
+    const cplx<R> w = conj(__ldg(tw_full + k));
+    s[f] = (Xk + Xc) + mul_i((Xk - Xc) * w);
+  }
+  __syncthreads();
+  fft_tile<R, MH, +1>(s, 1, MH, l, t, tw_half);
+  for (int f = tid; f < NL * MH; f += blockDim.x) {
+    const int line = f / MH, j = f % MH;
+    const int fld = line / LPB, r = line % LPB;
+    if (r >= nr) continue;
+    R* dst = phi3 + fld * field_n + (row0 + r) * g.nx;
+    const int x0 = 2 * j, x1 = 2 * j + 1;
+    if (x0 < g.nx) dst[x0] = s[f].x;
+    if (x1 < g.nx) dst[x1] = s[f].y;
+  }
+}
+
+// C2R along x of the 3 fields (rows y < ny, z < nz), keeping x < nx.
+template <typename R, int MH, int LPB>
+__global__ void __launch_bounds__(3 * LPB * (MH / FftPlan<MH>::E))
+k_ddi_c2r_x(const cplx<R>* __restrict__ spec, DdiGeom g, R* __restrict__ phi3, int64_t field_n,
+            const cplx<R>* __restrict__ tw_half, const cplx<R>* __restrict__ tw_full) {
+  constexpr int TPL = MH / FftPlan<MH>::E;
+  constexpr int NL = 3 * LPB;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);
+  cplx<R>* xs = s + NL * MH;
+  const int tid = threadIdx.x;
+  const int64_t n_rows = (int64_t)g.ny * g.nz;
+  const int64_t row0 = (int64_t)blockIdx.x * LPB;
+  const int nr = (int)min((int64_t)LPB, n_rows - row0);
+  for (int f = tid; f < NL * (MH + 1); f += blockDim.x) {
+    const int line = f / (MH + 1), k = f % (MH + 1);
+    const int fld = line / LPB, r = line % LPB;
+    cplx<R> v = mk<R>(0, 0);
+    if (r < nr) {
+      const int64_t row = row0 + r;
+      const int64_t y = row % g.ny, z = row / g.ny;
+      v = spec[fld * g.field_stride + (y + (int64_t)g.My * z) * g.Hx + k];
+    }
+    xs[f] = v;
+  }
+  __syncthreads();
+  for (int f = tid; f < NL * MH; f += blockDim.x) {
+    const int line = f / MH, k = f % MH;
+    const cplx<R> Xk = xs[line * (MH + 1) + k];
+    const cplx<R> Xc = conj(xs[line * (MH + 1) + (MH - k)]);
+    const cplx<R> w = conj(__ldg(tw_full + k));
+    s[f] = (Xk + Xc) + mul_i((Xk - Xc) * w);
+  }
+  __syncthreads();
+  const int t = tid % TPL, l = tid / TPL;
+  fft_tile<R, MH, +1>(s, 1, MH, l, t, tw_half);
+  for (int f = tid; f < NL * MH; f += blockDim.x) {
+    const int line = f / MH, j = f % MH;
+    const int fld = line / LPB, r = line % LPB;
+    if (r >= nr) continue;
+    R* dst = phi3 + fld * field_n + (row0 + r) * g.nx;
+    const int x0 = 2 * j, x1 = 2 * j + 1;
+    if (x0 < g.nx) dst[x0] = s[f].x;
+    if (x1 < g.nx) dst[x1] = s[f].y;
+  }
+}
+
+// Last axis of the DDI convolution (y in 2-D, z in 3-D): forward transform of
+// the 3 fields' lines (first n_in entries, zero beyond), contraction, inverse
+// transform, store of the first n_out entries.  Lines: inner index = position
+// in the lower axes of the spectrum (kx [, ky]), stride S between elements.
+template <typename R, int M, int W>
+__global__ void __launch_bounds__(3 * W * (M / FftPlan<M>::E))
+k_ddi_last(cplx<R>* __restrict__ spec, DdiGeom g, int64_t S, int64_t inner, int n_in, int n_out,
+           const cplx<R>* __restrict__ tw) {
+  constexpr int TPL = M / FftPlan<M>::E;
+  constexpr int NL = 3 * W;   // line index = fld*W + w
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);   // element (line, i) at s[i*NL + line]
+  const int tid = threadIdx.x;
+  const int64_t i0 = (int64_t)blockIdx.x * W;
+  const int nw = (int)min((int64_t)W, inner - i0);
+  for (int f = tid; f < NL * M; f += blockDim.x) {
+    const int i = f / NL, line = f % NL;
+    const int fld = line / W, w = line % W;
+    s[f] = (i < n_in && w < nw) ? spec[fld * g.field_stride + i0 + w + (int64_t)i * S] : mk<R>(0, 0);
+  }
+  __syncthreads();
+  const int line = tid % NL, t = tid / NL;
+  fft_tile<R, M, -1>(s, NL, 1, line, t, tw);
+  for (int f = tid; f < W * M; f += blockDim.x) {
+    const int i = f / W, w = f % W;
+    const int64_t pos = i0 + w;
+    double kx, ky, kz;
+    if (g.ndim == 2) {
+      kx = (double)pos * g.kmx;
+      ky = (double)freq_index(i, M) * g.kmy;
+      kz = 0.0;
+    } else {
+      kx = (double)(pos % g.Hx) * g.kmx;
+      ky = (double)freq_index((int)(pos / g.Hx), g.My) * g.kmy;
+      kz = (double)freq_index(i, M) * g.kmz;
+    }
+    cplx<R>& ax = s[i * NL + 0 * W + w];
+    cplx<R>& ay = s[i * NL + 1 * W + w];
+    cplx<R>& az = s[i * NL + 2 * W + w];
+    ddi_contract<R>(ax, ay, az, kx, ky, kz, g);
+  }
+  __syncthreads();
+  fft_tile<R, M, +1>(s, NL, 1, line, t, tw);
+  for (int f = tid; f < NL * M; f += blockDim.x) {
+    const int i = f / NL, ln = f % NL;
+    const int fld = ln / W, w = ln % W;
+    if (i < n_out && w < nw) spec[fld * g.field_stride + i0 + w + (int64_t)i * S] = s[f];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Pointwise potential stage (src/split_step.jl:48-133 minus the FFT work):
+//   [diag(tau_d)] [rot_a: spin mixing(tau_s)] [DDI rotation(tau_ddi)]
+//   [rot_b: spin mixing(tau_s)] [diag(tau_d)] [spin density out]
+// ---------------------------------------------------------------------------
+template <typename R>
+struct SpinTabs {
+  cplx<R> V[kMaxD * kMaxD];    // Fy eigenvectors (columns), ascending eigenvalues
+  cplx<R> Vt[kMaxD * kMaxD];   // adjoint
+  R fp[kMaxD];                 // f+(m_c) = sqrt(F(F+1) - m_c(m_c+1)), c >= 1
+  R m[kMaxD];                  // m_c = F - c
+};
+
+template <typename R>
+struct PotArgs {
+  cplx<R>* psi;
+  int64_t N;
+  const R* V;
+  const R* phi;                // DDI potential fields (3*N) or null
+  R* spin_out;                 // spin density output (3*N) or null
+  int pre_diag, rot_a, ddi_rot, rot_b, post_diag;
+  int itp;
+  R tau_d, tau_s, tau_ddi;
+  R c0, c1, c_lhy;
+  cplx<R> zee[kMaxD];          // per-component Zeeman factor for diag(tau_d)
+};
+
+template <typename R, int D>
+__device__ __forceinline__ void diag_point(cplx<R> (&v)[D], R Vp, const PotArgs<R>& a) {
+  R n = 0;
+#pragma unroll
+  for (int c = 0; c < D; ++c) n += abs2(v[c]);
+  const R Vint = a.c0 * n + a.c_lhy * n * sqrt(n);
+  cplx<R> base;
+  if (a.itp) {
+    base = mk<R>(exp(-(Vp + Vint) * a.tau_d), (R)0);
+  } else {
+    base = cis_(-(Vp + Vint) * a.tau_d);
+  }
+#pragma unroll
+  for (int c = 0; c < D; ++c) v[c] = v[c] * (base * a.zee[c]);
+}
+
+// <F> components from the raising operator (src/observables.jl:61-86).
+template <typename R, int D>
+__device__ __forceinline__ void spin_vector(const cplx<R> (&v)[D], const SpinTabs<R>& st, R& fx, R& fy,
+                                            R& fz) {
+  R z = 0, re = 0, im = 0;
+#pragma unroll
+  for (int c = 0; c < D; ++c) z += st.m[c] * abs2(v[c]);
+#pragma unroll
+  for (int c = 1; c < D; ++c) {
+    const cplx<R> p = cmulc(v[c - 1], v[c]);
+    re += st.fp[c] * p.x;
+    im += st.fp[c] * p.y;
+  }
+  fx = re;
+  fy = im;
+  fz = z;
+}
+
+// (n·F) v with n = (nx, ny, nz): tridiagonal in the m basis.
+template <typename R, int D>
+__device__ __forceinline__ void nF_apply(const cplx<R> (&v)[D], R nx, R ny, R nz, const SpinTabs<R>& st,
+                                         cplx<R> (&out)[D]) {
+  const cplx<R> nm = mk<R>(nx * (R)0.5, -ny * (R)0.5);  // (nx - i ny)/2 multiplies F+
+  const cplx<R> np = mk<R>(nx * (R)0.5, ny * (R)0.5);   // (nx + i ny)/2 multiplies F-
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    cplx<R> r = (nz * st.m[c]) * v[c];
+    if (c + 1 < D) r += nm * (st.fp[c + 1] * v[c + 1]);
+    if (c >= 1) r += np * (st.fp[c] * v[c - 1]);
+    out[c] = r;
+  }
+}
+
+// Spin-1 Rodrigues rotation exp(-i theta n·F) (src/spin_mixing.jl:71-98).
+template <typename R, int D>
+__device__ __forceinline__ void rodrigues_point(cplx<R> (&v)[D], R c1, R tau, int itp, const SpinTabs<R>& st) {
+  R fx, fy, fz;
+  spin_vector<R, D>(v, st, fx, fy, fz);
+  const R fm = sqrt(fx * fx + fy * fy + fz * fz);
+  if (fm < (R)1e-30) return;
+  const R inv = (R)1 / fm;
+  cplx<R> w[D], w2[D];
+  nF_apply<R, D>(v, fx * inv, fy * inv, fz * inv, st, w);
+  nF_apply<R, D>(w, fx * inv, fy * inv, fz * inv, st, w2);
+  const R th = c1 * fm * tau;
+  if (itp) {
+    const R sh = sinh(th), chm1 = cosh(th) - (R)1;
+#pragma unroll
+    for (int c = 0; c < D; ++c) v[c] = v[c] - sh * w[c] + chm1 * w2[c];
+  } else {
+    R sn, cs;
+    if constexpr (sizeof(R) == 8) sincos(th, &sn, &cs); else sincosf(th, &sn, &cs);
+    const R cm1 = cs - (R)1;
+#pragma unroll
+    for (int c = 0; c < D; ++c) v[c] = v[c] + mul_mi(sn * w[c]) + cm1 * w2[c];
+  }
+}
+
+// Euler-angle rotation exp(-i dt phi·F) (src/spinor_utils.jl:82-166).
+template <typename R, int D>
+__device__ __forceinline__ void euler_point(cplx<R> (&v)[D], R px, R py, R pz, R dt, int itp,
+                                            const SpinTabs<R>& st) {
+  constexpr int F = (D - 1) / 2;
+  const R pm = sqrt(px * px + py * py + pz * pz);
+  if (pm * fabs(dt) < (R)1e-14) return;
+  R cz = pz / pm;
+  cz = cz < (R)-1 ? (R)-1 : (cz > (R)1 ? (R)1 : cz);
+  const R beta = acos(cz);
+  const R alpha = atan2(py, px);
+  const R theta = pm * dt;
+  const cplx<R> z_neg_alpha = cis_(-alpha);
+  const cplx<R> z_beta = cis_(beta);
+  const cplx<R> rz_phase = cis_((R)F * alpha);
+  const cplx<R> ry_phase = cis_(-(R)F * beta);
+  cplx<R> w[D];
+  cplx<R> phase = rz_phase;
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    v[c] = phase * v[c];
+    phase = phase * z_neg_alpha;
+  }
+  phase = ry_phase;
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    cplx<R> s = mk<R>(0, 0);
+#pragma unroll
+    for (int j = 0; j < D; ++j) s += st.Vt[i * D + j] * v[j];
+    w[i] = phase * s;
+    phase = phase * z_beta;
+  }
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    cplx<R> s = mk<R>(0, 0);
+#pragma unroll
+    for (int j = 0; j < D; ++j) s += st.V[i * D + j] * w[j];
+    v[i] = s;
+  }
+  if (itp) {
+    R dz_r = exp(-(R)F * theta);
+    const R dz_step = exp(theta);
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      v[c] = v[c] * dz_r;
+      dz_r = dz_r * dz_step;
+    }
+  } else {
+    cplx<R> dz_phase = cis_(-(R)F * theta);
+    const cplx<R> z_theta = cis_(theta);
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      v[c] = v[c] * dz_phase;
+      dz_phase = dz_phase * z_theta;
+    }
+  }
+  phase = conj(ry_phase);
+  const cplx<R> z_neg_beta = conj(z_beta);
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    cplx<R> s = mk<R>(0, 0);
+#pragma unroll
+    for (int j = 0; j < D; ++j) s += st.Vt[i * D + j] * v[j];
+    w[i] = phase * s;
+    phase = phase * z_neg_beta;
+  }
+  phase = conj(rz_phase);
+  const cplx<R> z_alpha = conj(z_neg_alpha);
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    cplx<R> s = mk<R>(0, 0);
+#pragma unroll
+    for (int j = 0; j < D; ++j) s += st.V[i * D + j] * w[j];
+    v[i] = phase * s;
+    phase = phase * z_alpha;
+  }
+}
+
+// Spin mixing exp(-i c1 tau <F>·F) (src/spin_mixing.jl:1-66).
+template <typename R, int D>
+__device__ __forceinline__ void spin_mixing_point(cplx<R> (&v)[D], R c1, R tau, int itp, const SpinTabs<R>& st) {
+  if constexpr (D == 3) {
+    rodrigues_point<R, D>(v, c1, tau, itp, st);
+  } else if constexpr (D > 1) {
+    R fx, fy, fz;
+    spin_vector<R, D>(v, st, fx, fy, fz);
+    euler_point<R, D>(v, c1 * fx, c1 * fy, c1 * fz, tau, itp, st);
+  }
+}
+
+template <typename R, int D>
+__global__ void __launch_bounds__(256) k_potential(PotArgs<R> a, SpinTabs<R> st) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.N) return;
+  cplx<R> v[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) v[c] = a.psi[c * a.N + p];
+  const R Vp = a.V[p];
+  if (a.pre_diag) diag_point<R, D>(v, Vp, a);
+  if (a.rot_a) spin_mixing_point<R, D>(v, a.c1, a.tau_s, a.itp, st);
+  if (a.ddi_rot) {
+    euler_point<R, D>(v, a.phi[p], a.phi[a.N + p], a.phi[2 * a.N + p], a.tau_ddi, a.itp, st);
+  }
+  if (a.rot_b) spin_mixing_point<R, D>(v, a.c1, a.tau_s, a.itp, st);
+  if (a.post_diag) diag_point<R, D>(v, Vp, a);
+#pragma unroll
+  for (int c = 0; c < D; ++c) a.psi[c * a.N + p] = v[c];
+  if (a.spin_out) {
+    R fx, fy, fz;
+    spin_vector<R, D>(v, st, fx, fy, fz);
+    a.spin_out[p] = fx;
+    a.spin_out[a.N + p] = fy;
+    a.spin_out[2 * a.N + p] = fz;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// General-F tensor interaction (src/tensor_interaction.jl:130-240).
+// h_{cc'} = sum_J G[J][c][c'] conj(psi_{J-c}) psi_{J-c'} with
+// G[J][c][c'] = sum_S g_S CG(m,mu|S,M) CG(m',nu|S,M), M = 2F - J (the HF-entry sum
+// regrouped by M; same terms, fewer multiplies).  psi <- exp(-i h tau) psi is
+// evaluated by a Taylor series with sub-steps sized from the bound
+// ||h|| <= n * sum_S |g_S| (2S+1)/(2F+1); the series is cut when the bound of the
+// next term falls below the working precision.  exp(-i h tau) is the same
+// operator the reference forms from the eigen-decomposition V e^{-i Lambda tau} V^†.
+// ---------------------------------------------------------------------------
+template <typename R>
+struct TensorArgs {
+  cplx<R>* psi;
+  int64_t N;
+  const R* V;
+  const double* G;            // (4F+1) * D * D
+  double bound_coef;          // sum_S |g_S| (2S+1)/(2F+1)
+  int n_apply;                // 1 or 2 tensor applications
+  int pre_diag, post_diag;
+  int itp;
+  R tau;                      // tensor tau
+  R tau_d, c0, c_lhy;         // diagonal stage (same layout as PotArgs)
+  cplx<R> zee[kMaxD];
+  double eps;                 // series cut
+};
+
+template <typename R, int D>
+__device__ __forceinline__ void diag_point_t(cplx<R> (&v)[D], R Vp, const TensorArgs<R>& a) {
+  R n = 0;
+#pragma unroll
+  for (int c = 0; c < D; ++c) n += abs2(v[c]);
+  const R Vint = a.c0 * n + a.c_lhy * n * sqrt(n);
+  cplx<R> base;
+  if (a.itp) base = mk<R>(exp(-(Vp + Vint) * a.tau_d), (R)0);
+  else base = cis_(-(Vp + Vint) * a.tau_d);
+#pragma unroll
+  for (int c = 0; c < D; ++c) v[c] = v[c] * (base * a.zee[c]);
+}
+
+template <typename R, int D>
+__device__ __forceinline__ void tensor_point(cplx<R> (&v)[D], const TensorArgs<R>& a, cplx<R>* hs, int hstride) {
+  constexpr int F = (D - 1) / 2;
+  R nl = 0;
+#pragma unroll
+  for (int c = 0; c < D; ++c) nl += abs2(v[c]);
+  if (nl < (R)1e-20) return;
+  // build the upper triangle of h into shared memory
+  int hi = 0;
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+#pragma unroll
+    for (int cp = c; cp < D; ++cp) {
+      cplx<R> acc = mk<R>(0, 0);
+#pragma unroll
+      for (int J = cp; J <= c + D - 1; ++J) {
+        const R gcoef = (R)__ldg(a.G + ((size_t)J * D + c) * D + cp);
+        acc += gcoef * cmulc(v[J - c], v[J - cp]);
+      }
+      hs[hi * hstride] = acc;
+      ++hi;
+    }
+  }
+  const double x = a.bound_coef * (double)nl * fabs((double)a.tau);
+  int nsub = 1;
+  if (x > 0.5) nsub = (int)ceil(x / 0.5);
+  const double xs = x / nsub;
+  // number of terms: smallest K with xs^(K+1)/(K+1)! < eps
+  int K = 0;
+  {
+    double term = 1.0;
+    while (K < 40) {
+      term *= xs / (double)(K + 1);
+      if (term < a.eps) break;
+      ++K;
+    }
+    K = K + 1;
+  }
+  const R dtau = a.tau / (R)nsub;
+  for (int sub = 0; sub < nsub; ++sub) {
+    cplx<R> term[D], acc[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      term[c] = v[c];
+      acc[c] = v[c];
+    }
+    for (int k = 1; k <= K; ++k) {
+      cplx<R> y[D];
+#pragma unroll
+      for (int c = 0; c < D; ++c) y[c] = mk<R>(0, 0);
+      int idx = 0;
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+#pragma unroll
+        for (int cp = c; cp < D; ++cp) {
+          const cplx<R> h = hs[idx * hstride];
+          y[c] += h * term[cp];
+          if (cp != c) y[cp] += cmulc(h, term[c]);
+          ++idx;
+        }
+      }
+      const R f = dtau / (R)k;
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+        term[c] = a.itp ? (-f) * y[c] : mul_mi(f * y[c]);
+        acc[c] += term[c];
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < D; ++c) v[c] = acc[c];
+  }
+  (void)F;
+}
+
+template <typename R, int D>
+__global__ void __launch_bounds__(64) k_tensor(TensorArgs<R> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx<R>* hs = reinterpret_cast<cplx<R>*>(smem_raw) + threadIdx.x;
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= a.N) return;
+  cplx<R> v[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) v[c] = a.psi[c * a.N + p];
+  const R Vp = a.V[p];
+  if (a.pre_diag) diag_point_t<R, D>(v, Vp, a);
+  for (int r = 0; r < a.n_apply; ++r) tensor_point<R, D>(v, a, hs, blockDim.x);
+  if (a.post_diag) diag_point_t<R, D>(v, Vp, a);
+#pragma unroll
+  for (int c = 0; c < D; ++c) a.psi[c * a.N + p] = v[c];
+}
+
+// Spin density only (src/observables.jl:61-86).
+template <typename R, int D>
+__global__ void __launch_bounds__(256) k_spin_density(const cplx<R>* __restrict__ psi, int64_t N, SpinTabs<R> st,
+                                                      R* __restrict__ out) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= N) return;
+  cplx<R> v[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) v[c] = psi[c * N + p];
+  R fx, fy, fz;
+  spin_vector<R, D>(v, st, fx, fy, fz);
+  out[p] = fx;
+  out[N + p] = fy;
+  out[2 * N + p] = fz;
+}
+
+// ---------------------------------------------------------------------------
+// Reductions: per-block partial results (double), then a fixed-order finish.
+// ---------------------------------------------------------------------------
+constexpr int kRedThreads = 256;
+
+template <int K>
+__device__ __forceinline__ void block_reduce_store(double (&vals)[K], double* partials, bool is_max) {
+  __shared__ double red[K][kRedThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    double x = vals[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double y = __shfl_down_sync(0xffffffffu, x, o);
+      x = is_max ? fmax(x, y) : x + y;
+    }
+    if (lane == 0) red[k][warp] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < K) {
+    const int k = threadIdx.x;
+    double x = red[k][0];
+    for (int w = 1; w < kRedThreads / 32; ++w) x = is_max ? fmax(x, red[k][w]) : x + red[k][w];
+    partials[(size_t)blockIdx.x * K + k] = x;
+  }
+}
+
+// Sum (or max) K values over nb partial blocks into out[k].
+template <int K>
+__global__ void k_reduce_finish(const double* __restrict__ partials, int nb, int is_max, double* __restrict__ out) {
+  const int k = threadIdx.x;
+  if (k >= K) return;
+  double x = is_max ? 0.0 : 0.0;
+  for (int b = 0; b < nb; ++b) {
+    const double y = partials[(size_t)b * K + k];
+    x = is_max ? fmax(x, y) : x + y;
+  }
+  out[k] = x;
+}
+
+// Per-component sums of |psi_c|^2 (D values) and the NaN count (slot D).
+template <typename R, int D>
+__global__ void __launch_bounds__(kRedThreads) k_comp_norms(const cplx<R>* __restrict__ psi, int64_t N,
+                                                            double* partials) {
+  double acc[D + 1];
+#pragma unroll
+  for (int c = 0; c <= D; ++c) acc[c] = 0.0;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      const cplx<R> z = psi[c * N + p];
+      acc[c] += (double)z.x * (double)z.x + (double)z.y * (double)z.y;
+      if (isnan(z.x) || isnan(z.y)) acc[D] += 1.0;
+    }
+  }
+  block_reduce_store<D + 1>(acc, partials, false);
+}
+
+// Energy terms on the grid: [trap, n^2, |f|^2, n^{5/2}] (src/energy.jl:67-108).
+template <typename R, int D>
+__global__ void __launch_bounds__(kRedThreads) k_energy_local(const cplx<R>* __restrict__ psi, int64_t N,
+                                                              const R* __restrict__ V, SpinTabs<R> st,
+                                                              double* partials) {
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (int64_t)gridDim.x * blockDim.x) {
+    double n = 0.0, fz = 0.0, fre = 0.0, fim = 0.0;
+    cplx<R> prev = mk<R>(0, 0);
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      const cplx<R> z = psi[c * N + p];
+      const double a2 = (double)z.x * z.x + (double)z.y * z.y;
+      n += a2;
+      fz += (double)st.m[c] * a2;
+      if (c >= 1) {
+        const double pr = (double)prev.x * z.x + (double)prev.y * z.y;
+        const double pi = (double)prev.x * z.y - (double)prev.y * z.x;
+        fre += (double)st.fp[c] * pr;
+        fim += (double)st.fp[c] * pi;
+      }
+      prev = z;
+    }
+    acc[0] += (double)V[p] * n;
+    acc[1] += n * n;
+    acc[2] += fre * fre + fim * fim + fz * fz;
+    acc[3] += n * n * sqrt(n);
+  }
+  block_reduce_store<4>(acc, partials, false);
+}
+
+// Tensor energy sum_S g_S sum_M |A_SM|^2 (src/tensor_interaction.jl:247-276).
+// Pair table rows: (a_idx, c1, c2) packed into int4 .x/.y/.z, coefficient cg*... in pcg.
+template <typename R, int D>
+__global__ void __launch_bounds__(kRedThreads) k_tensor_energy(const cplx<R>* __restrict__ psi, int64_t N,
+                                                               const int4* __restrict__ pairs,
+                                                               const double* __restrict__ pcg, int n_pairs,
+                                                               const double* __restrict__ gA, int nA,
+                                                               double* partials) {
+  double acc[1] = {0.0};
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (int64_t)gridDim.x * blockDim.x) {
+    double2 v[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      const cplx<R> z = psi[c * N + p];
+      v[c] = make_double2((double)z.x, (double)z.y);
+    }
+    double e = 0.0;
+    int cur = -1;
+    double2 A = make_double2(0.0, 0.0);
+    for (int q = 0; q < n_pairs; ++q) {
+      const int4 pr = __ldg(pairs + q);
+      if (pr.x != cur) {
+        if (cur >= 0) e += 0.5 * gA[cur] * (A.x * A.x + A.y * A.y);
+        cur = pr.x;
+        A = make_double2(0.0, 0.0);
+      }
+      const double cg = __ldg(pcg + q);
+      const double2 a = v[pr.y], b = v[pr.z];
+      A.x += cg * (a.x * b.x - a.y * b.y);
+      A.y += cg * (a.x * b.y + a.y * b.x);
+    }
+    if (cur >= 0) e += 0.5 * gA[cur] * (A.x * A.x + A.y * A.y);
+    acc[0] += e;
+    (void)nA;
+  }
+  block_reduce_store<1>(acc, partials, false);
+}
+
+// Kinetic energy sum_k k^2 |psi_hat_c(k)|^2 over all components of a transformed buffer.
+template <typename R>
+__global__ void __launch_bounds__(kRedThreads) k_kinetic_sum(const cplx<R>* __restrict__ a, int64_t N, int D,
+                                                             PhaseTableArgs g, double* partials) {
+  double acc[1] = {0.0};
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < N * D; q += (int64_t)gridDim.x * blockDim.x) {
+    int64_t p = q % N;
+    double k2 = 0.0;
+    for (int ax = 0; ax < g.ndim; ++ax) {
+      const int n = g.n[ax];
+      const int m = (int)(p % n);
+      p /= n;
+      const double k = (double)freq_index(m, n) * g.kmult[ax];
+      k2 += k * k;
+    }
+    const cplx<R> z = a[q];
+    acc[0] += k2 * ((double)z.x * z.x + (double)z.y * z.y);
+  }
+  block_reduce_store<1>(acc, partials, false);
+}
+
+// sum Φ·F over the grid (src/energy.jl:111-121).
+template <typename R>
+__global__ void __launch_bounds__(kRedThreads) k_dot3(const R* __restrict__ a, const R* __restrict__ b, int64_t N,
+                                                      double* partials) {
+  double acc[1] = {0.0};
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (int64_t)gridDim.x * blockDim.x) {
+    acc[0] += (double)a[p] * b[p] + (double)a[N + p] * b[N + p] + (double)a[2 * N + p] * b[2 * N + p];
+  }
+  block_reduce_store<1>(acc, partials, false);
+}
+
+// [sum |a-b|^2, sum |b|^2] (src/adaptive.jl:42-50).
+template <typename R>
+__global__ void __launch_bounds__(kRedThreads) k_l2_change(const cplx<R>* __restrict__ a, const cplx<R>* __restrict__ b,
+                                                           int64_t n, double* partials) {
+  double acc[2] = {0.0, 0.0};
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    const cplx<R> x = a[q], y = b[q];
+    const double dr = (double)x.x - (double)y.x, di = (double)x.y - (double)y.y;
+    acc[0] += dr * dr + di * di;
+    acc[1] += (double)y.x * y.x + (double)y.y * y.y;
+  }
+  block_reduce_store<2>(acc, partials, false);
+}
+
+// [max |a|, max |a-b|] (src/ground_state.jl:148-150); b may be null.
+template <typename R>
+__global__ void __launch_bounds__(kRedThreads) k_max_abs(const cplx<R>* __restrict__ a, const cplx<R>* __restrict__ b,
+                                                         int64_t n, double* partials) {
+  double acc[2] = {0.0, 0.0};
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    const cplx<R> x = a[q];
+    acc[0] = fmax(acc[0], hypot((double)x.x, (double)x.y));
+    if (b) {
+      const cplx<R> y = b[q];
+      acc[1] = fmax(acc[1], hypot((double)x.x - (double)y.x, (double)x.y - (double)y.y));
+    }
+  }
+  block_reduce_store<2>(acc, partials, true);
+}
+
+// max |Φ| over the 3 DDI fields (src/ground_state.jl:12-17).
+template <typename R>
+__global__ void __launch_bounds__(kRedThreads) k_max_abs_real(const R* __restrict__ a, int64_t n, double* partials) {
+  double acc[1] = {0.0};
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+    acc[0] = fmax(acc[0], fabs((double)a[q]));
+  block_reduce_store<1>(acc, partials, true);
+}
+
+// ---------------------------------------------------------------------------
+// Elementwise helpers
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void k_scale(cplx<R>* a, int64_t n, double s) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+    a[q] = a[q] * (R)s;
+}
+
+// psi /= sqrt(sum_c sums[c]*dV) with the sums already on the device (src/split_step.jl:185-195).
+template <typename R>
+__global__ void k_normalize_apply(cplx<R>* a, int64_t N, int D, const double* __restrict__ sums, double dV) {
+  double ns = 0.0;
+  for (int c = 0; c < D; ++c) ns += sums[c] * dV;
+  const R s = (R)(1.0 / sqrt(ns));
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < N * D; q += (int64_t)gridDim.x * blockDim.x)
+    a[q] = a[q] * s;
+}
+
+// Per-component scale psi_c *= w[c] (constrained normalisation, src/ground_state.jl:312-317).
+template <typename R>
+__global__ void k_scale_comp(cplx<R>* a, int64_t N, int D, const double* w) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < N * D; q += (int64_t)gridDim.x * blockDim.x)
+    a[q] = a[q] * (R)w[q / N];
+}
+
+template <typename R>
+__global__ void k_from_f64(const double2* __restrict__ src, cplx<R>* __restrict__ dst, int64_t n) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+    dst[q] = mk<R>((R)src[q].x, (R)src[q].y);
+}
+
+template <typename R>
+__global__ void k_to_f64(const cplx<R>* __restrict__ src, double2* __restrict__ dst, int64_t n) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+    dst[q] = make_double2((double)src[q].x, (double)src[q].y);
+}
+
+template <typename R>
+__global__ void k_real_from_f64(const double* __restrict__ src, R* __restrict__ dst, int64_t n) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+    dst[q] = (R)src[q];
+}
+
+template <typename R>
+__global__ void k_real_to_f64(const R* __restrict__ src, double* __restrict__ dst, int64_t n) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x)
+    dst[q] = (double)src[q];
+}
+
+}  // namespace sbec

@@ -1,0 +1,473 @@
+"""SpinorBEC.jl's hot-path API over the C ABI (names follow the Julia API).
+
+=====================================  =================================================
+Julia (reference)                      here (every call runs on the GPU through libsbec)
+=====================================  =================================================
+make_workspace (initialization.jl:86)  make_workspace(...) -> Workspace
+split_step! (split_step.jl:10)         split_step(ws, n=1)
+_half_potential_step! (:48)            half_potential_step(ws, dt_half, imaginary_time)
+apply_kinetic_step_batched! (prop:130) kinetic_step(ws, dt, imaginary_time)
+_strang_core! / _yoshida_core!         strang_core(ws, dt) / yoshida_core(ws, dt)
+run_simulation! (simulation.jl:1)      run_simulation(ws, callback=None)
+run_simulation_adaptive! (adaptive:57) run_simulation_adaptive(ws, ...)
+run_simulation_yoshida! (yoshida:11)   run_simulation_yoshida(ws, ...)
+find_ground_state (ground_state:80)    find_ground_state(...)
+find_ground_state_multistart (:239)    find_ground_state_multistart(...)
+scan_continuation (:328)               scan_continuation(...)
+total_energy / total_norm / magnet.    total_energy(ws) / total_norm(ws) / magnetization(ws)
+=====================================  =================================================
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import math
+from typing import Callable, Optional
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, dptr, load
+from .host import (AdaptiveDtParams, AtomSpecies, Grid, InteractionParams, SimParams, SimulationResult,
+                   ZeemanParams, cell_volume, evaluate_potential, from_interleaved, init_psi, to_interleaved)
+
+PRECISIONS = {"fp64": _lib.SBEC_FP64, "fp32": _lib.SBEC_FP32_BULK, "fp32_bulk": _lib.SBEC_FP32_BULK}
+
+
+class Workspace:
+    """A device-resident workspace (``Workspace``, src/types.jl:387-407)."""
+
+    def __init__(self, handle, grid: Grid, F: int, sim_params: SimParams, precision: str, zeeman):
+        self._h = handle
+        self.grid = grid
+        self.F = F
+        self.D = 2 * F + 1
+        self.sim_params = sim_params
+        self.precision = precision
+        self.zeeman = zeeman
+        self._lib = load()
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise ValueError("workspace has been closed")
+        return self._h
+
+    def close(self) -> None:
+        if self._h is not None:
+            check(self._lib.sbec_ws_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- state
+    @property
+    def psi(self) -> np.ndarray:
+        n = int(np.prod(self.grid.config.n_points)) * self.D
+        buf = np.empty(2 * n, dtype=np.float64)
+        check(self._lib.sbec_get_psi(self.handle, dptr(buf)))
+        return from_interleaved(buf, self.grid.config.n_points, self.D)
+
+    @psi.setter
+    def psi(self, value: np.ndarray) -> None:
+        buf = to_interleaved(value)
+        check(self._lib.sbec_set_psi(self.handle, dptr(buf)))
+
+    @property
+    def t(self) -> float:
+        t = C.c_double()
+        s = C.c_int64()
+        check(self._lib.sbec_get_time(self.handle, C.byref(t), C.byref(s)))
+        return t.value
+
+    @property
+    def step(self) -> int:
+        t = C.c_double()
+        s = C.c_int64()
+        check(self._lib.sbec_get_time(self.handle, C.byref(t), C.byref(s)))
+        return s.value
+
+    def set_time(self, t: float, step: int) -> None:
+        check(self._lib.sbec_set_time(self.handle, float(t), int(step)))
+
+    def set_zeeman(self, p: float, q: float) -> None:
+        check(self._lib.sbec_set_zeeman(self.handle, float(p), float(q)))
+
+    def set_dt(self, dt: float) -> None:
+        check(self._lib.sbec_set_dt(self.handle, float(dt)))
+        self.sim_params = SimParams(dt, self.sim_params.n_steps, self.sim_params.imaginary_time,
+                                    self.sim_params.normalize_every, self.sim_params.save_every)
+
+    def tensor_channels(self):
+        act = C.c_int32()
+        n = C.c_int32()
+        S = (C.c_int32 * 32)()
+        g = (C.c_double * 32)()
+        check(self._lib.sbec_tensor_channels(self.handle, C.byref(act), C.byref(n), S, g))
+        return bool(act.value), {int(S[i]): float(g[i]) for i in range(n.value)}
+
+
+def make_workspace(*, grid: Grid, atom: AtomSpecies, interactions: InteractionParams, zeeman=None, potential=None,
+                   sim_params: SimParams, psi_init: Optional[np.ndarray] = None, enable_ddi: bool = False,
+                   c_dd: float = float("nan"), secular_ddi: bool = False, ddi_padding: bool = False,
+                   gS: Optional[dict] = None, precision: str = "fp64") -> Workspace:
+    """``make_workspace`` (src/initialization.jl:86-191) with a device-resident state."""
+    lib = load()
+    zeeman = ZeemanParams() if zeeman is None else zeeman
+    if callable(zeeman):
+        z0 = zeeman(0.0)
+    else:
+        z0 = zeeman
+    F = atom.F
+    if enable_ddi and math.isnan(c_dd) and atom.mu_mag > 0.0:
+        raise _lib.ArgumentError(
+            f"enable_ddi=true for dipolar atom {atom.name} but c_dd not specified. Pass c_dd in dimensionless units.")
+    cfg = _lib.sbec_config()
+    nd = grid.config.ndim
+    cfg.ndim = nd
+    for d in range(nd):
+        cfg.n[d] = grid.config.n_points[d]
+        cfg.L[d] = grid.config.box_size[d]
+    cfg.F = F
+    cfg.c0, cfg.c1, cfg.c_lhy = interactions.c0, interactions.c1, interactions.c_lhy
+    ce = tuple(interactions.c_extra)
+    if len(ce) > _lib.SBEC_MAX_C_EXTRA:
+        raise _lib.ArgumentError("too many c_extra entries")
+    cfg.n_c_extra = len(ce)
+    for i, v in enumerate(ce):
+        cfg.c_extra[i] = float(v)
+    if gS is not None:
+        cfg.gS_direct = 1
+        for S in range(0, 2 * F + 1, 2):
+            cfg.gS[S // 2] = float(gS.get(S, 0.0))
+    cfg.zeeman_p, cfg.zeeman_q = z0.p, z0.q
+    cfg.enable_ddi = int(bool(enable_ddi))
+    cfg.c_dd = 0.0 if math.isnan(c_dd) else float(c_dd)
+    cfg.secular_ddi = int(bool(secular_ddi))
+    cfg.ddi_padding = int(bool(ddi_padding))
+    cfg.dt = sim_params.dt
+    cfg.imaginary_time = int(bool(sim_params.imaginary_time))
+    cfg.normalize_every = int(sim_params.normalize_every)
+    if precision not in PRECISIONS:
+        raise _lib.ArgumentError(f"unknown precision {precision!r}")
+    cfg.precision = PRECISIONS[precision]
+    psi = init_psi(grid, F) if psi_init is None else psi_init
+    pbuf = to_interleaved(psi)
+    if pbuf.size != 2 * int(np.prod(grid.config.n_points)) * (2 * F + 1):
+        raise _lib.ArgumentError("psi_init has the wrong shape")
+    V = np.ascontiguousarray(evaluate_potential(potential, grid).ravel(order="F"))
+    h = C.c_void_p()
+    check(lib.sbec_ws_create(C.byref(cfg), dptr(pbuf), dptr(V), C.byref(h)))
+    return Workspace(h, grid, F, sim_params, precision, zeeman)
+
+
+# ---- operators ---------------------------------------------------------------
+
+def _zeeman_now(ws: Workspace) -> None:
+    if callable(ws.zeeman):
+        z = ws.zeeman(ws.t)
+        ws.set_zeeman(z.p, z.q)
+
+
+def half_potential_step(ws: Workspace, dt_half: float, imaginary_time: bool = False) -> None:
+    _zeeman_now(ws)
+    check(ws._lib.sbec_half_potential(ws.handle, float(dt_half), int(bool(imaginary_time))))
+
+
+def kinetic_step(ws: Workspace, dt: float, imaginary_time: bool = False) -> None:
+    check(ws._lib.sbec_kinetic(ws.handle, float(dt), int(bool(imaginary_time))))
+
+
+def split_step(ws: Workspace, n: int = 1) -> None:
+    """``split_step!`` repeated ``n`` times (src/split_step.jl:10-35)."""
+    check(ws._lib.sbec_split_step(ws.handle, int(n)))
+
+
+def strang_core(ws: Workspace, dt: float) -> None:
+    check(ws._lib.sbec_strang_core(ws.handle, float(dt)))
+
+
+def yoshida_core(ws: Workspace, dt: float) -> None:
+    check(ws._lib.sbec_yoshida_core(ws.handle, float(dt)))
+
+
+def normalize(ws: Workspace) -> None:
+    check(ws._lib.sbec_normalize(ws.handle))
+
+
+def normalize_constrained(ws: Workspace, target_Mz: float) -> None:
+    check(ws._lib.sbec_normalize_constrained(ws.handle, float(target_Mz)))
+
+
+# ---- reductions ----------------------------------------------------------------
+
+def total_energy(ws: Workspace) -> float:
+    E = C.c_double()
+    check(ws._lib.sbec_total_energy(ws.handle, C.byref(E)))
+    return E.value
+
+
+def energy_terms(ws: Workspace) -> dict:
+    t = _lib.sbec_energy_terms()
+    check(ws._lib.sbec_energy_breakdown(ws.handle, C.byref(t)))
+    return {k: getattr(t, k) for k, _ in t._fields_}
+
+
+def total_norm(ws: Workspace) -> float:
+    v = C.c_double()
+    check(ws._lib.sbec_total_norm(ws.handle, C.byref(v)))
+    return v.value
+
+
+def magnetization(ws: Workspace) -> float:
+    v = C.c_double()
+    check(ws._lib.sbec_magnetization(ws.handle, C.byref(v)))
+    return v.value
+
+
+def spin_density_vector(ws: Workspace):
+    n = int(np.prod(ws.grid.config.n_points))
+    out = np.empty(3 * n)
+    check(ws._lib.sbec_spin_density(ws.handle, dptr(out)))
+    shp = ws.grid.config.n_points
+    return tuple(out[i * n:(i + 1) * n].reshape(shp, order="F") for i in range(3))
+
+
+def ddi_potential(ws: Workspace, padded: bool = False):
+    n = int(np.prod(ws.grid.config.n_points))
+    out = np.empty(3 * n)
+    check(ws._lib.sbec_ddi_potential(ws.handle, int(bool(padded)), dptr(out)))
+    shp = ws.grid.config.n_points
+    return tuple(out[i * n:(i + 1) * n].reshape(shp, order="F") for i in range(3))
+
+
+# ---- drivers -------------------------------------------------------------------
+
+class _Recorder:
+    def __init__(self, ws: Workspace, callback, keep_psi: bool, use_count_arg: bool):
+        self.ws = ws
+        self.res = SimulationResult()
+        self.callback = callback
+        self.keep_psi = keep_psi
+        self.first = True
+        self.count = 0
+        self.err = None
+
+        def _cb(user, snap_p):
+            try:
+                s = snap_p.contents
+                self.res.times.append(s.t)
+                self.res.energies.append(s.energy)
+                self.res.norms.append(s.norm)
+                self.res.magnetizations.append(s.magnetization)
+                if self.keep_psi:
+                    n = int(np.prod(ws.grid.config.n_points)) * ws.D
+                    arr = np.ctypeslib.as_array(s.psi, shape=(2 * n,)).copy()
+                    self.res.psi_snapshots.append(from_interleaved(arr, ws.grid.config.n_points, ws.D))
+                if self.first:
+                    self.first = False
+                elif self.callback is not None:
+                    self.count += 1
+                    self.callback(ws, s.step if not use_count_arg else self.count)
+                return 0
+            except Exception as e:  # surface Python errors after the C call returns
+                self.err = e
+                return 1
+
+        self.cfunc = _lib.CALLBACK(_cb)
+
+    def raise_pending(self):
+        if self.err is not None:
+            raise self.err
+
+
+def run_simulation(ws: Workspace, callback: Optional[Callable] = None, keep_psi: bool = True) -> SimulationResult:
+    """``run_simulation!`` (src/simulation.jl:1-94): leapfrog real time or the standard ITP loop."""
+    sp = ws.sim_params
+    rec = _Recorder(ws, callback, keep_psi, use_count_arg=False)
+    st = ws._lib.sbec_run_simulation(ws.handle, sp.n_steps, sp.save_every, rec.cfunc, None)
+    rec.raise_pending()
+    check(st)
+    return rec.res
+
+
+def _adaptive_params(adaptive: AdaptiveDtParams) -> _lib.sbec_adaptive_params:
+    p = _lib.sbec_adaptive_params()
+    p.dt_init, p.dt_min, p.dt_max, p.tol = adaptive.dt_init, adaptive.dt_min, adaptive.dt_max, adaptive.tol
+    p.error_mode = 0 if adaptive.error_mode == "step_change" else 1
+    return p
+
+
+def run_simulation_adaptive(ws: Workspace, adaptive: AdaptiveDtParams = None, *, t_end: float,
+                            save_interval: float, callback=None, keep_psi: bool = True) -> dict:
+    """``run_simulation_adaptive!`` (src/adaptive.jl:57-296)."""
+    adaptive = AdaptiveDtParams() if adaptive is None else adaptive
+    rec = _Recorder(ws, callback, keep_psi, use_count_arg=True)
+    out = _lib.sbec_adaptive_result()
+    st = ws._lib.sbec_run_adaptive(ws.handle, C.byref(_adaptive_params(adaptive)), float(t_end),
+                                   float(save_interval), rec.cfunc, None, C.byref(out))
+    rec.raise_pending()
+    check(st)
+    _final_snapshot(ws, rec)
+    return dict(result=rec.res, n_accepted=out.n_accepted, n_rejected=out.n_rejected, final_dt=out.final_dt)
+
+
+def run_simulation_yoshida(ws: Workspace, adaptive: AdaptiveDtParams = None, *, t_end: float,
+                           save_interval: float, callback=None, keep_psi: bool = True,
+                           max_accepted: Optional[int] = None) -> dict:
+    """``run_simulation_yoshida!`` (src/yoshida.jl:11-98)."""
+    adaptive = AdaptiveDtParams() if adaptive is None else adaptive
+    rec = _Recorder(ws, callback, keep_psi, use_count_arg=True)
+    out = _lib.sbec_adaptive_result()
+    st = ws._lib.sbec_run_yoshida(ws.handle, C.byref(_adaptive_params(adaptive)), float(t_end), float(save_interval),
+                                  int(max_accepted or 0), rec.cfunc, None, C.byref(out))
+    rec.raise_pending()
+    check(st)
+    _final_snapshot(ws, rec)
+    return dict(result=rec.res, n_accepted=out.n_accepted, n_rejected=out.n_rejected, final_dt=out.final_dt)
+
+
+def _final_snapshot(ws: Workspace, rec: _Recorder) -> None:
+    """Closing `_record_snapshot!` when the last save time differs from t (src/yoshida.jl:93-95)."""
+    t = ws.t
+    if not rec.res.times or abs(rec.res.times[-1] - t) > 1e-12:
+        rec.res.times.append(t)
+        rec.res.energies.append(total_energy(ws))
+        rec.res.norms.append(total_norm(ws))
+        rec.res.magnetizations.append(magnetization(ws))
+        if rec.keep_psi:
+            rec.res.psi_snapshots.append(ws.psi)
+
+
+ITP_EXPONENT_LIMIT = 50.0
+
+
+def _zeeman_energies(z: ZeemanParams, F: int) -> np.ndarray:
+    return np.array([-z.p * (F - c) + z.q * (F - c) ** 2 for c in range(2 * F + 1)])
+
+
+def _validate_itp(zeeman, interactions: InteractionParams, F: int, dt: float, psi, c_dd: float) -> None:
+    """``_validate_itp_zeeman`` / ``_validate_itp_interactions`` (src/ground_state.jl:31-78)."""
+    if not callable(zeeman):
+        if float(np.max(np.abs(_zeeman_energies(zeeman, F)))) * dt / 4 > ITP_EXPONENT_LIMIT:
+            raise _lib.ArgumentError(f"Zeeman p={zeeman.p} with F={F} and dt={dt} causes overflow in imaginary time")
+    n_peak = float(np.max(np.sum(np.abs(psi) ** 2, axis=-1))) if psi is not None else 1.0
+    max_c = max(abs(interactions.c0), abs(interactions.c1))
+    if max_c > 1e-30 and max_c * n_peak * dt / 4 > ITP_EXPONENT_LIMIT:
+        raise _lib.ArgumentError("Spin interaction may cause overflow in imaginary time; reduce c0/c1 or dt")
+    if c_dd > 0 and c_dd * F * n_peak * dt / 2 > ITP_EXPONENT_LIMIT:
+        raise _lib.ArgumentError("DDI may cause overflow in imaginary time; reduce c_dd or dt")
+
+
+def find_ground_state(*, grid: Grid, atom: AtomSpecies, interactions: InteractionParams, zeeman=None,
+                      potential=None, dt: float = 0.001, n_steps: int = 10000, tol: float = 1e-10,
+                      initial_state: str = "polar", psi_init=None, enable_ddi: bool = False,
+                      c_dd: float = float("nan"), secular_ddi: bool = False, adaptive_dt: bool = False,
+                      dt_max: Optional[float] = None, target_magnetization: Optional[float] = None,
+                      precision: str = "fp64") -> dict:
+    """``find_ground_state`` (src/ground_state.jl:80-237)."""
+    zeeman = ZeemanParams() if zeeman is None else zeeman
+    psi0 = init_psi(grid, atom.F, initial_state) if psi_init is None else np.array(psi_init, order="F", copy=True)
+    eff_cdd = c_dd if (enable_ddi and not math.isnan(c_dd)) else 0.0
+    _validate_itp(zeeman, interactions, atom.F, dt, psi0, eff_cdd)
+    if adaptive_dt:
+        return _find_ground_state_adaptive(grid, atom, interactions, zeeman, potential, dt, n_steps, tol, psi0,
+                                           enable_ddi, c_dd, secular_ddi, 10.0 * dt if dt_max is None else dt_max,
+                                           precision)
+    use_c = target_magnetization is not None
+    sp = SimParams(dt, n_steps, True, 0 if use_c else 1, max(1, n_steps // 10))
+    ws = make_workspace(grid=grid, atom=atom, interactions=interactions, zeeman=zeeman, potential=potential,
+                        sim_params=sp, psi_init=psi0, enable_ddi=enable_ddi, c_dd=c_dd, secular_ddi=secular_ddi,
+                        precision=precision)
+    r = _lib.sbec_gs_result()
+    check(ws._lib.sbec_ground_state(ws.handle, n_steps, float(tol), sp.save_every,
+                                    float(target_magnetization) if use_c else float("nan"), C.byref(r)))
+    return dict(workspace=ws, converged=bool(r.converged), energy=r.energy, dE=r.dE, dpsi=r.dpsi, steps=r.steps)
+
+
+def _find_ground_state_adaptive(grid, atom, interactions, zeeman, potential, dt, n_steps, tol, psi0, enable_ddi,
+                                c_dd, secular_ddi, dt_max, precision):
+    """``_find_ground_state_adaptive`` (src/ground_state.jl:172-237): host loop over device blocks."""
+    current_dt = dt
+    check_every = max(1, n_steps // 100)
+    sp = SimParams(current_dt, check_every, True, 1, check_every)
+    ws = make_workspace(grid=grid, atom=atom, interactions=interactions, zeeman=zeeman, potential=potential,
+                        sim_params=sp, psi_init=psi0, enable_ddi=enable_ddi, c_dd=c_dd, secular_ddi=secular_ddi,
+                        precision=precision)
+    E_prev = total_energy(ws)
+    converged = False
+    total = 0
+    final_dE = final_dpsi = float("nan")
+    while total < n_steps:
+        backup = ws.psi
+        split_step(ws, check_every)
+        total += check_every
+        E = total_energy(ws)
+        if math.isnan(E) or E > E_prev:
+            ws.psi = backup
+            current_dt = max(current_dt * 0.5, 1e-8)
+            ws.set_dt(current_dt)
+        else:
+            psi = ws.psi
+            dE = abs(E - E_prev)
+            pmax = float(np.max(np.abs(psi)))
+            dpsi = float(np.max(np.abs(psi - backup))) / pmax if pmax > 0 else 0.0
+            final_dE, final_dpsi = dE, dpsi
+            if dE < tol and dpsi < tol:
+                converged = True
+                break
+            E_prev = E
+            new_dt = min(current_dt * 1.1, dt_max)
+            if new_dt != current_dt:
+                current_dt = new_dt
+                ws.set_dt(current_dt)
+    return dict(workspace=ws, converged=converged, energy=total_energy(ws), dE=final_dE, dpsi=final_dpsi,
+                steps=total)
+
+
+def find_ground_state_multistart(*, initial_states=("polar", "ferromagnetic", "uniform", "antiferromagnetic"),
+                                 n_random: int = 3, seed: int = 42, grid, atom, interactions, **kw) -> dict:
+    """``find_ground_state_multistart`` (src/ground_state.jl:239-277); random seeds are seed+i."""
+    results = []
+    for state in initial_states:
+        if state == "random":
+            for i in range(1, n_random + 1):
+                psi0 = init_psi(grid, atom.F, "random", seed=seed + i)
+                r = find_ground_state(grid=grid, atom=atom, interactions=interactions, psi_init=psi0, **kw)
+                results.append(dict(initial_state="random", idx=i, **r))
+        else:
+            r = find_ground_state(grid=grid, atom=atom, interactions=interactions, initial_state=state, **kw)
+            results.append(dict(initial_state=state, idx=0, **r))
+    best = min(results, key=lambda r: r["energy"])
+    return dict(workspace=best["workspace"], converged=best["converged"], energy=best["energy"],
+                initial_state=best["initial_state"], all_results=results)
+
+
+def scan_continuation(*, param_values, make_interactions: Callable, grid, atom, initial_state="polar",
+                      energy_jump_threshold=0.1, n_steps_continuation=500, n_steps_fresh=5000, **kw) -> list:
+    """``scan_continuation`` (src/ground_state.jl:328-378), phase classification left to the caller."""
+    results = []
+    prev_psi = None
+    prev_E = float("nan")
+    for val in param_values:
+        inter = make_interactions(val)
+        if prev_psi is not None:
+            r = find_ground_state(grid=grid, atom=atom, interactions=inter, psi_init=prev_psi,
+                                  n_steps=n_steps_continuation, **kw)
+        else:
+            r = find_ground_state(grid=grid, atom=atom, interactions=inter, initial_state=initial_state,
+                                  n_steps=n_steps_fresh, **kw)
+        if not math.isnan(prev_E) and abs(r["energy"] - prev_E) / max(abs(prev_E), 1e-30) > energy_jump_threshold:
+            r = find_ground_state_multistart(grid=grid, atom=atom, interactions=inter, n_steps=n_steps_fresh, **kw)
+        psi = r["workspace"].psi
+        results.append(dict(param=val, energy=r["energy"], converged=r["converged"], psi=psi))
+        prev_psi = psi
+        prev_E = r["energy"]
+    return results
+
+
+__all__ = [n for n in dir() if not n.startswith("_")]

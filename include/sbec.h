@@ -1,0 +1,194 @@
+/*
+ * sbec.h — C ABI of the GB300-native split-step engine for SpinorBEC.jl.
+ *
+ * The library replaces the Julia hot path of SpinorBEC.jl (anko9801/BEC-simulation):
+ * the per-step operators, the integrators and the drivers that loop over them.
+ * A Julia shim keeps the reference API (make_workspace, split_step!, run_simulation!,
+ * run_simulation_adaptive!, run_simulation_yoshida!, find_ground_state, ...) and
+ * forwards to these entry points with `ccall`; the Python package `spinorbec` in
+ * this repository mirrors the same API over ctypes.
+ *
+ * Conventions
+ *  - Wavefunction buffers on the host are the reference's own layout
+ *    (src/types.jl:239-244): complex Float64, interleaved re/im, column-major
+ *    psi[x,(y,(z,))c], x fastest, one planar block of prod(n) points per
+ *    component; component c (0-based) carries m = F - c.
+ *  - The library copies host buffers; it never keeps a caller pointer after a call returns.
+ *  - Every entry point returns an sbec_status.  On failure, sbec_last_error() returns a
+ *    message for the calling thread (valid until that thread's next call).
+ *  - A workspace owns all its device memory and one CUDA stream.  Distinct workspaces are
+ *    independent; one workspace must be used from one host thread at a time.
+ *  - There is no CPU fallback: without a usable CUDA device every entry point that needs
+ *    one returns SBEC_ERR_DEVICE.
+ */
+#ifndef SBEC_H
+#define SBEC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum sbec_status {
+  SBEC_OK = 0,
+  SBEC_ERR_INVALID = 1,      /* invalid argument / configuration (ArgumentError in the reference) */
+  SBEC_ERR_UNSUPPORTED = 2,  /* option outside the GPU path (Raman, loss, nematic-only c2, non power-of-two n) */
+  SBEC_ERR_OOM = 3,          /* device allocation failed */
+  SBEC_ERR_NUMERIC = 4,      /* NaN / ITP overflow detected (src/ground_state.jl:4-29) */
+  SBEC_ERR_DEVICE = 5,       /* CUDA error or no device */
+  SBEC_ERR_CALLBACK = 6      /* a host callback returned non-zero (the run stops) */
+} sbec_status;
+
+typedef enum sbec_precision {
+  SBEC_FP64 = 0,             /* plain form: complex FP64 everywhere */
+  SBEC_FP32_BULK = 1         /* FFTs and pointwise phases in FP32; reductions, norm, energy, errors in FP64 */
+} sbec_precision;
+
+#define SBEC_MAX_C_EXTRA 32
+#define SBEC_MAX_CHANNELS 32
+
+/* Workspace configuration: the arguments of `make_workspace`
+ * (src/initialization.jl:86-101) that reach the hot path. */
+typedef struct sbec_config {
+  int32_t ndim;              /* 1, 2 or 3 */
+  int32_t n[3];              /* points per axis (GridConfig.n_points, src/types.jl:7-20) */
+  double L[3];               /* box size per axis (GridConfig.box_size) */
+  int32_t F;                 /* spin (atom.F) */
+  double c0, c1, c_lhy;      /* InteractionParams (src/types.jl:145-162) */
+  int32_t n_c_extra;         /* InteractionParams.c_extra: c_extra[i] = c_{i+2} */
+  double c_extra[SBEC_MAX_C_EXTRA];
+  int32_t gS_direct;         /* 1: use gS[] below as channel couplings g_S (S = 0,2,...,2F), bypassing
+                                the c0/c1/c_extra activation rule (_make_tensor_cache_from_channels) */
+  double gS[SBEC_MAX_CHANNELS];
+  double zeeman_p, zeeman_q; /* ZeemanParams (src/types.jl:172-178); time-dependent: sbec_set_zeeman */
+  int32_t enable_ddi;
+  double c_dd;
+  int32_t secular_ddi;
+  int32_t ddi_padding;
+  double dt;                 /* SimParams.dt */
+  int32_t imaginary_time;    /* SimParams.imaginary_time */
+  int32_t normalize_every;   /* SimParams.normalize_every (ITP renormalisation period) */
+  int32_t precision;         /* sbec_precision */
+} sbec_config;
+
+typedef struct sbec_ws sbec_ws;
+
+/* Observables recorded at save points: `_record_snapshot!` (src/simulation_utils.jl:9-15). */
+typedef struct sbec_snapshot {
+  double t;
+  int64_t step;
+  double energy, norm, magnetization;
+  const double* psi;         /* host copy (interleaved, reference layout), valid during the callback only */
+} sbec_snapshot;
+
+/* Save-point callback; return non-zero to stop the run (sbec returns SBEC_ERR_CALLBACK). */
+typedef int (*sbec_callback)(void* user, const sbec_snapshot* snap);
+
+/* AdaptiveDtParams (src/types.jl:343-361); error_mode 0 = :step_change, 1 = :richardson. */
+typedef struct sbec_adaptive_params {
+  double dt_init, dt_min, dt_max, tol;
+  int32_t error_mode;
+} sbec_adaptive_params;
+
+typedef struct sbec_adaptive_result {
+  int64_t n_accepted, n_rejected;
+  double final_dt;
+} sbec_adaptive_result;
+
+/* find_ground_state result tuple (src/ground_state.jl:165-169). */
+typedef struct sbec_gs_result {
+  int32_t converged;
+  double energy, dE, dpsi;
+  int64_t steps;
+} sbec_gs_result;
+
+typedef struct sbec_energy_terms {
+  double kinetic, trap, zeeman, c0, c1, ddi, lhy, tensor;
+} sbec_energy_terms;
+
+/* ---- diagnostics ------------------------------------------------------- */
+const char* sbec_last_error(void);
+const char* sbec_version(void);
+/* Number of usable CUDA devices (0 when none); never fails. */
+int sbec_device_count(void);
+
+/* ---- lifecycle ----------------------------------------------------------
+ * sbec_ws_create replaces make_workspace (src/initialization.jl:86-191): builds the
+ * device-resident psi, potential, kinetic-phase tables, spin-matrix tables, the
+ * tensor-interaction tables (activated as in src/initialization.jl:164-185) and the
+ * DDI buffers (src/ddi.jl:51-102, src/ddi_padded.jl:6-49).
+ * psi: n_total*D complex (2*n_total*D doubles); V: n_total doubles or NULL (NoPotential). */
+sbec_status sbec_ws_create(const sbec_config* cfg, const double* psi, const double* V, sbec_ws** out);
+sbec_status sbec_ws_destroy(sbec_ws* ws);
+
+/* ---- state -------------------------------------------------------------
+ * ws.state.psi / t / step (src/types.jl:239-244). */
+sbec_status sbec_set_psi(sbec_ws* ws, const double* psi);
+sbec_status sbec_get_psi(sbec_ws* ws, double* psi);
+sbec_status sbec_set_time(sbec_ws* ws, double t, int64_t step);
+sbec_status sbec_get_time(sbec_ws* ws, double* t, int64_t* step);
+/* zeeman_at(z, t) evaluated by the host for TimeDependentZeeman (src/zeeman.jl:20-21). */
+sbec_status sbec_set_zeeman(sbec_ws* ws, double p, double q);
+/* Replaces the potential values (evaluate_potential, src/potentials.jl:1-32). */
+sbec_status sbec_set_potential(sbec_ws* ws, const double* V);
+/* _rebuild_workspace_with_dt (src/ground_state.jl:380-392): new dt for split_step!. */
+sbec_status sbec_set_dt(sbec_ws* ws, double dt);
+/* Query: whether the tensor path is active and the channel couplings g_S it uses. */
+sbec_status sbec_tensor_channels(sbec_ws* ws, int32_t* active, int32_t* n_channels, int32_t* S, double* gS);
+
+/* ---- operators ---------------------------------------------------------- */
+/* _half_potential_step!(ws, dt_half, ...) (src/split_step.jl:48-133). */
+sbec_status sbec_half_potential(sbec_ws* ws, double dt_half, int32_t imaginary_time);
+/* apply_kinetic_step_batched! with the phase for `dt` (src/propagators.jl:130-145);
+ * imaginary_time selects exp(-k^2 dt/2) instead of cis(-k^2 dt/2). */
+sbec_status sbec_kinetic(sbec_ws* ws, double dt, int32_t imaginary_time);
+/* _normalize_psi! (src/split_step.jl:185-195). */
+sbec_status sbec_normalize(sbec_ws* ws);
+/* _normalize_psi_constrained! (src/ground_state.jl:279-320). */
+sbec_status sbec_normalize_constrained(sbec_ws* ws, double target_Mz);
+
+/* ---- integrators -------------------------------------------------------- */
+/* split_step!(ws) repeated n times (src/split_step.jl:10-35). */
+sbec_status sbec_split_step(sbec_ws* ws, int64_t n);
+/* _strang_core! / _yoshida_core! (src/split_step.jl:146-183). */
+sbec_status sbec_strang_core(sbec_ws* ws, double dt);
+sbec_status sbec_yoshida_core(sbec_ws* ws, double dt);
+
+/* ---- drivers ------------------------------------------------------------ */
+/* run_simulation!(ws; callback) (src/simulation.jl:1-94): leapfrog-fused real time or the
+ * standard ITP loop; the callback receives each save point (initial state included). */
+sbec_status sbec_run_simulation(sbec_ws* ws, int64_t n_steps, int64_t save_every,
+                                sbec_callback cb, void* user);
+/* run_simulation_adaptive! (src/adaptive.jl:57-296). */
+sbec_status sbec_run_adaptive(sbec_ws* ws, const sbec_adaptive_params* p, double t_end,
+                              double save_interval, sbec_callback cb, void* user,
+                              sbec_adaptive_result* out);
+/* run_simulation_yoshida! (src/yoshida.jl:11-98); max_accepted <= 0 means no cap. */
+sbec_status sbec_run_yoshida(sbec_ws* ws, const sbec_adaptive_params* p, double t_end,
+                             double save_interval, int64_t max_accepted, sbec_callback cb,
+                             void* user, sbec_adaptive_result* out);
+/* The ITP loop of find_ground_state on an existing ITP workspace (src/ground_state.jl:116-169):
+ * convergence checked every check_every steps; target_Mz = NaN disables the constraint. */
+sbec_status sbec_ground_state(sbec_ws* ws, int64_t n_steps, double tol, int64_t check_every,
+                              double target_Mz, sbec_gs_result* out);
+
+/* ---- reductions --------------------------------------------------------- */
+/* total_energy (src/energy.jl:6-54) and its terms. */
+sbec_status sbec_total_energy(sbec_ws* ws, double* E);
+sbec_status sbec_energy_breakdown(sbec_ws* ws, sbec_energy_terms* out);
+/* total_norm, magnetization (src/observables.jl:13-31). */
+sbec_status sbec_total_norm(sbec_ws* ws, double* norm);
+sbec_status sbec_magnetization(sbec_ws* ws, double* Mz);
+/* Spin density (Fx, Fy, Fz) on the grid (src/observables.jl:61-86); 3*n_total doubles. */
+sbec_status sbec_spin_density(sbec_ws* ws, double* out);
+/* Dipolar potential (Φx, Φy, Φz) on the grid for the current psi (src/ddi.jl:108-163,
+ * src/ddi_padded.jl:55-85); padded selects the zero-padded convolution. */
+sbec_status sbec_ddi_potential(sbec_ws* ws, int32_t padded, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SBEC_H */

@@ -1,0 +1,48 @@
+"""FP32-bulk form: FFTs and pointwise phases in FP32, reductions in FP64.
+Each result states its error against the FP64 oracle; the bars are the chosen
+form's targets (ground-state energy within 1e-6 relative, norm kept to 1e-7 per
+renormalised ITP step and to ~1e-6 over real-time runs)."""
+
+import numpy as np
+import pytest
+
+import oracle as O
+import spinorbec as S
+from parity_util import make_pair, rel_psi_err
+
+pytestmark = pytest.mark.gpu
+
+
+def test_fp32_ground_state_energy(gpu):
+    og = O.make_grid(O.GridConfig((64, 64), (20.0, 20.0)))
+    hg = S.make_grid(S.GridConfig((64, 64), (20.0, 20.0)))
+    kw = dict(dt=0.005, n_steps=1000, tol=1e-8, initial_state="ferromagnetic")
+    ro = O.find_ground_state(grid=og, atom=O.Rb87, interactions=O.InteractionParams(10.0, -0.5),
+                             V=O.harmonic_potential(og, (1.0, 1.0)), **kw)
+    rg = S.find_ground_state(grid=hg, atom=S.Rb87, interactions=S.InteractionParams(10.0, -0.5),
+                             potential=S.HarmonicTrap(1.0, 1.0), precision="fp32", **kw)
+    err = abs(rg["energy"] - ro["energy"]) / abs(ro["energy"])
+    assert err < 1e-6, err
+    assert abs(S.total_norm(rg["workspace"]) - 1.0) < 1e-7
+
+
+@pytest.mark.parametrize("case", ["f1", "f6_tensor_ddi"])
+def test_fp32_real_time_error_bounded(gpu, case):
+    if case == "f1":
+        ws_o, ws_g = make_pair((64, 64), (20.0, 20.0), 1, c0=10.0, c1=0.5, omega=(1.0, 1.0), zeeman=(0.0, 0.1),
+                               dt=1e-3, precision="fp32", state="polar")
+        steps = 200
+    else:
+        ip = O.interaction_params_from_constraint(c_total=4689.0, c1_ratio=1 / 36, F=6, c_extra=(0.0, 0.0, 50.0))
+        ws_o, ws_g = make_pair((8, 8, 8), (24.0, 24.0, 24.0), 6, c0=ip.c0, c1=ip.c1, c_extra=ip.c_extra,
+                               omega=(1.0, 1.0, 1.2), ddi=True, c_dd=100.0, padded=True, dt=1e-3,
+                               precision="fp32", state="ferromagnetic")
+        steps = 20
+    N0 = S.total_norm(ws_g)
+    E0 = O.total_energy(ws_o)
+    for _ in range(steps):
+        O.split_step(ws_o)
+    S.split_step(ws_g, steps)
+    assert rel_psi_err(ws_g.psi, ws_o.psi) < 5e-5
+    assert abs(S.total_norm(ws_g) - N0) / N0 < 2e-6
+    assert abs(S.total_energy(ws_g) - O.total_energy(ws_o)) / abs(E0) < 1e-5
