@@ -665,4 +665,43 @@ sbec_status sbec_ddi_potential(sbec_ws* ws, int32_t padded, double* out) {
   SBEC_API_END
 }
 
+sbec_status sbec_profile_enable(sbec_ws* ws, int32_t enable) {
+  SBEC_API_BEGIN
+  E(ws).sync();
+  E(ws).prof.enable(enable != 0);
+  SBEC_API_END
+}
+
+sbec_status sbec_profile_read(sbec_ws* ws, sbec_kernel_stat* out, int32_t max, int32_t* n) {
+  SBEC_API_BEGIN
+  const auto& st = E(ws).prof.read();
+  int32_t i = 0;
+  for (const auto& kv : st) {
+    if (out && i < max) {
+      std::memset(out[i].name, 0, sizeof(out[i].name));
+      std::strncpy(out[i].name, kv.first.c_str(), sizeof(out[i].name) - 1);
+      out[i].launches = kv.second.launches;
+      out[i].ms = kv.second.ms;
+      out[i].bytes = kv.second.bytes;
+    }
+    ++i;
+  }
+  if (n) *n = i;
+  SBEC_API_END
+}
+
+sbec_status sbec_launch_count(sbec_ws* ws, int64_t* n) {
+  SBEC_API_BEGIN
+  need(n, "n");
+  *n = E(ws).prof.total_launches();
+  SBEC_API_END
+}
+
+sbec_status sbec_ws_stream(sbec_ws* ws, void** stream) {
+  SBEC_API_BEGIN
+  need(stream, "stream");
+  *stream = (void*)E(ws).stream();
+  SBEC_API_END
+}
+
 }  // extern "C"

@@ -74,6 +74,39 @@ __device__ __forceinline__ float2 cis_(float x) {
   return mk<float>(c, s);
 }
 
+// x * (wh + wl) where wh + wl is a unit complex number split into a float head
+// and tail: the tail term removes the systematic magnitude error of the rounded
+// head, so FP32 products with fixed twiddles / phases round without bias.
+__device__ __forceinline__ float2 cmul_comp(float2 x, float2 wh, float2 wl) {
+  const float sr = fmaf(x.x, wl.x, -x.y * wl.y);
+  const float si = fmaf(x.x, wl.y, x.y * wl.x);
+  return mk<float>(fmaf(x.x, wh.x, fmaf(-x.y, wh.y, sr)), fmaf(x.x, wh.y, fmaf(x.y, wh.x, si)));
+}
+__device__ __forceinline__ double2 cmul_comp(double2 x, double2 wh, double2) { return x * wh; }
+
+// Twiddle / phase table: head values and (FP32 only) tails.
+template <typename R>
+struct Tw {
+  const cplx<R>* hi;
+  const cplx<R>* lo;
+};
+
+template <typename R>
+__device__ __forceinline__ cplx<R> tw_mul(cplx<R> x, const Tw<R>& t, int idx, bool conj_w) {
+  cplx<R> w = __ldg(t.hi + idx);
+  if constexpr (sizeof(R) == 4) {
+    cplx<R> wl = __ldg(t.lo + idx);
+    if (conj_w) {
+      w.y = -w.y;
+      wl.y = -wl.y;
+    }
+    return cmul_comp(x, w, wl);
+  } else {
+    if (conj_w) w.y = -w.y;
+    return x * w;
+  }
+}
+
 template <typename R>
 __device__ __forceinline__ cplx<R> ldg(const cplx<R>* p) {
   return __ldg(p);

@@ -3,11 +3,95 @@
 
 #include <cuda_runtime.h>
 
+#include <map>
 #include <memory>
+#include <string>
+#include <vector>
 
 #include "sbec_setup.h"
 
 namespace sbec {
+
+void cuda_check(cudaError_t e, const char* what);
+
+// Per-kernel-category launch counts and (when enabled) CUDA-event durations on
+// the workspace stream; the counterpart of the reference's @timeit_debug
+// substep timers (src/split_step.jl:15-131, src/SpinorBEC.jl:175-186).
+class Profiler {
+ public:
+  struct Stat {
+    long long launches = 0;
+    double ms = 0.0;
+    double bytes = 0.0;  // algorithmic bytes summed over timed launches
+  };
+  ~Profiler() { release(); }
+  void enable(bool on) {
+    drain();
+    enabled_ = on;
+    stats_.clear();
+  }
+  bool enabled() const { return enabled_; }
+  long long total_launches() const { return total_; }
+  void begin(cudaStream_t s) {
+    if (!enabled_) return;
+    cur_ = get_event();
+    cuda_check(cudaEventRecord(cur_, s), "cudaEventRecord");
+  }
+  void end(cudaStream_t s, const char* name, double bytes) {
+    ++total_;
+    if (!enabled_) return;
+    cudaEvent_t stop = get_event();
+    cuda_check(cudaEventRecord(stop, s), "cudaEventRecord");
+    pending_.push_back({name, cur_, stop, bytes});
+    if (pending_.size() > 4000) drain();
+  }
+  const std::map<std::string, Stat>& read() {
+    drain();
+    return stats_;
+  }
+
+ private:
+  struct Pending {
+    std::string name;
+    cudaEvent_t a, b;
+    double bytes;
+  };
+  cudaEvent_t get_event() {
+    if (free_.empty()) {
+      cudaEvent_t e;
+      cuda_check(cudaEventCreate(&e), "cudaEventCreate");
+      all_.push_back(e);
+      return e;
+    }
+    cudaEvent_t e = free_.back();
+    free_.pop_back();
+    return e;
+  }
+  void drain() {
+    for (auto& p : pending_) {
+      cuda_check(cudaEventSynchronize(p.b), "cudaEventSynchronize");
+      float ms = 0.f;
+      cuda_check(cudaEventElapsedTime(&ms, p.a, p.b), "cudaEventElapsedTime");
+      Stat& st = stats_[p.name];
+      st.launches += 1;
+      st.ms += ms;
+      st.bytes += p.bytes;
+      free_.push_back(p.a);
+      free_.push_back(p.b);
+    }
+    pending_.clear();
+  }
+  void release() {
+    for (auto e : all_) cudaEventDestroy(e);
+    all_.clear();
+  }
+  bool enabled_ = false;
+  long long total_ = 0;
+  cudaEvent_t cur_ = nullptr;
+  std::vector<Pending> pending_;
+  std::vector<cudaEvent_t> free_, all_;
+  std::map<std::string, Stat> stats_;
+};
 
 // Buffers a driver can save psi into (adaptive loops, convergence checks).
 enum Slot { kPsi = 0, kSlotA = 1, kSlotB = 2, kSlotC = 3, kNumSlots = 4 };
@@ -18,6 +102,7 @@ class EngineBase {
   virtual ~EngineBase() = default;
   const Setup& setup() const { return s_; }
   cudaStream_t stream() const { return stream_; }
+  Profiler prof;
 
   double zeeman_p = 0.0, zeeman_q = 0.0;
   double t = 0.0;
@@ -54,7 +139,5 @@ class EngineBase {
 
 std::unique_ptr<EngineBase> make_engine_f64(const Setup& s);
 std::unique_ptr<EngineBase> make_engine_f32(const Setup& s);
-
-void cuda_check(cudaError_t e, const char* what);
 
 }  // namespace sbec

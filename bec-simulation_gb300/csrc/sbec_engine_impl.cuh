@@ -18,39 +18,42 @@ namespace sbec {
 // ---------------------------------------------------------------------------
 // Tile shapes
 // ---------------------------------------------------------------------------
+// Tiles are kept small (about 64 threads) so that the 2-D grids of a single solve
+// (e.g. 768 lines of 256) still spread over all 152 SMs; strided tiles are at
+// least one 32-byte sector wide so every global access moves whole sectors.
 template <typename R, int N>
 constexpr int x_lines_per_block() {
   constexpr int tpl = N / FftPlan<N>::E;
-  constexpr int target = (sizeof(R) == 8 ? 2048 : 4096) / N;
-  constexpr int lpb = target < 1 ? 1 : target;
-  return lpb * tpl > 1024 ? 1024 / tpl : lpb;
+  constexpr int lpb = 64 / tpl;
+  return lpb < 1 ? 1 : lpb;
 }
 
 template <typename R, int N>
 constexpr int strided_width() {
   constexpr int tpl = N / FftPlan<N>::E;
-  constexpr int smem_budget = 96 * 1024;
-  int w = sizeof(R) == 8 ? 16 : 32;
-  while (w > 1 && (w * tpl > 1024 || (long)w * N * (int)sizeof(cplx<R>) > smem_budget)) w /= 2;
+  constexpr int sector = 32 / (int)sizeof(cplx<R>);
+  int w = 64 / tpl;
+  if (w < sector) w = sector;
+  while (w > 1 && (w * tpl > 1024 || (long)w * N * (int)sizeof(cplx<R>) > 96 * 1024)) w /= 2;
   return w;
 }
 
 template <typename R, int MH>
 constexpr int ddi_x_rows_per_block() {
   constexpr int tpl = MH / FftPlan<MH>::E;
-  constexpr int smem_budget = 96 * 1024;
-  int lpb = 8;
-  while (lpb > 1 && (3 * lpb * tpl > 1024 || (long)3 * lpb * (2 * MH + 1) * (int)sizeof(cplx<R>) > smem_budget))
-    lpb /= 2;
+  int lpb = 64 / (3 * tpl);
+  if (lpb < 1) lpb = 1;
+  while (lpb > 1 && (long)3 * lpb * (2 * MH + 1) * (int)sizeof(cplx<R>) > 96 * 1024) lpb /= 2;
   return lpb;
 }
 
 template <typename R, int M>
 constexpr int ddi_last_width() {
   constexpr int tpl = M / FftPlan<M>::E;
-  constexpr int smem_budget = 100 * 1024;
-  int w = sizeof(R) == 8 ? 8 : 16;
-  while (w > 1 && (3 * w * tpl > 1024 || (long)3 * w * M * (int)sizeof(cplx<R>) > smem_budget)) w /= 2;
+  constexpr int sector = 32 / (int)sizeof(cplx<R>);
+  int w = 64 / (3 * tpl);
+  if (w < sector) w = sector;
+  while (w > 1 && (3 * w * tpl > 1024 || (long)3 * w * M * (int)sizeof(cplx<R>) > 100 * 1024)) w /= 2;
   return w;
 }
 
@@ -116,8 +119,10 @@ class Engine final : public EngineBase {
     psi_[kPsi] = alloc<cplx<R>>(nc_);
     V_ = alloc<R>(N_);
     cuda_check(cudaMemsetAsync(V_, 0, sizeof(R) * N_, stream_), "memset V");
-    for (int a = 0; a < s_.ndim; ++a) ptab_[a] = alloc<cplx<R>>(s_.n[a]);
-    for (int a = s_.ndim; a < 3; ++a) ptab_[a] = nullptr;
+    for (int a = 0; a < s_.ndim; ++a) {
+      ptab_[a] = alloc<cplx<R>>(s_.n[a]);
+      ptab_lo_[a] = sizeof(R) == 4 ? alloc<cplx<R>>(s_.n[a]) : nullptr;
+    }
     for (int a = 0; a < s_.ndim; ++a) twiddle(s_.n[a]);
     partials_ = alloc<double>((size_t)kMaxBlocks * 16);
     results_ = alloc<double>(64);
@@ -191,8 +196,9 @@ class Engine final : public EngineBase {
     } else {
       double* tmp = reinterpret_cast<double*>(stage_);
       cuda_check(cudaMemcpyAsync(tmp, host, sizeof(double) * N_, cudaMemcpyHostToDevice, stream_), "V upload");
+      pb();
       k_real_from_f64<R><<<grid_for(N_), 256, 0, stream_>>>(tmp, V_, N_);
-      launch_check("k_real_from_f64");
+      done("convert", 12.0 * N_);
     }
     sync();
   }
@@ -258,16 +264,18 @@ class Engine final : public EngineBase {
 
   void normalize() override {
     comp_norms_async(psi_[kPsi]);
+    pb();
     k_normalize_apply<R><<<grid_for(nc_), 256, 0, stream_>>>(psi_[kPsi], N_, s_.D, results_ + 1, s_.dV);
-    launch_check("k_normalize_apply");
+    done("normalize", 2.0 * (double)sizeof(cplx<R>) * nc_);
   }
 
   void scale_components(const double* w) override {
     std::memcpy(host_res_, w, sizeof(double) * s_.D);
     cuda_check(cudaMemcpyAsync(results_ + 32, host_res_, sizeof(double) * s_.D, cudaMemcpyHostToDevice, stream_),
                "weights");
+    pb();
     k_scale_comp<R><<<grid_for(nc_), 256, 0, stream_>>>(psi_[kPsi], N_, s_.D, results_ + 32);
-    launch_check("k_scale_comp");
+    done("elementwise", 2.0 * (double)sizeof(cplx<R>) * nc_);
     sync();
   }
 
@@ -294,8 +302,9 @@ class Engine final : public EngineBase {
     {
       PhaseTableArgs g = phase_geom(0.0, false);
       const int nb = red_blocks(nc_);
+      pb();
       k_kinetic_sum<R><<<nb, kRedThreads, 0, stream_>>>(scr, N_, s_.D, g, partials_);
-      launch_check("k_kinetic_sum");
+      done("reduce", (double)sizeof(cplx<R>) * nc_);
       finish<1>(nb, false, 0);
     }
     comp_norms_async(psi_[kPsi]);  // -> results_[1 .. D+1]
@@ -313,8 +322,9 @@ class Engine final : public EngineBase {
       SBEC_SWITCH_D(s_.D, launch_spin_density_d, spin3_);
       ddi_conv(0, spin3_, phi_per_);
       const int nb = red_blocks(N_);
+      pb();
       k_dot3<R><<<nb, kRedThreads, 0, stream_>>>(phi_per_, spin3_, N_, partials_);
-      launch_check("k_dot3");
+      done("reduce", 6.0 * (double)sizeof(R) * N_);
       finish<1>(nb, false, 31);
     }
     fetch(32);
@@ -340,8 +350,9 @@ class Engine final : public EngineBase {
 
   double l2_change(int a, int b) override {
     const int nb = red_blocks(nc_);
+    pb();
     k_l2_change<R><<<nb, kRedThreads, 0, stream_>>>(slot(a), slot(b), nc_, partials_);
-    launch_check("k_l2_change");
+    done("reduce", 2.0 * (double)sizeof(cplx<R>) * nc_);
     finish<2>(nb, false, 0);
     fetch(2);
     return host_res_[0] / std::max(host_res_[1], 1e-300);
@@ -349,8 +360,9 @@ class Engine final : public EngineBase {
 
   void max_abs(int a, int b, double* max_a, double* max_diff) override {
     const int nb = red_blocks(nc_);
+    pb();
     k_max_abs<R><<<nb, kRedThreads, 0, stream_>>>(slot(a), b >= 0 ? slot(b) : nullptr, nc_, partials_);
-    launch_check("k_max_abs");
+    done("reduce", (b >= 0 ? 2.0 : 1.0) * (double)sizeof(cplx<R>) * nc_);
     finish<2>(nb, true, 0);
     fetch(2);
     *max_a = host_res_[0];
@@ -360,8 +372,9 @@ class Engine final : public EngineBase {
   double ddi_phi_max() override {
     if (!s_.ddi) return 0.0;
     const int nb = red_blocks(3 * N_);
+    pb();
     k_max_abs_real<R><<<nb, kRedThreads, 0, stream_>>>(s_.padded ? phi_per_ : phi3_, 3 * N_, partials_);
-    launch_check("k_max_abs_real");
+    done("reduce", 3.0 * (double)sizeof(R) * N_);
     finish<1>(nb, true, 0);
     fetch(1);
     return host_res_[0];
@@ -405,6 +418,11 @@ class Engine final : public EngineBase {
   }
 
   void launch_check(const char* what) { cuda_check(cudaGetLastError(), what); }
+  void pb() { prof.begin(stream_); }
+  void done(const char* name, double bytes) {
+    cuda_check(cudaGetLastError(), name);
+    prof.end(stream_, name, bytes);
+  }
 
   int grid_for(int64_t n) const {
     const int64_t b = (n + 255) / 256;
@@ -417,8 +435,9 @@ class Engine final : public EngineBase {
 
   template <int K>
   void finish(int nb, bool is_max, int out_off) {
+    pb();
     k_reduce_finish<K><<<1, 32, 0, stream_>>>(partials_, nb, is_max ? 1 : 0, results_ + out_off);
-    launch_check("k_reduce_finish");
+    done("reduce_finish", 8.0 * K * nb);
   }
 
   void fetch(int n) {
@@ -447,8 +466,9 @@ class Engine final : public EngineBase {
     } else {
       cuda_check(cudaMemcpyAsync(stage_, host_psi_, sizeof(double) * 2 * nc_, cudaMemcpyHostToDevice, stream_),
                  "psi upload");
+      pb();
       k_from_f64<R><<<grid_for(nc_), 256, 0, stream_>>>(stage_, psi_[kPsi], nc_);
-      launch_check("k_from_f64");
+      done("convert", (16.0 + (double)sizeof(cplx<R>)) * nc_);
     }
   }
 
@@ -457,8 +477,9 @@ class Engine final : public EngineBase {
       cuda_check(cudaMemcpyAsync(host_psi_, psi_[kPsi], sizeof(double) * 2 * nc_, cudaMemcpyDeviceToHost, stream_),
                  "psi download");
     } else {
+      pb();
       k_to_f64<R><<<grid_for(nc_), 256, 0, stream_>>>(psi_[kPsi], stage_, nc_);
-      launch_check("k_to_f64");
+      done("convert", (16.0 + (double)sizeof(cplx<R>)) * nc_);
       cuda_check(cudaMemcpyAsync(host_psi_, stage_, sizeof(double) * 2 * nc_, cudaMemcpyDeviceToHost, stream_),
                  "psi download");
     }
@@ -471,8 +492,9 @@ class Engine final : public EngineBase {
     } else {
       double* dtmp = reinterpret_cast<double*>(stage_);
       if (3 * N_ > 2 * nc_) fail(SBEC_ERR_INVALID, "staging buffer too small");
+      pb();
       k_real_to_f64<R><<<grid_for(3 * N_), 256, 0, stream_>>>(src, dtmp, 3 * N_);
-      launch_check("k_real_to_f64");
+      done("convert", (8.0 + (double)sizeof(R)) * 3 * N_);
       cuda_check(cudaMemcpyAsync(tmp, dtmp, sizeof(double) * 3 * N_, cudaMemcpyDeviceToHost, stream_), "download");
     }
     sync();
@@ -488,19 +510,30 @@ class Engine final : public EngineBase {
     return host_tmp_;
   }
 
-  // twiddle table W_n^e = exp(-2 pi i e/n), e = 0..n-1 (computed in long double).
-  const cplx<R>* twiddle(int n) {
+  // twiddle table W_n^e = exp(-2 pi i e/n), e = 0..n-1 (computed in long double);
+  // FP32 tables carry the tail (value - rounded head) for compensated products.
+  Tw<R> twiddle(int n) {
     auto it = tw_.find(n);
     if (it != tw_.end()) return it->second;
-    std::vector<cplx<R>> h(n);
+    std::vector<cplx<R>> h(n), l(n);
     for (int e = 0; e < n; ++e) {
       const long double ang = -2.0L * 3.141592653589793238462643383279502884L * (long double)e / (long double)n;
-      h[e] = mk<R>((R)std::cos(ang), (R)std::sin(ang));
+      const long double c = std::cos(ang), sn = std::sin(ang);
+      h[e] = mk<R>((R)c, (R)sn);
+      l[e] = mk<R>((R)(c - (long double)h[e].x), (R)(sn - (long double)h[e].y));
     }
-    cplx<R>* d = alloc<cplx<R>>(n);
-    upload(d, h.data(), n);
-    tw_[n] = d;
-    return d;
+    Tw<R> t{};
+    cplx<R>* dh = alloc<cplx<R>>(n);
+    upload(dh, h.data(), n);
+    t.hi = dh;
+    t.lo = nullptr;
+    if (sizeof(R) == 4) {
+      cplx<R>* dl = alloc<cplx<R>>(n);
+      upload(dl, l.data(), n);
+      t.lo = dl;
+    }
+    tw_[n] = t;
+    return t;
   }
 
   PhaseTableArgs phase_geom(double dtv, bool it) const {
@@ -520,8 +553,14 @@ class Engine final : public EngineBase {
     if (dtv == phase_dt_ && (it ? 1 : 0) == phase_itp_) return;
     PhaseTableArgs g = phase_geom(dtv, it);
     dim3 grid(8, s_.ndim);
-    k_phase_tables<R><<<grid, 256, 0, stream_>>>(ptab_[0], ptab_[1], ptab_[2], g);
-    launch_check("k_phase_tables");
+    PhaseOut<R> po{};
+    for (int a = 0; a < 3; ++a) {
+      po.hi[a] = ptab_[a];
+      po.lo[a] = ptab_lo_[a];
+    }
+    pb();
+    k_phase_tables<R><<<grid, 256, 0, stream_>>>(po, g);
+    done("phase_tables", 0.0);
     phase_dt_ = dtv;
     phase_itp_ = it ? 1 : 0;
   }
@@ -530,7 +569,8 @@ class Engine final : public EngineBase {
     PhaseRef<R> p{};
     p.ndim = s_.ndim;
     for (int a = 0; a < 3; ++a) {
-      p.tab[a] = ptab_[a];
+      p.tab[a].hi = ptab_[a];
+      p.tab[a].lo = ptab_lo_[a];
       p.n[a] = s_.n[a];
     }
     return p;
@@ -546,8 +586,9 @@ class Engine final : public EngineBase {
     static const bool once = (set_smem(kern, smem), true);
     (void)once;
     const int64_t blocks = (n_lines + LPB - 1) / LPB;
+    pb();
     kern<<<(unsigned)blocks, LPB * TPL, smem, stream_>>>(data, n_lines, mode, phase_ref(), twiddle(NN));
-    launch_check("k_fft_x");
+    done(mode == 2 ? "fft_x_kinetic" : "fft_x", 2.0 * (double)sizeof(cplx<R>) * (double)n_lines * NN);
   }
 
   template <int NN>
@@ -560,9 +601,10 @@ class Engine final : public EngineBase {
     static const bool once = (set_smem(kern, smem), true);
     (void)once;
     dim3 grid((unsigned)((inner + W - 1) / W), (unsigned)outer);
+    pb();
     kern<<<grid, W * TPL, smem, stream_>>>(data, S, inner, outer_stride, n_in, n_out, mode, phase_ref(),
                                            twiddle(NN));
-    launch_check("k_fft_strided");
+    done(mode == 2 ? "fft_last_kinetic" : "fft_strided", (double)sizeof(cplx<R>) * (double)(n_in + n_out) * (double)inner * (double)outer);
   }
 
   // Full spatial FFT of a D-component buffer: forward only (kinetic=false), or the
@@ -619,9 +661,10 @@ class Engine final : public EngineBase {
     static const bool once = (set_smem(kern, smem), true);
     (void)once;
     const int64_t rows = (int64_t)g.ny * g.nz;
+    pb();
     kern<<<(unsigned)((rows + LPB - 1) / LPB), 3 * LPB * TPL, smem, stream_>>>(f3, N_, spec, g, phi3, twiddle(MH),
                                                                                twiddle(2 * MH));
-    launch_check("k_ddi_r2c_x");
+    done("ddi_r2c_x", (3.0 * (double)sizeof(R) * g.nx + 3.0 * (double)sizeof(cplx<R>) * g.Hx) * (double)rows);
   }
 
   template <int MH>
@@ -633,9 +676,10 @@ class Engine final : public EngineBase {
     static const bool once = (set_smem(kern, smem), true);
     (void)once;
     const int64_t rows = (int64_t)g.ny * g.nz;
+    pb();
     kern<<<(unsigned)((rows + LPB - 1) / LPB), 3 * LPB * TPL, smem, stream_>>>(spec, g, phi3, N_, twiddle(MH),
                                                                                twiddle(2 * MH));
-    launch_check("k_ddi_c2r_x");
+    done("ddi_c2r_x", (3.0 * (double)sizeof(R) * g.nx + 3.0 * (double)sizeof(cplx<R>) * g.Hx) * (double)rows);
   }
 
   template <int M>
@@ -646,9 +690,10 @@ class Engine final : public EngineBase {
     auto kern = k_ddi_last<R, M, W>;
     static const bool once = (set_smem(kern, smem), true);
     (void)once;
+    pb();
     kern<<<(unsigned)((inner + W - 1) / W), 3 * W * TPL, smem, stream_>>>(spec, g, S, inner, n_in, n_out,
                                                                          twiddle(M));
-    launch_check("k_ddi_last");
+    done("ddi_last", 3.0 * (double)sizeof(cplx<R>) * (double)(n_in + n_out) * (double)inner);
   }
 
   // Φ = C_dd Q * F on convolution grid `kind` (0 periodic, 1 zero padded).
@@ -684,12 +729,12 @@ class Engine final : public EngineBase {
     a.c0 = (R)s_.c0;
     a.c1 = (R)s_.c1;
     a.c_lhy = (R)s_.c_lhy;
-    zeeman_factors(tau_d, it, a.zee);
+    zeeman_factors(tau_d, it, a.zee, a.zee_lo);
     return a;
   }
 
   // Zeeman factors (src/propagators.jl:95-116): cis(-E_c tau) or exp(-(E_c - min E) tau).
-  void zeeman_factors(double tau, bool it, cplx<R>* out) const {
+  void zeeman_factors(double tau, bool it, cplx<R>* out, cplx<R>* out_lo) const {
     const int D = s_.D, F = s_.F;
     double E[kMaxD];
     double emin = INFINITY;
@@ -699,12 +744,17 @@ class Engine final : public EngineBase {
       emin = std::min(emin, E[c]);
     }
     for (int c = 0; c < D; ++c) {
+      double re, im;
       if (it) {
-        out[c] = mk<R>((R)std::exp(-((E[c] - emin) * tau)), (R)0);
+        re = std::exp(-((E[c] - emin) * tau));
+        im = 0.0;
       } else {
         const double arg = -(E[c] * tau);
-        out[c] = mk<R>((R)std::cos(arg), (R)std::sin(arg));
+        re = std::cos(arg);
+        im = std::sin(arg);
       }
+      out[c] = mk<R>((R)re, (R)im);
+      out_lo[c] = mk<R>((R)(re - (double)out[c].x), (R)(im - (double)out[c].y));
     }
   }
 
@@ -721,14 +771,15 @@ class Engine final : public EngineBase {
     a.c0 = (R)s_.c0;
     a.c_lhy = (R)s_.c_lhy;
     a.eps = sizeof(R) == 8 ? 1e-17 : 1e-8;
-    zeeman_factors(tau_d, it, a.zee);
+    zeeman_factors(tau_d, it, a.zee, a.zee_lo);
     return a;
   }
 
   template <int D>
   void launch_potential_d(const PotArgs<R>& a) {
+    pb();
     k_potential<R, D><<<(unsigned)((N_ + 255) / 256), 256, 0, stream_>>>(a, st_);
-    launch_check("k_potential");
+    done("potential", (2.0 * (double)sizeof(cplx<R>) * D + (double)sizeof(R) * (1 + (a.phi ? 3 : 0) + (a.spin_out ? 3 : 0))) * (double)N_);
   }
   void launch_potential(const PotArgs<R>& a) { SBEC_SWITCH_D(s_.D, launch_potential_d, a); }
 
@@ -739,34 +790,39 @@ class Engine final : public EngineBase {
     auto kern = k_tensor<R, D>;
     static const bool once = (set_smem(kern, smem), true);
     (void)once;
+    pb();
     kern<<<(unsigned)((N_ + T - 1) / T), T, smem, stream_>>>(a);
-    launch_check("k_tensor");
+    done("tensor", (2.0 * (double)sizeof(cplx<R>) * D + (double)sizeof(R)) * (double)N_);
   }
   void launch_tensor(const TensorArgs<R>& a) { SBEC_SWITCH_D(s_.D, launch_tensor_d, a); }
 
   template <int D>
   void launch_spin_density_d(R* out) {
+    pb();
     k_spin_density<R, D><<<(unsigned)((N_ + 255) / 256), 256, 0, stream_>>>(psi_[kPsi], N_, st_, out);
-    launch_check("k_spin_density");
+    done("spin_density", ((double)sizeof(cplx<R>) * D + 3.0 * (double)sizeof(R)) * (double)N_);
   }
 
   template <int D>
   void launch_energy_local_d(int nb) {
+    pb();
     k_energy_local<R, D><<<nb, kRedThreads, 0, stream_>>>(psi_[kPsi], N_, V_, st_, partials_);
-    launch_check("k_energy_local");
+    done("reduce", ((double)sizeof(cplx<R>) * D + (double)sizeof(R)) * (double)N_);
   }
 
   template <int D>
   void launch_tensor_energy_d(int nb) {
+    pb();
     k_tensor_energy<R, D><<<nb, kRedThreads, 0, stream_>>>(psi_[kPsi], N_, pairs_, pcg_, (int)s_.pair_a.size(), gA_,
                                                           (int)s_.gA.size(), partials_);
-    launch_check("k_tensor_energy");
+    done("reduce", (double)sizeof(cplx<R>) * D * (double)N_);
   }
 
   template <int D>
   void launch_comp_norms_d(const cplx<R>* buf, int nb) {
+    pb();
     k_comp_norms<R, D><<<nb, kRedThreads, 0, stream_>>>(buf, N_, partials_);
-    launch_check("k_comp_norms");
+    done("reduce", (double)sizeof(cplx<R>) * D * (double)N_);
   }
 
   // per-component sums into results_[1..D], NaN count into results_[D+1]
@@ -790,7 +846,8 @@ class Engine final : public EngineBase {
   R* V_ = nullptr;
   R* tmp3_ = nullptr;
   cplx<R>* ptab_[3] = {nullptr, nullptr, nullptr};
-  std::map<int, cplx<R>*> tw_;
+  cplx<R>* ptab_lo_[3] = {nullptr, nullptr, nullptr};
+  std::map<int, Tw<R>> tw_;
   double* partials_ = nullptr;
   double* results_ = nullptr;
   double* host_res_ = nullptr;

@@ -44,16 +44,32 @@ __device__ __forceinline__ cplx<R> twmul(cplx<R> x, int k) {
   const int j = k * (16 / N);
   if (j == 0) return x;
   if (j == 4) return SIGN < 0 ? mul_mi(x) : mul_i(x);
-  if (j == 2) {
-    const R h = (R)0.70710678118654752440;
-    return SIGN < 0 ? mk<R>(h * (x.x + x.y), h * (x.y - x.x)) : mk<R>(h * (x.x - x.y), h * (x.y + x.x));
+  if (j == 2 || j == 6) {
+    R a, b;  // x * (±1 + SIGN i) before the 1/sqrt(2) scale
+    if (j == 2) {
+      a = SIGN < 0 ? x.x + x.y : x.x - x.y;
+      b = SIGN < 0 ? x.y - x.x : x.y + x.x;
+    } else {
+      a = SIGN < 0 ? x.y - x.x : -(x.x + x.y);
+      b = SIGN < 0 ? -(x.x + x.y) : x.x - x.y;
+    }
+    if constexpr (sizeof(R) == 4) {
+      const float hh = 0.70710677f, hl = 1.2101617e-08f;  // 1/sqrt(2) = hh + hl
+      return mk<R>(fmaf(a, hl, a * hh), fmaf(b, hl, b * hh));
+    } else {
+      const R h = (R)0.70710678118654752440;
+      return mk<R>(h * a, h * b);
+    }
   }
-  if (j == 6) {
-    const R h = (R)0.70710678118654752440;
-    return SIGN < 0 ? mk<R>(h * (x.y - x.x), -h * (x.x + x.y)) : mk<R>(-h * (x.x + x.y), h * (x.x - x.y));
+  if constexpr (sizeof(R) == 4) {
+    const double c = cos16(j), sn = SIGN * sin16(j);
+    const float2 wh = mk<float>((float)c, (float)sn);
+    const float2 wl = mk<float>((float)(c - (double)wh.x), (float)(sn - (double)wh.y));
+    return cmul_comp(x, wh, wl);
+  } else {
+    const cplx<R> w = mk<R>((R)cos16(j), (R)(SIGN * sin16(j)));
+    return x * w;
   }
-  const cplx<R> w = mk<R>((R)cos16(j), (R)(SIGN * sin16(j)));
-  return x * w;
 }
 
 // In-register DFT of compile-time size N (1, 2, 4, 8, 16) by radix-2 decimation in time.
@@ -85,8 +101,7 @@ __device__ __forceinline__ void dft(cplx<R>* v) {
 
 // One Stockham stage.  tw holds W_N^e = exp(-2*pi*i*e/N), e = 0..N-1 (forward sign).
 template <typename R, int N, int E, int RAD, int SIGN>
-__device__ __forceinline__ void fft_stage(cplx<R>* s, int SI, int SL, int l, int t, int Ns,
-                                          const cplx<R>* __restrict__ tw) {
+__device__ __forceinline__ void fft_stage(cplx<R>* s, int SI, int SL, int l, int t, int Ns, const Tw<R>& tw) {
   constexpr int TPL = N / E;
   constexpr int NBT = E / RAD;
   constexpr int STRIDE = N / RAD;
@@ -105,11 +120,7 @@ __device__ __forceinline__ void fft_stage(cplx<R>* s, int SI, int SL, int l, int
     if (Ns > 1) {
       const int step = jm * (N / (Ns * RAD));
 #pragma unroll
-      for (int r = 1; r < RAD; ++r) {
-        cplx<R> w = __ldg(tw + r * step);
-        if (SIGN > 0) w.y = -w.y;
-        v[b * RAD + r] = v[b * RAD + r] * w;
-      }
+      for (int r = 1; r < RAD; ++r) v[b * RAD + r] = tw_mul<R>(v[b * RAD + r], tw, r * step, SIGN > 0);
     }
     dft<R, RAD, SIGN>(&v[b * RAD]);
     const int base = (j - jm) * RAD + jm;
@@ -120,8 +131,7 @@ __device__ __forceinline__ void fft_stage(cplx<R>* s, int SI, int SL, int l, int
 }
 
 template <typename R, int N, int E, int SIGN, int RAD, int... REST>
-__device__ __forceinline__ void run_stages(cplx<R>* s, int SI, int SL, int l, int t, int Ns,
-                                           const cplx<R>* __restrict__ tw) {
+__device__ __forceinline__ void run_stages(cplx<R>* s, int SI, int SL, int l, int t, int Ns, const Tw<R>& tw) {
   fft_stage<R, N, E, RAD, SIGN>(s, SI, SL, l, t, Ns, tw);
   if constexpr (sizeof...(REST) > 0) run_stages<R, N, E, SIGN, REST...>(s, SI, SL, l, t, Ns * RAD, tw);
 }
@@ -133,7 +143,7 @@ template <int N> struct FftPlan;
     static constexpr int E = EE;                                                                 \
     template <typename R, int SIGN>                                                              \
     static __device__ __forceinline__ void run(cplx<R>* s, int SI, int SL, int l, int t,        \
-                                               const cplx<R>* __restrict__ tw) {                 \
+                                               const Tw<R>& tw) {                                \
       run_stages<R, NN, EE, SIGN, __VA_ARGS__>(s, SI, SL, l, t, 1, tw);                          \
     }                                                                                            \
   };
@@ -154,8 +164,7 @@ SBEC_PLAN(4096, 16, 16, 16, 16)
 // Transform every line of a shared-memory tile (all threads of the block participate).
 // Caller must __syncthreads() after filling the tile; the function ends synchronised.
 template <typename R, int N, int SIGN>
-__device__ __forceinline__ void fft_tile(cplx<R>* s, int SI, int SL, int l, int t,
-                                         const cplx<R>* __restrict__ tw) {
+__device__ __forceinline__ void fft_tile(cplx<R>* s, int SI, int SL, int l, int t, const Tw<R>& tw) {
   FftPlan<N>::template run<R, SIGN>(s, SI, SL, l, t, tw);
 }
 

@@ -25,10 +25,17 @@ struct PhaseTableArgs {
 };
 
 template <typename R>
-__global__ void k_phase_tables(cplx<R>* tab0, cplx<R>* tab1, cplx<R>* tab2, PhaseTableArgs a) {
+struct PhaseOut {
+  cplx<R>* hi[3];
+  cplx<R>* lo[3];
+};
+
+template <typename R>
+__global__ void k_phase_tables(PhaseOut<R> out, PhaseTableArgs a) {
   const int axis = blockIdx.y;
   if (axis >= a.ndim) return;
-  cplx<R>* tab = axis == 0 ? tab0 : (axis == 1 ? tab1 : tab2);
+  cplx<R>* tab = out.hi[axis];
+  cplx<R>* tlo = out.lo[axis];
   const int n = a.n[axis];
   for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < n; m += gridDim.x * blockDim.x) {
     const int idx = m < (n + 1) / 2 ? m : m - n;
@@ -45,13 +52,15 @@ __global__ void k_phase_tables(cplx<R>* tab0, cplx<R>* tab1, cplx<R>* tab2, Phas
       re *= a.scale;
       im *= a.scale;
     }
-    tab[m] = mk<R>((R)re, (R)im);
+    const cplx<R> h = mk<R>((R)re, (R)im);
+    tab[m] = h;
+    if (tlo) tlo[m] = mk<R>((R)(re - (double)h.x), (R)(im - (double)h.y));
   }
 }
 
 template <typename R>
 struct PhaseRef {
-  const cplx<R>* tab[3];
+  Tw<R> tab[3];
   int n[3];
   int ndim;
 };
@@ -62,8 +71,7 @@ struct PhaseRef {
 // ---------------------------------------------------------------------------
 template <typename R, int N, int LPB>
 __global__ void __launch_bounds__(LPB * (N / FftPlan<N>::E))
-k_fft_x(cplx<R>* __restrict__ data, int64_t n_lines, int mode, PhaseRef<R> ph,
-        const cplx<R>* __restrict__ tw) {
+k_fft_x(cplx<R>* __restrict__ data, int64_t n_lines, int mode, PhaseRef<R> ph, Tw<R> tw) {
   constexpr int TPL = N / FftPlan<N>::E;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);
@@ -79,7 +87,7 @@ k_fft_x(cplx<R>* __restrict__ data, int64_t n_lines, int mode, PhaseRef<R> ph,
   } else {
     fft_tile<R, N, -1>(s, 1, N, l, t, tw);
     if (mode == 2) {
-      for (int f = tid; f < LPB * N; f += blockDim.x) s[f] = s[f] * __ldg(ph.tab[0] + (f % N));
+      for (int f = tid; f < LPB * N; f += blockDim.x) s[f] = tw_mul<R>(s[f], ph.tab[0], f % N, false);
       __syncthreads();
       fft_tile<R, N, +1>(s, 1, N, l, t, tw);
     }
@@ -97,11 +105,12 @@ k_fft_x(cplx<R>* __restrict__ data, int64_t n_lines, int mode, PhaseRef<R> ph,
 template <typename R, int N, int W>
 __global__ void __launch_bounds__(W * (N / FftPlan<N>::E))
 k_fft_strided(cplx<R>* __restrict__ data, int64_t S, int64_t inner, int64_t outer_stride, int n_in,
-              int n_out, int mode, PhaseRef<R> ph, const cplx<R>* __restrict__ tw) {
+              int n_out, int mode, PhaseRef<R> ph, Tw<R> tw) {
   constexpr int TPL = N / FftPlan<N>::E;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);
   __shared__ cplx<R> inner_ph[W];
+  __shared__ int inner_idx[W][2];
   const int tid = threadIdx.x;
   const int64_t i0 = (int64_t)blockIdx.x * W;
   const int nw = (int)min((int64_t)W, inner - i0);
@@ -114,10 +123,12 @@ k_fft_strided(cplx<R>* __restrict__ data, int64_t S, int64_t inner, int64_t oute
     // lower-axis factors of the kinetic phase for this line
     int64_t pos = i0 + tid;
     cplx<R> f = mk<R>(1, 0);
+    inner_idx[tid][1] = -1;
     for (int a = 0; a < ph.ndim - 1; ++a) {
       const int ia = (int)(pos % ph.n[a]);
       pos /= ph.n[a];
-      f = f * __ldg(ph.tab[a] + ia);
+      inner_idx[tid][a] = ia;
+      f = f * __ldg(ph.tab[a].hi + ia);
     }
     inner_ph[tid] = f;
   }
@@ -128,10 +139,17 @@ k_fft_strided(cplx<R>* __restrict__ data, int64_t S, int64_t inner, int64_t oute
   } else {
     fft_tile<R, N, -1>(s, W, 1, w, t, tw);
     if (mode == 2) {
-      const cplx<R>* last = ph.tab[ph.ndim - 1];
+      const Tw<R> last = ph.tab[ph.ndim - 1];
       for (int f = tid; f < W * N; f += blockDim.x) {
         const int i = f / W, ww = f % W;
-        s[f] = s[f] * (inner_ph[ww] * __ldg(last + i));
+        if constexpr (sizeof(R) == 8) {
+          s[f] = s[f] * (inner_ph[ww] * __ldg(last.hi + i));
+        } else {
+          // FP32: one compensated product per axis factor (unbiased rounding)
+          cplx<R> v = tw_mul<R>(s[f], ph.tab[0], inner_idx[ww][0], false);
+          if (ph.ndim == 3) v = tw_mul<R>(v, ph.tab[1], inner_idx[ww][1], false);
+          s[f] = tw_mul<R>(v, last, i, false);
+        }
       }
       __syncthreads();
       fft_tile<R, N, +1>(s, W, 1, w, t, tw);
@@ -195,6 +213,22 @@ __device__ __forceinline__ void ddi_contract(cplx<R>& fx, cplx<R>& fy, cplx<R>& 
 
 __device__ __forceinline__ int freq_index(int m, int M) { return m < (M + 1) / 2 ? m : m - M; }
 
+// C2R pre-processing for a half spectrum X[0..MH]: returns 2 Z_k with
+// Z_k = E_k + i O_k, E_k = (X_k + conj X_{MH-k})/2, O_k = (X_k - conj X_{MH-k}) W^{-k}/2.
+// Like FFTW's / pocketfft's c2r, only the real parts of the DC and Nyquist
+// entries are used (their imaginary parts are dropped); the DDI spectrum at the
+// x-Nyquist plane is not Hermitian in (ky, kz) because Q_xy, Q_xz are odd there.
+template <typename R>
+__device__ __forceinline__ cplx<R> c2r_pre(const cplx<R>* X, int k, int MH, const Tw<R>& tw_full) {
+  cplx<R> Xk = X[k];
+  cplx<R> Xc = conj(X[MH - k]);
+  if (k == 0) {
+    Xk.y = 0;
+    Xc.y = 0;
+  }
+  return (Xk + Xc) + mul_i(tw_mul<R>(Xk - Xc, tw_full, k, true));
+}
+
 // R2C along x of the 3 real fields, via a complex FFT of length MH = Mx/2 on
 // z[j] = f[2j] + i f[2j+1] followed by the split X[k] = E_k + W_Mx^k O_k.
 // Rows (y < ny, z < nz) only; output row (y, z) at spectrum row y + My*z.
@@ -203,8 +237,7 @@ __device__ __forceinline__ int freq_index(int m, int M) { return m < (M + 1) / 2
 template <typename R, int MH, int LPB>
 __global__ void __launch_bounds__(3 * LPB * (MH / FftPlan<MH>::E))
 k_ddi_r2c_x(const R* __restrict__ f3, int64_t field_n, cplx<R>* __restrict__ spec, DdiGeom g,
-            R* __restrict__ phi3, const cplx<R>* __restrict__ tw_half,
-            const cplx<R>* __restrict__ tw_full) {
+            R* __restrict__ phi3, Tw<R> tw_half, Tw<R> tw_full) {
   constexpr int TPL = MH / FftPlan<MH>::E;
   constexpr int NL = 3 * LPB;  // lines in the tile: field-major
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -236,8 +269,7 @@ k_ddi_r2c_x(const R* __restrict__ f3, int64_t field_n, cplx<R>* __restrict__ spe
     const cplx<R> Zc = conj(s[line * MH + ((MH - k) % MH)]);
     const cplx<R> E = (R)0.5 * (Zk + Zc);
     const cplx<R> O = (R)0.5 * mul_mi(Zk - Zc);
-    const cplx<R> w = __ldg(tw_full + (k % (2 * MH)));
-    xs[f] = (k == MH) ? (E - O) : E + w * O;
+    xs[f] = (k == MH) ? (E - O) : E + tw_mul<R>(O, tw_full, k % (2 * MH), false);
   }
   __syncthreads();
   if (g.ndim > 1) {
@@ -263,10 +295,7 @@ k_ddi_r2c_x(const R* __restrict__ f3, int64_t field_n, cplx<R>* __restrict__ spe
   // C2R: Z_k = (X_k + conj X_{MH-k}) + i (X_k - conj X_{MH-k}) W_Mx^{-k}, k < MH
   for (int f = tid; f < NL * MH; f += blockDim.x) {
     const int line = f / MH, k = f % MH;
-    const cplx<R> Xk = xs[line * (MH + 1) + k];
-    const cplx<R> Xc = conj(xs[line * (MH + 1) + (MH - k)]);
-    const cplx<R> w = conj(__ldg(tw_full + k));
-    s[f] = (Xk + Xc) + mul_i((Xk - Xc) * w);
+    s[f] = c2r_pre(xs + line * (MH + 1), k, MH, tw_full);
   }
   __syncthreads();
   fft_tile<R, MH, +1>(s, 1, MH, l, t, tw_half);
@@ -285,7 +314,7 @@ k_ddi_r2c_x(const R* __restrict__ f3, int64_t field_n, cplx<R>* __restrict__ spe
 template <typename R, int MH, int LPB>
 __global__ void __launch_bounds__(3 * LPB * (MH / FftPlan<MH>::E))
 k_ddi_c2r_x(const cplx<R>* __restrict__ spec, DdiGeom g, R* __restrict__ phi3, int64_t field_n,
-            const cplx<R>* __restrict__ tw_half, const cplx<R>* __restrict__ tw_full) {
+            Tw<R> tw_half, Tw<R> tw_full) {
   constexpr int TPL = MH / FftPlan<MH>::E;
   constexpr int NL = 3 * LPB;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -309,10 +338,7 @@ k_ddi_c2r_x(const cplx<R>* __restrict__ spec, DdiGeom g, R* __restrict__ phi3, i
   __syncthreads();
   for (int f = tid; f < NL * MH; f += blockDim.x) {
     const int line = f / MH, k = f % MH;
-    const cplx<R> Xk = xs[line * (MH + 1) + k];
-    const cplx<R> Xc = conj(xs[line * (MH + 1) + (MH - k)]);
-    const cplx<R> w = conj(__ldg(tw_full + k));
-    s[f] = (Xk + Xc) + mul_i((Xk - Xc) * w);
+    s[f] = c2r_pre(xs + line * (MH + 1), k, MH, tw_full);
   }
   __syncthreads();
   const int t = tid % TPL, l = tid / TPL;
@@ -334,8 +360,7 @@ k_ddi_c2r_x(const cplx<R>* __restrict__ spec, DdiGeom g, R* __restrict__ phi3, i
 // in the lower axes of the spectrum (kx [, ky]), stride S between elements.
 template <typename R, int M, int W>
 __global__ void __launch_bounds__(3 * W * (M / FftPlan<M>::E))
-k_ddi_last(cplx<R>* __restrict__ spec, DdiGeom g, int64_t S, int64_t inner, int n_in, int n_out,
-           const cplx<R>* __restrict__ tw) {
+k_ddi_last(cplx<R>* __restrict__ spec, DdiGeom g, int64_t S, int64_t inner, int n_in, int n_out, Tw<R> tw) {
   constexpr int TPL = M / FftPlan<M>::E;
   constexpr int NL = 3 * W;   // line index = fld*W + w
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -403,7 +428,41 @@ struct PotArgs {
   R tau_d, tau_s, tau_ddi;
   R c0, c1, c_lhy;
   cplx<R> zee[kMaxD];          // per-component Zeeman factor for diag(tau_d)
+  cplx<R> zee_lo[kMaxD];       // FP32 tails of the Zeeman factors
 };
+
+// psi_c *= exp(-i Veff tau) * zee_c  (real time) or exp(-Veff tau) * zee_c (imaginary time),
+// src/propagators.jl:95-116.  FP64 keeps the reference's product order; FP32 applies
+// the potential phase as psi + psi*(cos x - 1, -sin x) with cos x - 1 = -2 sin^2(x/2):
+// for the small angles of the trap centre cosf(x) rounds to 1 while sinf(x) does not,
+// and a plain product would change |psi| systematically every step.
+template <typename R, int D>
+__device__ __forceinline__ void diag_apply(cplx<R> (&v)[D], R veff, R tau, int itp, const cplx<R>* zee,
+                                           const cplx<R>* zee_lo) {
+  if (itp) {
+    const R e = exp(-veff * tau);
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      if constexpr (sizeof(R) == 8) v[c] = v[c] * (mk<R>(e, (R)0) * zee[c]);
+      else v[c] = cmul_comp(v[c], zee[c], zee_lo[c]) * e;
+    }
+    return;
+  }
+  if constexpr (sizeof(R) == 8) {
+    const cplx<R> base = cis_(-veff * tau);
+#pragma unroll
+    for (int c = 0; c < D; ++c) v[c] = v[c] * (base * zee[c]);
+  } else {
+    const float x = veff * tau;
+    const float sn = sinf(x), sh = sinf(0.5f * x);
+    const float2 w1 = mk<float>(-2.0f * sh * sh, -sn);
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      const float2 z = cmul_comp(v[c], zee[c], zee_lo[c]);
+      v[c] = z + z * w1;
+    }
+  }
+}
 
 template <typename R, int D>
 __device__ __forceinline__ void diag_point(cplx<R> (&v)[D], R Vp, const PotArgs<R>& a) {
@@ -411,14 +470,7 @@ __device__ __forceinline__ void diag_point(cplx<R> (&v)[D], R Vp, const PotArgs<
 #pragma unroll
   for (int c = 0; c < D; ++c) n += abs2(v[c]);
   const R Vint = a.c0 * n + a.c_lhy * n * sqrt(n);
-  cplx<R> base;
-  if (a.itp) {
-    base = mk<R>(exp(-(Vp + Vint) * a.tau_d), (R)0);
-  } else {
-    base = cis_(-(Vp + Vint) * a.tau_d);
-  }
-#pragma unroll
-  for (int c = 0; c < D; ++c) v[c] = v[c] * (base * a.zee[c]);
+  diag_apply<R, D>(v, Vp + Vint, a.tau_d, a.itp, a.zee, a.zee_lo);
 }
 
 // <F> components from the raising operator (src/observables.jl:61-86).
@@ -471,9 +523,9 @@ __device__ __forceinline__ void rodrigues_point(cplx<R> (&v)[D], R c1, R tau, in
 #pragma unroll
     for (int c = 0; c < D; ++c) v[c] = v[c] - sh * w[c] + chm1 * w2[c];
   } else {
-    R sn, cs;
-    if constexpr (sizeof(R) == 8) sincos(th, &sn, &cs); else sincosf(th, &sn, &cs);
-    const R cm1 = cs - (R)1;
+    R sn, sh;
+    if constexpr (sizeof(R) == 8) sn = sin(th), sh = sin(th * (R)0.5); else sn = sinf(th), sh = sinf(th * 0.5f);
+    const R cm1 = (R)-2 * sh * sh;  // cos(th) - 1 without cancellation
 #pragma unroll
     for (int c = 0; c < D; ++c) v[c] = v[c] + mul_mi(sn * w[c]) + cm1 * w2[c];
   }
@@ -557,6 +609,58 @@ __device__ __forceinline__ void euler_point(cplx<R> (&v)[D], R px, R py, R pz, R
   }
 }
 
+// exp(-i tau phi·F) v (or exp(-tau phi·F) v in imaginary time) by a Taylor series
+// of the tridiagonal phi·F, with sub-steps so each has ||tau phi·F|| <= 1/2 and the
+// series cut once the bound of the next term is below eps.  Used by the FP32 form
+// in place of the Euler-angle phases, whose FP32 recurrences carry a systematic
+// magnitude error; the operator is the same exp(-i dt phi·F) as
+// src/spinor_utils.jl:82-166 and the skip threshold |phi||dt| < 1e-14 is kept.
+template <typename R, int D>
+__device__ __forceinline__ void rotate_taylor(cplx<R> (&v)[D], R px, R py, R pz, R tau, int itp,
+                                              const SpinTabs<R>& st, float eps) {
+  constexpr int F = (D - 1) / 2;
+  const R pm = sqrt(px * px + py * py + pz * pz);
+  if (pm * fabs(tau) < (R)1e-14) return;
+  const float bound = (float)(pm * fabs(tau)) * (float)F;
+  const int nsub = bound > 0.5f ? (int)ceilf(bound / 0.5f) : 1;
+  const float xs = bound / (float)nsub;
+  int K = 1;
+  {
+    float term = xs;
+    while (K < 30 && term >= eps) {
+      ++K;
+      term *= xs / (float)K;
+    }
+  }
+  const R dt = tau / (R)nsub;
+  for (int sub = 0; sub < nsub; ++sub) {
+    cplx<R> term[D], acc[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) term[c] = acc[c] = v[c];
+    for (int k = 1; k <= K; ++k) {
+      cplx<R> y[D];
+      nF_apply<R, D>(term, px, py, pz, st, y);
+      const R f = dt / (R)k;
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+        term[c] = itp ? (-f) * y[c] : mul_mi(f * y[c]);
+        acc[c] += term[c];
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < D; ++c) v[c] = acc[c];
+  }
+}
+
+// Spin rotation used by the DDI step and general-D spin mixing: the reference's
+// Euler-angle form in FP64, the Taylor form in FP32.
+template <typename R, int D>
+__device__ __forceinline__ void spin_rotate(cplx<R> (&v)[D], R px, R py, R pz, R tau, int itp,
+                                            const SpinTabs<R>& st) {
+  if constexpr (sizeof(R) == 8) euler_point<R, D>(v, px, py, pz, tau, itp, st);
+  else rotate_taylor<R, D>(v, px, py, pz, tau, itp, st, 1e-8f);
+}
+
 // Spin mixing exp(-i c1 tau <F>·F) (src/spin_mixing.jl:1-66).
 template <typename R, int D>
 __device__ __forceinline__ void spin_mixing_point(cplx<R> (&v)[D], R c1, R tau, int itp, const SpinTabs<R>& st) {
@@ -565,7 +669,7 @@ __device__ __forceinline__ void spin_mixing_point(cplx<R> (&v)[D], R c1, R tau, 
   } else if constexpr (D > 1) {
     R fx, fy, fz;
     spin_vector<R, D>(v, st, fx, fy, fz);
-    euler_point<R, D>(v, c1 * fx, c1 * fy, c1 * fz, tau, itp, st);
+    spin_rotate<R, D>(v, c1 * fx, c1 * fy, c1 * fz, tau, itp, st);
   }
 }
 
@@ -580,7 +684,7 @@ __global__ void __launch_bounds__(256) k_potential(PotArgs<R> a, SpinTabs<R> st)
   if (a.pre_diag) diag_point<R, D>(v, Vp, a);
   if (a.rot_a) spin_mixing_point<R, D>(v, a.c1, a.tau_s, a.itp, st);
   if (a.ddi_rot) {
-    euler_point<R, D>(v, a.phi[p], a.phi[a.N + p], a.phi[2 * a.N + p], a.tau_ddi, a.itp, st);
+    spin_rotate<R, D>(v, a.phi[p], a.phi[a.N + p], a.phi[2 * a.N + p], a.tau_ddi, a.itp, st);
   }
   if (a.rot_b) spin_mixing_point<R, D>(v, a.c1, a.tau_s, a.itp, st);
   if (a.post_diag) diag_point<R, D>(v, Vp, a);
@@ -618,6 +722,7 @@ struct TensorArgs {
   R tau;                      // tensor tau
   R tau_d, c0, c_lhy;         // diagonal stage (same layout as PotArgs)
   cplx<R> zee[kMaxD];
+  cplx<R> zee_lo[kMaxD];
   double eps;                 // series cut
 };
 
@@ -627,11 +732,7 @@ __device__ __forceinline__ void diag_point_t(cplx<R> (&v)[D], R Vp, const Tensor
 #pragma unroll
   for (int c = 0; c < D; ++c) n += abs2(v[c]);
   const R Vint = a.c0 * n + a.c_lhy * n * sqrt(n);
-  cplx<R> base;
-  if (a.itp) base = mk<R>(exp(-(Vp + Vint) * a.tau_d), (R)0);
-  else base = cis_(-(Vp + Vint) * a.tau_d);
-#pragma unroll
-  for (int c = 0; c < D; ++c) v[c] = v[c] * (base * a.zee[c]);
+  diag_apply<R, D>(v, Vp + Vint, a.tau_d, a.itp, a.zee, a.zee_lo);
 }
 
 template <typename R, int D>

@@ -105,6 +105,10 @@ class sbec_energy_terms(C.Structure):
     _fields_ = [(k, C.c_double) for k in ("kinetic", "trap", "zeeman", "c0", "c1", "ddi", "lhy", "tensor")]
 
 
+class sbec_kernel_stat(C.Structure):
+    _fields_ = [("name", C.c_char * 32), ("launches", C.c_int64), ("ms", C.c_double), ("bytes", C.c_double)]
+
+
 CALLBACK = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(sbec_snapshot))
 
 _P = C.c_void_p
@@ -142,6 +146,10 @@ _PROTOS = {
     "sbec_magnetization": (C.c_int, [_P, _D]),
     "sbec_spin_density": (C.c_int, [_P, _D]),
     "sbec_ddi_potential": (C.c_int, [_P, C.c_int32, _D]),
+    "sbec_profile_enable": (C.c_int, [_P, C.c_int32]),
+    "sbec_profile_read": (C.c_int, [_P, C.POINTER(sbec_kernel_stat), C.c_int32, C.POINTER(C.c_int32)]),
+    "sbec_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "sbec_ws_stream": (C.c_int, [_P, C.POINTER(C.c_void_p)]),
 }
 
 _lib = None

@@ -102,6 +102,29 @@ class Workspace:
         self.sim_params = SimParams(dt, self.sim_params.n_steps, self.sim_params.imaginary_time,
                                     self.sim_params.normalize_every, self.sim_params.save_every)
 
+    # ---- tracing
+    def profile(self, enable: bool = True) -> None:
+        check(self._lib.sbec_profile_enable(self.handle, int(bool(enable))))
+
+    def profile_read(self) -> dict:
+        buf = (_lib.sbec_kernel_stat * 64)()
+        n = C.c_int32()
+        check(self._lib.sbec_profile_read(self.handle, buf, 64, C.byref(n)))
+        return {buf[i].name.decode(): dict(launches=buf[i].launches, ms=buf[i].ms, bytes=buf[i].bytes)
+                for i in range(min(n.value, 64))}
+
+    @property
+    def launch_count(self) -> int:
+        n = C.c_int64()
+        check(self._lib.sbec_launch_count(self.handle, C.byref(n)))
+        return n.value
+
+    @property
+    def stream_ptr(self) -> int:
+        p = C.c_void_p()
+        check(self._lib.sbec_ws_stream(self.handle, C.byref(p)))
+        return int(p.value or 0)
+
     def tensor_channels(self):
         act = C.c_int32()
         n = C.c_int32()

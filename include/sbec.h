@@ -187,6 +187,22 @@ sbec_status sbec_spin_density(sbec_ws* ws, double* out);
  * src/ddi_padded.jl:55-85); padded selects the zero-padded convolution. */
 sbec_status sbec_ddi_potential(sbec_ws* ws, int32_t padded, double* out);
 
+/* ---- tracing (the reference's @timeit_debug substep timers, src/split_step.jl:15-131) ---- */
+typedef struct sbec_kernel_stat {
+  char name[32];             /* kernel category: fft_x, fft_last_kinetic, potential, tensor, ddi_*, reduce, ... */
+  int64_t launches;          /* timed launches since profiling was enabled */
+  double ms;                 /* summed CUDA-event durations on the workspace stream */
+  double bytes;              /* summed algorithmic bytes (one read + one write of each array touched) */
+} sbec_kernel_stat;
+/* Enable (1) or disable (0) per-launch CUDA-event timing; either call resets the statistics. */
+sbec_status sbec_profile_enable(sbec_ws* ws, int32_t enable);
+/* Copy up to max statistics into out; *n receives the number of categories. */
+sbec_status sbec_profile_read(sbec_ws* ws, sbec_kernel_stat* out, int32_t max, int32_t* n);
+/* Number of kernels this workspace has launched since creation. */
+sbec_status sbec_launch_count(sbec_ws* ws, int64_t* n);
+/* The workspace's CUDA stream (cudaStream_t), for callers that order or time work on it. */
+sbec_status sbec_ws_stream(sbec_ws* ws, void** stream);
+
 #ifdef __cplusplus
 }
 #endif

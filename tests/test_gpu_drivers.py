@@ -7,6 +7,7 @@ import pytest
 
 import oracle as O
 import spinorbec as S
+from oracle.spinorbec_oracle import _gaussian
 from parity_util import ENERGY_TOL_FP64, PSI_TOL_FP64, make_pair, rel_psi_err
 
 pytestmark = pytest.mark.gpu
@@ -137,7 +138,7 @@ def test_yoshida_3d_f6_tensor_ddi_padded(gpu):
     ip = O.interaction_params_from_constraint(c_total=4689.0, c1_ratio=1 / 36, F=6, c_extra=(0.0, 0.0, 50.0))
     og = O.make_grid(O.GridConfig((8, 8, 8), (24.0, 24.0, 24.0)))
     psi = np.zeros((8, 8, 8, 13), dtype=np.complex128, order="F")
-    g = O._gaussian(og, (3.0, 3.0, 3.0))
+    g = _gaussian(og, (3.0, 3.0, 3.0))
     rng = np.random.Generator(np.random.PCG64(11))
     psi[..., 0] = g * np.exp(1j * 0.01 * rng.standard_normal(g.shape))
     psi /= np.sqrt(np.sum(np.abs(psi) ** 2) * O.cell_volume(og))

@@ -36,7 +36,7 @@ def test_kinetic_step(gpu, n, L, itp):
 
 
 CASES = {
-    "f1_sm_zeeman_lhy": dict(F=1, c0=10.0, c1=-0.5, omega=None, zeeman=(0.3, 0.1), c_lhy=0.7),
+    "f1_sm_zeeman_lhy": dict(F=1, c0=10.0, c1=-0.5, zeeman=(0.3, 0.1), c_lhy=0.7),
     "f1_afm": dict(F=1, c0=10.0, c1=0.5, zeeman=(0.0, 0.1)),
     "f2_euler": dict(F=2, c0=30.0, c1=2.0, zeeman=(0.2, -0.05)),
     "f6_euler": dict(F=6, c0=50.0, c1=3.0, zeeman=(0.1, 0.02)),
