@@ -74,6 +74,10 @@ void kinetic(sbec_ws* ws, double dt, bool itp) {
   ws->eng->kinetic(dt, itp);
 }
 
+// split_step! x n through the fused row passes when the workspace allows it
+// (no DDI / tensor, renormalisation every step or never); else operator by operator.
+void split_steps(sbec_ws* ws, long long n);
+
 // split_step! (src/split_step.jl:10-35)
 void split_step_once(sbec_ws* ws) {
   EngineBase& e = *ws->eng;
@@ -85,6 +89,22 @@ void split_step_once(sbec_ws* ws) {
   e.t += it ? 0.0 : dt;
   e.step += 1;
   if (it && e.normalize_every > 0 && e.step % e.normalize_every == 0) e.normalize();
+}
+
+void split_steps(sbec_ws* ws, long long n) {
+  EngineBase& e = *ws->eng;
+  const bool it = e.itp;
+  const bool norm_each = it && e.normalize_every == 1;
+  const bool no_norm = !it || e.normalize_every <= 0;
+  if (n > 0 && e.fused_path() && (norm_each || no_norm)) {
+    e.fused_split_steps(n, e.dt, ws->kin_dt, ws->kin_itp, it, norm_each);
+    for (long long i = 0; i < n; ++i) {
+      e.t += it ? 0.0 : e.dt;
+      e.step += 1;
+    }
+    return;
+  }
+  for (long long i = 0; i < n; ++i) split_step_once(ws);
 }
 
 // _strang_core! (src/split_step.jl:146-152)
@@ -349,7 +369,7 @@ sbec_status sbec_normalize_constrained(sbec_ws* ws, double target_Mz) {
 sbec_status sbec_split_step(sbec_ws* ws, int64_t n) {
   SBEC_API_BEGIN
   E(ws);
-  for (int64_t i = 0; i < n; ++i) split_step_once(ws);
+  split_steps(ws, n);
   ws->eng->sync();
   SBEC_API_END
 }
@@ -378,9 +398,30 @@ sbec_status sbec_run_simulation(sbec_ws* ws, int64_t n_steps, int64_t save_every
   if (save_every <= 0) fail(SBEC_ERR_INVALID, "save_every must be positive");
   check_cb(snapshot(ws, cb, user));
   if (e.itp) {
-    for (int64_t step = 1; step <= n_steps; ++step) {
-      split_step_once(ws);
+    int64_t step = 0;
+    while (step < n_steps) {
+      const int64_t nxt = std::min(n_steps, (step / save_every + 1) * save_every);
+      split_steps(ws, nxt - step);
+      step = nxt;
       if (step % save_every == 0) check_cb(snapshot(ws, cb, user));
+    }
+  } else if (e.fused_path() && !ws->kin_itp && ws->kin_dt == e.dt) {
+    // leapfrog with the fused row passes: identical operator sequence
+    const double dt = e.dt;
+    e.lf_open(dt);
+    int64_t step = 0;
+    while (step < n_steps) {
+      const int64_t seg_end = std::min(n_steps, (step / save_every + 1) * save_every);
+      const int64_t nseg = seg_end - step;
+      e.lf_steps(nseg - 1, dt);
+      e.lf_close(dt);
+      for (int64_t i = 0; i < nseg; ++i) {
+        e.t += dt;
+        e.step += 1;
+      }
+      step = seg_end;
+      if (step % save_every == 0) check_cb(snapshot(ws, cb, user));
+      if (step < n_steps) e.lf_open(dt);
     }
   } else {
     const double dt = e.dt;
@@ -590,7 +631,16 @@ sbec_status sbec_ground_state(sbec_ws* ws, int64_t n_steps, double tol, int64_t 
   double final_dE = NAN, final_dpsi = NAN;
   int64_t steps = 0;
   for (int64_t step = 1; step <= n_steps; ++step) {
-    split_step_once(ws);
+    if (!use_c && step > 10 && step % check_every != 0) {
+      // run up to the next convergence check in one fused block
+      const int64_t nxt = std::min(n_steps, (step / check_every + 1) * check_every) - 1;
+      split_steps(ws, nxt - step + 1);
+      step = nxt;
+      steps = step;
+      if (step == n_steps) break;
+      continue;
+    }
+    split_steps(ws, 1);
     steps = step;
     if (step <= 10) check_itp_overflow(e, step);
     if (use_c) normalize_constrained(e, target_Mz);

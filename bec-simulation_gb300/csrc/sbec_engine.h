@@ -132,6 +132,16 @@ class EngineBase {
   virtual void ddi_potential(bool padded, double* host3N) = 0;
   virtual void sync() = 0;
 
+  // Fused paths (no DDI, no tensor, supported line length / D): a leapfrog step is a
+  // row pass plus the last-axis pass; an ITP split_step defers its renormalisation
+  // into the next row pass.
+  virtual bool fused_path() const = 0;
+  virtual void lf_open(double dt) = 0;               // V(dt/2), forward x
+  virtual void lf_steps(long long n, double dt) = 0;  // n x [K(dt) with merged V(dt)]
+  virtual void lf_close(double dt) = 0;              // K(dt), V(dt/2)
+  virtual void fused_split_steps(long long n, double dt, double kin_dt, bool kin_itp, bool itp,
+                                 bool normalize) = 0;
+
  protected:
   Setup s_;
   cudaStream_t stream_ = nullptr;

@@ -394,6 +394,90 @@ class Engine final : public EngineBase {
     download_real3(phi_per_, host3N);
   }
 
+  // ---------------- fused paths ----------------
+  bool fused_path() const override {
+    if (s_.ddi || s_.tensor) return false;
+    if (!(s_.D == 1 || s_.D == 3 || s_.D == 5)) return false;
+    const int nx = s_.n[0];
+    if (nx < 16 || nx > 4096) return false;
+    return row_smem_bytes(nx) <= 200 * 1024;
+  }
+
+  void lf_open(double dtv) override {
+    update_phase(dtv, false);
+    RowArgs<R> a = row_args(false);
+    a.p1 = pot_full(dtv / 2, false);
+    a.flags = RP_POT1 | (s_.ndim > 1 ? RP_FWD_X : 0);
+    launch_row(a);
+  }
+
+  void lf_steps(long long n, double dtv) override {
+    update_phase(dtv, false);
+    for (long long i = 0; i < n; ++i) {
+      if (s_.ndim == 1) {
+        RowArgs<R> a = row_args(false);
+        a.p2 = pot_full(dtv, false);
+        a.flags = RP_KIN_X | RP_POT2;
+        launch_row(a);
+      } else {
+        last_axes_kinetic();
+        RowArgs<R> a = row_args(false);
+        a.p1 = pot_full(dtv, false);
+        a.flags = RP_INV_X | RP_POT1 | RP_FWD_X;
+        launch_row(a);
+      }
+    }
+  }
+
+  void lf_close(double dtv) override {
+    update_phase(dtv, false);
+    RowArgs<R> a = row_args(false);
+    if (s_.ndim == 1) {
+      a.p2 = pot_full(dtv / 2, false);
+      a.flags = RP_KIN_X | RP_POT2;
+    } else {
+      last_axes_kinetic();
+      a.p1 = pot_full(dtv / 2, false);
+      a.flags = RP_INV_X | RP_POT1;
+    }
+    launch_row(a);
+  }
+
+  // split_step! x n (src/split_step.jl:10-35) as row passes; with `normalize` the
+  // renormalisation of step k is applied at the start of step k+1 (and flushed at
+  // the end), using the |psi|^2 sums the closing pass of step k accumulated.
+  void fused_split_steps(long long n, double dtv, double kin_dt, bool kin_itp, bool it, bool normalize) override {
+    update_phase(kin_dt, kin_itp);
+    bool pending = false;
+    for (long long i = 0; i < n; ++i) {
+      if (s_.ndim == 1) {
+        RowArgs<R> a = row_args(pending);
+        a.p1 = pot_full(dtv / 2, it);
+        a.p2 = pot_full(dtv / 2, it);
+        a.flags |= RP_POT1 | RP_KIN_X | RP_POT2 | (normalize ? RP_NORM : 0);
+        const int nb = launch_row(a);
+        if (normalize) finish_row_norm(nb);
+      } else {
+        RowArgs<R> a = row_args(pending);
+        a.p1 = pot_full(dtv / 2, it);
+        a.flags |= RP_POT1 | RP_FWD_X;
+        launch_row(a);
+        last_axes_kinetic();
+        RowArgs<R> b = row_args(false);
+        b.p1 = pot_full(dtv / 2, it);
+        b.flags = RP_INV_X | RP_POT1 | (normalize ? RP_NORM : 0);
+        const int nb = launch_row(b);
+        if (normalize) finish_row_norm(nb);
+      }
+      pending = normalize;
+    }
+    if (pending) {
+      pb();
+      k_normalize_apply<R><<<grid_for(nc_), 256, 0, stream_>>>(psi_[kPsi], N_ * s_.D, 1, results_ + 40, s_.dV);
+      done("normalize", 2.0 * (double)sizeof(cplx<R>) * nc_);
+    }
+  }
+
   void sync() override { cuda_check(cudaStreamSynchronize(stream_), "stream sync"); }
 
  private:
@@ -630,6 +714,119 @@ class Engine final : public EngineBase {
                                  (int64_t)nx * ny, ny, ny, 1);
     }
     if (kinetic) SBEC_SWITCH_POW2(nx, launch_fft_x, buf, (int64_t)ny * nz * D, 1);
+  }
+
+  // ---- fused row pass launchers
+  template <int NN, int D>
+  static constexpr int row_rpb() {
+    constexpr int tpl = NN / FftPlan<NN>::E;
+    constexpr int r = 64 / (D * tpl);
+    return r < 1 ? 1 : r;
+  }
+
+  static int plan_radix(int n) {  // FftPlan<n>::E on the host
+    switch (n) {
+      case 32: case 64: case 512: return 8;
+      case 2: case 4: case 8: return n;
+      default: return 16;
+    }
+  }
+
+  size_t row_smem_bytes(int nx) const {
+    const int tpl = nx / plan_radix(nx);
+    int rpb = 64 / (s_.D * std::max(tpl, 1));
+    if (rpb < 1) rpb = 1;
+    return sizeof(cplx<R>) * (size_t)s_.D * rpb * nx;
+  }
+
+  PotArgs<R> pot_full(double tau_half, bool it) const {
+    // the half-potential stage without DDI/tensor: diag(tau/2) SM(tau/2) SM(tau/2) diag(tau/2)
+    PotArgs<R> a = pot_args(tau_half / 2, it);
+    const bool sm = std::fabs(s_.c1) >= 1e-30 && s_.D > 1;
+    a.pre_diag = 1;
+    a.rot_a = sm;
+    a.rot_b = sm;
+    a.post_diag = 1;
+    a.tau_s = (R)(tau_half / 2);
+    return a;
+  }
+
+  RowArgs<R> row_args(bool scale) const {
+    RowArgs<R> a{};
+    a.psi = psi_[kPsi];
+    a.N = N_;
+    a.n_rows = N_ / s_.n[0];
+    a.flags = scale ? RP_SCALE : 0;
+    a.norm_total = results_ + 40;
+    a.dV = s_.dV;
+    a.partials = partials_;
+    return a;
+  }
+
+  template <int NN, int D>
+  int launch_row_nd(const RowArgs<R>& a) {
+    constexpr int RPB = row_rpb<NN, D>();
+    constexpr int TPL = NN / FftPlan<NN>::E;
+    const size_t smem = sizeof(cplx<R>) * D * RPB * NN;
+    auto kern = k_row_pass<R, NN, D, RPB>;
+    static const bool once = (set_smem(kern, smem), true);
+    (void)once;
+    const int nb = (int)((a.n_rows + RPB - 1) / RPB);
+    pb();
+    kern<<<nb, D * RPB * TPL, smem, stream_>>>(a, st_, phase_ref(), twiddle(NN));
+    done("row_pass", 2.0 * (double)sizeof(cplx<R>) * nc_ + (double)sizeof(R) * N_ * ((a.flags & RP_POT1) ? 1 : 0));
+    return nb;
+  }
+
+  template <int NN>
+  int launch_row_n(const RowArgs<R>& a) {
+    switch (s_.D) {
+      case 1: return launch_row_nd<NN, 1>(a);
+      case 3: return launch_row_nd<NN, 3>(a);
+      case 5: return launch_row_nd<NN, 5>(a);
+      default: fail(SBEC_ERR_UNSUPPORTED, "fused path needs D in {1,3,5}");
+    }
+  }
+
+  int launch_row(const RowArgs<R>& a) {
+    if (a.flags & RP_NORM) {
+      if ((a.n_rows + 0) > (int64_t)kMaxBlocks * 64) fail(SBEC_ERR_UNSUPPORTED, "too many rows for the norm partials");
+    }
+    switch (s_.n[0]) {
+      case 16: return launch_row_n<16>(a);
+      case 32: return launch_row_n<32>(a);
+      case 64: return launch_row_n<64>(a);
+      case 128: return launch_row_n<128>(a);
+      case 256: return launch_row_n<256>(a);
+      case 512: return launch_row_n<512>(a);
+      case 1024: return launch_row_n<1024>(a);
+      case 2048: return launch_row_n<2048>(a);
+      case 4096: return launch_row_n<4096>(a);
+      default: fail(SBEC_ERR_UNSUPPORTED, "fused path line length");
+    }
+  }
+
+  void finish_row_norm(int nb) {
+    if (nb > kMaxBlocks * 16) fail(SBEC_ERR_UNSUPPORTED, "too many row blocks");
+    pb();
+    k_reduce_finish<1><<<1, 32, 0, stream_>>>(partials_, nb, 0, results_ + 40);
+    done("reduce_finish", 8.0 * nb);
+  }
+
+  // The kinetic passes over the axes above x: 2-D: y fwd*phase*inv;
+  // 3-D: y fwd, z fwd*phase*inv, y inv.
+  void last_axes_kinetic() {
+    const int nx = s_.n[0], ny = s_.n[1], nz = s_.n[2];
+    const int64_t D = s_.D;
+    if (s_.ndim == 2) {
+      SBEC_SWITCH_POW2_STRIDED(ny, launch_fft_strided, psi_[kPsi], (int64_t)nx, (int64_t)nx, D, N_, ny, ny, 2);
+    } else {
+      SBEC_SWITCH_POW2_STRIDED(ny, launch_fft_strided, psi_[kPsi], (int64_t)nx, (int64_t)nx, (int64_t)nz * D,
+                               (int64_t)nx * ny, ny, ny, 0);
+      SBEC_SWITCH_POW2_STRIDED(nz, launch_fft_strided, psi_[kPsi], (int64_t)nx * ny, (int64_t)nx * ny, D, N_, nz, nz, 2);
+      SBEC_SWITCH_POW2_STRIDED(ny, launch_fft_strided, psi_[kPsi], (int64_t)nx, (int64_t)nx, (int64_t)nz * D,
+                               (int64_t)nx * ny, ny, ny, 1);
+    }
   }
 
   // ---- DDI

@@ -700,6 +700,123 @@ __global__ void __launch_bounds__(256) k_potential(PotArgs<R> a, SpinTabs<R> st)
 }
 
 // ---------------------------------------------------------------------------
+// Fused row pass for the no-DDI, no-tensor path: a tile of RPB x-rows (fixed y,z)
+// with all D components in shared memory runs, in order and as selected by flags,
+//   [scale by 1/sqrt(norm) (deferred ITP renormalisation)] [inverse x FFT]
+//   [potential stage 1] [forward x FFT | 1-D kinetic step fwd*phase*inv]
+//   [potential stage 2] [per-block sums of |psi|^2 for the next renormalisation]
+// so a leapfrog step is this pass plus the last-axis pass (2-D) and psi makes one
+// round trip through HBM/L2 per pass instead of one per operator.
+// ---------------------------------------------------------------------------
+enum RowFlags {
+  RP_SCALE = 1,
+  RP_INV_X = 2,
+  RP_POT1 = 4,
+  RP_FWD_X = 8,
+  RP_KIN_X = 16,
+  RP_POT2 = 32,
+  RP_NORM = 64
+};
+
+template <typename R>
+struct RowArgs {
+  cplx<R>* psi;
+  int64_t N;          // points per component
+  int64_t n_rows;     // N / nx
+  int flags;
+  PotArgs<R> p1, p2;  // potential stages (diag, spin mixing)
+  const double* norm_total;  // sum |psi|^2 of the previous pass (RP_SCALE)
+  double dV;
+  double* partials;   // RP_NORM: one double per block
+};
+
+template <typename R, int D>
+__device__ __forceinline__ void pot_stage(cplx<R> (&v)[D], R Vp, const PotArgs<R>& a, const SpinTabs<R>& st) {
+  if (a.pre_diag) diag_point<R, D>(v, Vp, a);
+  if (a.rot_a) spin_mixing_point<R, D>(v, a.c1, a.tau_s, a.itp, st);
+  if (a.rot_b) spin_mixing_point<R, D>(v, a.c1, a.tau_s, a.itp, st);
+  if (a.post_diag) diag_point<R, D>(v, Vp, a);
+}
+
+template <typename R, int N, int D, int RPB>
+__global__ void __launch_bounds__(D * RPB * (N / FftPlan<N>::E))
+k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
+  constexpr int TPL = N / FftPlan<N>::E;
+  constexpr int NL = D * RPB;  // line = c*RPB + r
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);
+  __shared__ double red[32];
+  const int tid = threadIdx.x;
+  const int64_t row0 = (int64_t)blockIdx.x * RPB;
+  const int nr = (int)min((int64_t)RPB, a.n_rows - row0);
+  R scale = (R)1;
+  if (a.flags & RP_SCALE) scale = (R)(1.0 / sqrt(a.norm_total[0] * a.dV));
+  for (int f = tid; f < NL * N; f += blockDim.x) {
+    const int line = f / N, x = f % N;
+    const int c = line / RPB, r = line % RPB;
+    cplx<R> v = mk<R>(0, 0);
+    if (r < nr) v = a.psi[c * a.N + (row0 + r) * N + x];
+    if (a.flags & RP_SCALE) v = v * scale;
+    s[f] = v;
+  }
+  __syncthreads();
+  const int t = tid % TPL, l = tid / TPL;
+  if (a.flags & RP_INV_X) fft_tile<R, N, +1>(s, 1, N, l, t, tw);
+  if (a.flags & RP_POT1) {
+    for (int p = tid; p < RPB * N; p += blockDim.x) {
+      const int r = p / N, x = p % N;
+      if (r >= nr) continue;
+      cplx<R> v[D];
+#pragma unroll
+      for (int c = 0; c < D; ++c) v[c] = s[(c * RPB + r) * N + x];
+      pot_stage<R, D>(v, a.p1.V[(row0 + r) * N + x], a.p1, st);
+#pragma unroll
+      for (int c = 0; c < D; ++c) s[(c * RPB + r) * N + x] = v[c];
+    }
+    __syncthreads();
+  }
+  if (a.flags & (RP_FWD_X | RP_KIN_X)) fft_tile<R, N, -1>(s, 1, N, l, t, tw);
+  if (a.flags & RP_KIN_X) {
+    for (int f = tid; f < NL * N; f += blockDim.x) s[f] = tw_mul<R>(s[f], ph.tab[0], f % N, false);
+    __syncthreads();
+    fft_tile<R, N, +1>(s, 1, N, l, t, tw);
+  }
+  double acc = 0.0;
+  if (a.flags & (RP_POT2 | RP_NORM)) {
+    for (int p = tid; p < RPB * N; p += blockDim.x) {
+      const int r = p / N, x = p % N;
+      if (r >= nr) continue;
+      cplx<R> v[D];
+#pragma unroll
+      for (int c = 0; c < D; ++c) v[c] = s[(c * RPB + r) * N + x];
+      if (a.flags & RP_POT2) {
+        pot_stage<R, D>(v, a.p2.V[(row0 + r) * N + x], a.p2, st);
+#pragma unroll
+        for (int c = 0; c < D; ++c) s[(c * RPB + r) * N + x] = v[c];
+      }
+#pragma unroll
+      for (int c = 0; c < D; ++c) acc += (double)v[c].x * v[c].x + (double)v[c].y * v[c].y;
+    }
+    __syncthreads();
+  }
+  for (int f = tid; f < NL * N; f += blockDim.x) {
+    const int line = f / N, x = f % N;
+    const int c = line / RPB, r = line % RPB;
+    if (r < nr) a.psi[c * a.N + (row0 + r) * N + x] = s[f];
+  }
+  if (a.flags & RP_NORM) {
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((tid & 31) == 0) red[tid >> 5] = acc;
+    __syncthreads();
+    if (tid == 0) {
+      double x = 0.0;
+      for (int w = 0; w < (int)((blockDim.x + 31) >> 5); ++w) x += red[w];
+      a.partials[blockIdx.x] = x;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // General-F tensor interaction (src/tensor_interaction.jl:130-240).
 // h_{cc'} = sum_J G[J][c][c'] conj(psi_{J-c}) psi_{J-c'} with
 // G[J][c][c'] = sum_S g_S CG(m,mu|S,M) CG(m',nu|S,M), M = 2F - J (the HF-entry sum
