@@ -32,6 +32,7 @@ class Profiler {
   }
   bool enabled() const { return enabled_; }
   long long total_launches() const { return total_; }
+  void add_launches(long long n) { total_ += n; }
   void begin(cudaStream_t s) {
     if (!enabled_) return;
     cur_ = get_event();

@@ -7,6 +7,7 @@
 #include <complex>
 #include <cstring>
 #include <map>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -23,14 +24,14 @@ namespace sbec {
 // least one 32-byte sector wide so every global access moves whole sectors.
 template <typename R, int N>
 constexpr int x_lines_per_block() {
-  constexpr int tpl = N / FftPlan<N>::E;
+  constexpr int tpl = N / PlanOf<R, N>::E;
   constexpr int lpb = 64 / tpl;
   return lpb < 1 ? 1 : lpb;
 }
 
 template <typename R, int N>
 constexpr int strided_width() {
-  constexpr int tpl = N / FftPlan<N>::E;
+  constexpr int tpl = N / PlanOf<R, N>::E;
   constexpr int sector = 32 / (int)sizeof(cplx<R>);
   int w = 64 / tpl;
   if (w < sector) w = sector;
@@ -40,7 +41,7 @@ constexpr int strided_width() {
 
 template <typename R, int MH>
 constexpr int ddi_x_rows_per_block() {
-  constexpr int tpl = MH / FftPlan<MH>::E;
+  constexpr int tpl = MH / PlanOf<R, MH>::E;
   int lpb = 64 / (3 * tpl);
   if (lpb < 1) lpb = 1;
   while (lpb > 1 && (long)3 * lpb * (2 * MH + 1) * (int)sizeof(cplx<R>) > 96 * 1024) lpb /= 2;
@@ -49,7 +50,7 @@ constexpr int ddi_x_rows_per_block() {
 
 template <typename R, int M>
 constexpr int ddi_last_width() {
-  constexpr int tpl = M / FftPlan<M>::E;
+  constexpr int tpl = M / PlanOf<R, M>::E;
   constexpr int sector = 32 / (int)sizeof(cplx<R>);
   int w = 64 / (3 * tpl);
   if (w < sector) w = sector;
@@ -172,6 +173,8 @@ class Engine final : public EngineBase {
 
   ~Engine() override {
     cudaStreamSynchronize(stream_);
+    for (auto& kv : graphs_)
+      if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
     for (void* p : allocs_) cudaFree(p);
     if (host_res_) cudaFreeHost(host_res_);
     if (host_psi_) cudaFreeHost(host_psi_);
@@ -413,6 +416,10 @@ class Engine final : public EngineBase {
 
   void lf_steps(long long n, double dtv) override {
     update_phase(dtv, false);
+    if (n <= 0) return;
+    const GraphKey key{1, n, dtv, 0.0, zeeman_p, zeeman_q, 0};
+    if (graph_replay(key)) return;
+    graph_begin(key);
     for (long long i = 0; i < n; ++i) {
       if (s_.ndim == 1) {
         RowArgs<R> a = row_args(false);
@@ -427,6 +434,7 @@ class Engine final : public EngineBase {
         launch_row(a);
       }
     }
+    graph_end(key);
   }
 
   void lf_close(double dtv) override {
@@ -448,6 +456,10 @@ class Engine final : public EngineBase {
   // the end), using the |psi|^2 sums the closing pass of step k accumulated.
   void fused_split_steps(long long n, double dtv, double kin_dt, bool kin_itp, bool it, bool normalize) override {
     update_phase(kin_dt, kin_itp);
+    if (n <= 0) return;
+    const GraphKey key{2, n, dtv, kin_dt, zeeman_p, zeeman_q, (kin_itp ? 1 : 0) | (it ? 2 : 0) | (normalize ? 4 : 0)};
+    if (graph_replay(key)) return;
+    graph_begin(key);
     bool pending = false;
     for (long long i = 0; i < n; ++i) {
       if (s_.ndim == 1) {
@@ -476,6 +488,60 @@ class Engine final : public EngineBase {
       k_normalize_apply<R><<<grid_for(nc_), 256, 0, stream_>>>(psi_[kPsi], N_ * s_.D, 1, results_ + 40, s_.dV);
       done("normalize", 2.0 * (double)sizeof(cplx<R>) * nc_);
     }
+    graph_end(key);
+  }
+
+  // ---- CUDA graphs of repeated step blocks.  A block runs eagerly the first
+  // time a key is seen (creating lazily built tables), is captured on the
+  // second and replayed from then on; profiling runs stay eager so every
+  // launch keeps its own events.
+  struct GraphKey {
+    int kind;
+    long long n;
+    double dt, kin_dt, zp, zq;
+    int flags;
+    bool operator<(const GraphKey& o) const {
+      return std::tie(kind, n, dt, kin_dt, zp, zq, flags) < std::tie(o.kind, o.n, o.dt, o.kin_dt, o.zp, o.zq, o.flags);
+    }
+  };
+  struct GraphEntry {
+    int seen = 0;
+    cudaGraphExec_t exec = nullptr;
+    long long launches = 0;
+  };
+
+  bool graph_replay(const GraphKey& k) {
+    if (prof.enabled() || !use_graphs_) return false;
+    auto it = graphs_.find(k);
+    if (it == graphs_.end() || !it->second.exec) return false;
+    cuda_check(cudaGraphLaunch(it->second.exec, stream_), "cudaGraphLaunch");
+    prof.add_launches(it->second.launches);
+    return true;
+  }
+
+  void graph_begin(const GraphKey& k) {
+    capturing_ = false;
+    if (prof.enabled() || !use_graphs_) return;
+    GraphEntry& g = graphs_[k];
+    if (g.seen++ == 0) return;  // first use: eager
+    if (graphs_.size() > 64) return;
+    cuda_check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+    capturing_ = true;
+    cap_launch0_ = prof.total_launches();
+  }
+
+  void graph_end(const GraphKey& k) {
+    if (!capturing_) return;
+    capturing_ = false;
+    cudaGraph_t graph = nullptr;
+    cuda_check(cudaStreamEndCapture(stream_, &graph), "cudaStreamEndCapture");
+    GraphEntry& g = graphs_[k];
+    cuda_check(cudaGraphInstantiate(&g.exec, graph, 0), "cudaGraphInstantiate");
+    cudaGraphDestroy(graph);
+    g.launches = prof.total_launches() - cap_launch0_;
+    prof.add_launches(-g.launches);  // counted again on each replay
+    cuda_check(cudaGraphLaunch(g.exec, stream_), "cudaGraphLaunch");
+    prof.add_launches(g.launches);
   }
 
   void sync() override { cuda_check(cudaStreamSynchronize(stream_), "stream sync"); }
@@ -664,7 +730,7 @@ class Engine final : public EngineBase {
   template <int NN>
   void launch_fft_x(cplx<R>* data, int64_t n_lines, int mode) {
     constexpr int LPB = x_lines_per_block<R, NN>();
-    constexpr int TPL = NN / FftPlan<NN>::E;
+    constexpr int TPL = NN / PlanOf<R, NN>::E;
     const size_t smem = sizeof(cplx<R>) * LPB * NN;
     auto kern = k_fft_x<R, NN, LPB>;
     static const bool once = (set_smem(kern, smem), true);
@@ -679,7 +745,7 @@ class Engine final : public EngineBase {
   void launch_fft_strided(cplx<R>* data, int64_t S, int64_t inner, int64_t outer, int64_t outer_stride, int n_in,
                           int n_out, int mode) {
     constexpr int W = strided_width<R, NN>();
-    constexpr int TPL = NN / FftPlan<NN>::E;
+    constexpr int TPL = NN / PlanOf<R, NN>::E;
     const size_t smem = sizeof(cplx<R>) * W * NN;
     auto kern = k_fft_strided<R, NN, W>;
     static const bool once = (set_smem(kern, smem), true);
@@ -719,21 +785,13 @@ class Engine final : public EngineBase {
   // ---- fused row pass launchers
   template <int NN, int D>
   static constexpr int row_rpb() {
-    constexpr int tpl = NN / FftPlan<NN>::E;
+    constexpr int tpl = NN / PlanOf<R, NN>::E;
     constexpr int r = 64 / (D * tpl);
     return r < 1 ? 1 : r;
   }
 
-  static int plan_radix(int n) {  // FftPlan<n>::E on the host
-    switch (n) {
-      case 32: case 64: case 512: return 8;
-      case 2: case 4: case 8: return n;
-      default: return 16;
-    }
-  }
-
   size_t row_smem_bytes(int nx) const {
-    const int tpl = nx / plan_radix(nx);
+    const int tpl = nx / plan_radix_host(sizeof(R) == 4, nx);
     int rpb = 64 / (s_.D * std::max(tpl, 1));
     if (rpb < 1) rpb = 1;
     return sizeof(cplx<R>) * (size_t)s_.D * rpb * nx;
@@ -766,7 +824,7 @@ class Engine final : public EngineBase {
   template <int NN, int D>
   int launch_row_nd(const RowArgs<R>& a) {
     constexpr int RPB = row_rpb<NN, D>();
-    constexpr int TPL = NN / FftPlan<NN>::E;
+    constexpr int TPL = NN / PlanOf<R, NN>::E;
     const size_t smem = sizeof(cplx<R>) * D * RPB * NN;
     auto kern = k_row_pass<R, NN, D, RPB>;
     static const bool once = (set_smem(kern, smem), true);
@@ -852,7 +910,7 @@ class Engine final : public EngineBase {
   template <int MH>
   void launch_ddi_r2c(const R* f3, cplx<R>* spec, const DdiGeom& g, R* phi3) {
     constexpr int LPB = ddi_x_rows_per_block<R, MH>();
-    constexpr int TPL = MH / FftPlan<MH>::E;
+    constexpr int TPL = MH / PlanOf<R, MH>::E;
     const size_t smem = sizeof(cplx<R>) * 3 * LPB * (2 * MH + 1);
     auto kern = k_ddi_r2c_x<R, MH, LPB>;
     static const bool once = (set_smem(kern, smem), true);
@@ -867,7 +925,7 @@ class Engine final : public EngineBase {
   template <int MH>
   void launch_ddi_c2r(const cplx<R>* spec, const DdiGeom& g, R* phi3) {
     constexpr int LPB = ddi_x_rows_per_block<R, MH>();
-    constexpr int TPL = MH / FftPlan<MH>::E;
+    constexpr int TPL = MH / PlanOf<R, MH>::E;
     const size_t smem = sizeof(cplx<R>) * 3 * LPB * (2 * MH + 1);
     auto kern = k_ddi_c2r_x<R, MH, LPB>;
     static const bool once = (set_smem(kern, smem), true);
@@ -882,7 +940,7 @@ class Engine final : public EngineBase {
   template <int M>
   void launch_ddi_last(cplx<R>* spec, const DdiGeom& g, int64_t S, int64_t inner, int n_in, int n_out) {
     constexpr int W = ddi_last_width<R, M>();
-    constexpr int TPL = M / FftPlan<M>::E;
+    constexpr int TPL = M / PlanOf<R, M>::E;
     const size_t smem = sizeof(cplx<R>) * 3 * W * M;
     auto kern = k_ddi_last<R, M, W>;
     static const bool once = (set_smem(kern, smem), true);
@@ -1061,6 +1119,10 @@ class Engine final : public EngineBase {
   R* phi3_ = nullptr;
   R* phi_per_ = nullptr;
   cplx<R>* spec_[2] = {nullptr, nullptr};
+  std::map<GraphKey, GraphEntry> graphs_;
+  bool use_graphs_ = true;
+  bool capturing_ = false;
+  long long cap_launch0_ = 0;
   double phase_dt_ = NAN;
   int phase_itp_ = -1;
   std::vector<void*> allocs_;

@@ -55,7 +55,8 @@ __device__ __forceinline__ cplx<R> twmul(cplx<R> x, int k) {
     }
     if constexpr (sizeof(R) == 4) {
       const float hh = 0.70710677f, hl = 1.2101617e-08f;  // 1/sqrt(2) = hh + hl
-      return mk<R>(fmaf(a, hl, a * hh), fmaf(b, hl, b * hh));
+      // single rounding of a*hh + a*hl: the tail must not be added after the head is rounded
+      return mk<R>(fmaf(a, hh, a * hl), fmaf(b, hh, b * hl));
     } else {
       const R h = (R)0.70710678118654752440;
       return mk<R>(h * a, h * b);
@@ -136,10 +137,14 @@ __device__ __forceinline__ void run_stages(cplx<R>* s, int SI, int SL, int l, in
   if constexpr (sizeof...(REST) > 0) run_stages<R, N, E, SIGN, REST...>(s, SI, SL, l, t, Ns * RAD, tw);
 }
 
-// Radix plan per line length: E = largest radix; stages run in the listed order.
+// Radix plans per line length: E = largest radix; stages run in the listed order.
+// FP64 (FP64-throughput bound) uses radix-16 stages, which need the fewest
+// twiddle multiplies; FP32 (latency / bandwidth bound) uses radix-4/8 stages so
+// each line is spread over 4x more threads and the SMs hold more warps.
 template <int N> struct FftPlan;
-#define SBEC_PLAN(NN, EE, ...)                                                                   \
-  template <> struct FftPlan<NN> {                                                               \
+template <int N> struct FftPlan32;
+#define SBEC_PLAN(STRUCT, NN, EE, ...)                                                          \
+  template <> struct STRUCT<NN> {                                                                \
     static constexpr int E = EE;                                                                 \
     template <typename R, int SIGN>                                                              \
     static __device__ __forceinline__ void run(cplx<R>* s, int SI, int SL, int l, int t,        \
@@ -147,25 +152,58 @@ template <int N> struct FftPlan;
       run_stages<R, NN, EE, SIGN, __VA_ARGS__>(s, SI, SL, l, t, 1, tw);                          \
     }                                                                                            \
   };
-SBEC_PLAN(2, 2, 2)
-SBEC_PLAN(4, 4, 4)
-SBEC_PLAN(8, 8, 8)
-SBEC_PLAN(16, 16, 16)
-SBEC_PLAN(32, 8, 8, 4)
-SBEC_PLAN(64, 8, 8, 8)
-SBEC_PLAN(128, 16, 16, 8)
-SBEC_PLAN(256, 16, 16, 16)
-SBEC_PLAN(512, 8, 8, 8, 8)
-SBEC_PLAN(1024, 16, 16, 8, 8)
-SBEC_PLAN(2048, 16, 16, 16, 8)
-SBEC_PLAN(4096, 16, 16, 16, 16)
+SBEC_PLAN(FftPlan, 2, 2, 2)
+SBEC_PLAN(FftPlan, 4, 4, 4)
+SBEC_PLAN(FftPlan, 8, 8, 8)
+SBEC_PLAN(FftPlan, 16, 16, 16)
+SBEC_PLAN(FftPlan, 32, 8, 8, 4)
+SBEC_PLAN(FftPlan, 64, 8, 8, 8)
+SBEC_PLAN(FftPlan, 128, 16, 16, 8)
+SBEC_PLAN(FftPlan, 256, 16, 16, 16)
+SBEC_PLAN(FftPlan, 512, 8, 8, 8, 8)
+SBEC_PLAN(FftPlan, 1024, 16, 16, 8, 8)
+SBEC_PLAN(FftPlan, 2048, 16, 16, 16, 8)
+SBEC_PLAN(FftPlan, 4096, 16, 16, 16, 16)
+SBEC_PLAN(FftPlan32, 2, 2, 2)
+SBEC_PLAN(FftPlan32, 4, 4, 4)
+SBEC_PLAN(FftPlan32, 8, 4, 4, 2)
+SBEC_PLAN(FftPlan32, 16, 4, 4, 4)
+SBEC_PLAN(FftPlan32, 32, 4, 4, 4, 2)
+SBEC_PLAN(FftPlan32, 64, 4, 4, 4, 4)
+SBEC_PLAN(FftPlan32, 128, 4, 4, 4, 4, 2)
+SBEC_PLAN(FftPlan32, 256, 4, 4, 4, 4, 4)
+SBEC_PLAN(FftPlan32, 512, 8, 8, 8, 8)
+SBEC_PLAN(FftPlan32, 1024, 8, 8, 8, 4, 4)
+SBEC_PLAN(FftPlan32, 2048, 8, 8, 8, 8, 4)
+SBEC_PLAN(FftPlan32, 4096, 8, 8, 8, 8, 8)
 #undef SBEC_PLAN
+
+template <typename R, int N>
+struct PlanSel {
+  using type = FftPlan<N>;
+};
+template <int N>
+struct PlanSel<float, N> {
+  using type = FftPlan32<N>;
+};
+template <typename R, int N>
+using PlanOf = typename PlanSel<R, N>::type;
+
+// host-side mirror of PlanOf<R, N>::E
+inline int plan_radix_host(bool fp32, int n) {
+  if (fp32) return n <= 4 ? n : (n <= 256 ? 4 : 8);
+  switch (n) {
+    case 32: case 64: case 512: return 8;
+    case 2: case 4: case 8: return n;
+    default: return 16;
+  }
+}
 
 // Transform every line of a shared-memory tile (all threads of the block participate).
 // Caller must __syncthreads() after filling the tile; the function ends synchronised.
 template <typename R, int N, int SIGN>
 __device__ __forceinline__ void fft_tile(cplx<R>* s, int SI, int SL, int l, int t, const Tw<R>& tw) {
-  FftPlan<N>::template run<R, SIGN>(s, SI, SL, l, t, tw);
+  PlanOf<R, N>::template run<R, SIGN>(s, SI, SL, l, t, tw);
 }
 
 }  // namespace sbec

@@ -70,9 +70,9 @@ struct PhaseRef {
 // 2: forward, x phase (1-D kinetic step), inverse.
 // ---------------------------------------------------------------------------
 template <typename R, int N, int LPB>
-__global__ void __launch_bounds__(LPB * (N / FftPlan<N>::E))
+__global__ void __launch_bounds__(LPB * (N / PlanOf<R, N>::E))
 k_fft_x(cplx<R>* __restrict__ data, int64_t n_lines, int mode, PhaseRef<R> ph, Tw<R> tw) {
-  constexpr int TPL = N / FftPlan<N>::E;
+  constexpr int TPL = N / PlanOf<R, N>::E;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);
   const int tid = threadIdx.x;
@@ -103,10 +103,10 @@ k_fft_x(cplx<R>* __restrict__ data, int64_t n_lines, int mode, PhaseRef<R> ph, T
 // kinetic step; the line's lower-axis coordinates come from i0 + w).
 // ---------------------------------------------------------------------------
 template <typename R, int N, int W>
-__global__ void __launch_bounds__(W * (N / FftPlan<N>::E))
+__global__ void __launch_bounds__(W * (N / PlanOf<R, N>::E))
 k_fft_strided(cplx<R>* __restrict__ data, int64_t S, int64_t inner, int64_t outer_stride, int n_in,
               int n_out, int mode, PhaseRef<R> ph, Tw<R> tw) {
-  constexpr int TPL = N / FftPlan<N>::E;
+  constexpr int TPL = N / PlanOf<R, N>::E;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);
   __shared__ cplx<R> inner_ph[W];
@@ -235,10 +235,10 @@ __device__ __forceinline__ cplx<R> c2r_pre(const cplx<R>* X, int k, int MH, cons
 // tw_half: W_MH table; tw_full: W_Mx table.  For 1-D (ndim == 1) the kernel
 // also contracts and returns to real space (the x axis is the last axis).
 template <typename R, int MH, int LPB>
-__global__ void __launch_bounds__(3 * LPB * (MH / FftPlan<MH>::E))
+__global__ void __launch_bounds__(3 * LPB * (MH / PlanOf<R, MH>::E))
 k_ddi_r2c_x(const R* __restrict__ f3, int64_t field_n, cplx<R>* __restrict__ spec, DdiGeom g,
             R* __restrict__ phi3, Tw<R> tw_half, Tw<R> tw_full) {
-  constexpr int TPL = MH / FftPlan<MH>::E;
+  constexpr int TPL = MH / PlanOf<R, MH>::E;
   constexpr int NL = 3 * LPB;  // lines in the tile: field-major
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);   // NL * MH
@@ -312,10 +312,10 @@ k_ddi_r2c_x(const R* __restrict__ f3, int64_t field_n, cplx<R>* __restrict__ spe
 
 // C2R along x of the 3 fields (rows y < ny, z < nz), keeping x < nx.
 template <typename R, int MH, int LPB>
-__global__ void __launch_bounds__(3 * LPB * (MH / FftPlan<MH>::E))
+__global__ void __launch_bounds__(3 * LPB * (MH / PlanOf<R, MH>::E))
 k_ddi_c2r_x(const cplx<R>* __restrict__ spec, DdiGeom g, R* __restrict__ phi3, int64_t field_n,
             Tw<R> tw_half, Tw<R> tw_full) {
-  constexpr int TPL = MH / FftPlan<MH>::E;
+  constexpr int TPL = MH / PlanOf<R, MH>::E;
   constexpr int NL = 3 * LPB;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);
@@ -359,9 +359,9 @@ k_ddi_c2r_x(const cplx<R>* __restrict__ spec, DdiGeom g, R* __restrict__ phi3, i
 // transform, store of the first n_out entries.  Lines: inner index = position
 // in the lower axes of the spectrum (kx [, ky]), stride S between elements.
 template <typename R, int M, int W>
-__global__ void __launch_bounds__(3 * W * (M / FftPlan<M>::E))
+__global__ void __launch_bounds__(3 * W * (M / PlanOf<R, M>::E))
 k_ddi_last(cplx<R>* __restrict__ spec, DdiGeom g, int64_t S, int64_t inner, int n_in, int n_out, Tw<R> tw) {
-  constexpr int TPL = M / FftPlan<M>::E;
+  constexpr int TPL = M / PlanOf<R, M>::E;
   constexpr int NL = 3 * W;   // line index = fld*W + w
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);   // element (line, i) at s[i*NL + line]
@@ -739,9 +739,9 @@ __device__ __forceinline__ void pot_stage(cplx<R> (&v)[D], R Vp, const PotArgs<R
 }
 
 template <typename R, int N, int D, int RPB>
-__global__ void __launch_bounds__(D * RPB * (N / FftPlan<N>::E))
+__global__ void __launch_bounds__(D * RPB * (N / PlanOf<R, N>::E))
 k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
-  constexpr int TPL = N / FftPlan<N>::E;
+  constexpr int TPL = N / PlanOf<R, N>::E;
   constexpr int NL = D * RPB;  // line = c*RPB + r
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);
