@@ -658,7 +658,7 @@ template <typename R, int D>
 __device__ __forceinline__ void spin_rotate(cplx<R> (&v)[D], R px, R py, R pz, R tau, int itp,
                                             const SpinTabs<R>& st) {
   if constexpr (sizeof(R) == 8) euler_point<R, D>(v, px, py, pz, tau, itp, st);
-  else rotate_taylor<R, D>(v, px, py, pz, tau, itp, st, 1e-8f);
+  else rotate_taylor<R, D>(v, px, py, pz, tau, itp, st, 1e-13f);
 }
 
 // Spin mixing exp(-i c1 tau <F>·F) (src/spin_mixing.jl:1-66).
