@@ -29,6 +29,10 @@ void cuda_check(cudaError_t e, const char* what) {
 
 using namespace sbec;
 
+struct sbec_batch {
+  std::unique_ptr<EngineBase> eng;
+};
+
 struct sbec_ws {
   std::unique_ptr<EngineBase> eng;
   double kin_dt = 0.0;    // parameters of the current kinetic phase (the batched kinetic cache)
@@ -712,6 +716,122 @@ sbec_status sbec_ddi_potential(sbec_ws* ws, int32_t padded, double* out) {
   SBEC_API_BEGIN
   need(out, "out");
   E(ws).ddi_potential(padded != 0, out);
+  SBEC_API_END
+}
+
+// ---- batches of independent ITP solves (find_ground_state per solve, one schedule)
+sbec_status sbec_batch_create(const sbec_config* cfg, int32_t n_solves, const double* c0, const double* c1,
+                              const double* psi, const double* V, sbec_batch** out) {
+  SBEC_API_BEGIN
+  need(cfg, "config");
+  need(c0, "c0");
+  need(c1, "c1");
+  need(psi, "psi");
+  need(out, "out");
+  *out = nullptr;
+  if (!cfg->imaginary_time || cfg->normalize_every != 1)
+    fail(SBEC_ERR_INVALID, "batched ground states need imaginary_time=1 and normalize_every=1");
+  if (cfg->n_c_extra != 0 || cfg->gS_direct || cfg->enable_ddi)
+    fail(SBEC_ERR_UNSUPPORTED, "batched ground states support contact c0/c1 (+LHY) couplings without DDI");
+  Setup s = build_setup(*cfg);
+  if (sbec_device_count() < 1) fail(SBEC_ERR_DEVICE, "no CUDA device available (the GPU path has no CPU fallback)");
+  auto b = std::make_unique<sbec_batch>();
+  b->eng = cfg->precision == SBEC_FP32_BULK ? make_engine_f32(s) : make_engine_f64(s);
+  EngineBase& e = *b->eng;
+  e.zeeman_p = cfg->zeeman_p;
+  e.zeeman_q = cfg->zeeman_q;
+  e.dt = cfg->dt;
+  e.itp = true;
+  e.normalize_every = 1;
+  if (V) e.set_potential(V);
+  e.batch_init(n_solves, c0, c1, psi);
+  *out = b.release();
+  SBEC_API_END
+}
+
+sbec_status sbec_batch_destroy(sbec_batch* b) {
+  SBEC_API_BEGIN
+  delete b;
+  SBEC_API_END
+}
+
+sbec_status sbec_batch_get_psi(sbec_batch* b, int32_t solve, double* psi) {
+  SBEC_API_BEGIN
+  need(b, "batch");
+  need(psi, "psi");
+  b->eng->batch_get_psi(solve, psi);
+  SBEC_API_END
+}
+
+sbec_status sbec_batch_energies(sbec_batch* b, double* E) {
+  SBEC_API_BEGIN
+  need(b, "batch");
+  need(E, "E");
+  EngineBase& e = *b->eng;
+  std::vector<int> all(e.n_solves());
+  for (int i = 0; i < e.n_solves(); ++i) all[i] = i;
+  e.batch_set_active(all);
+  e.batch_energies(E);
+  SBEC_API_END
+}
+
+// The find_ground_state ITP loop (src/ground_state.jl:116-169) for every solve of
+// the batch; a solve leaves the active set at the check where it converges.  The
+// NaN guard of steps 1-10 (src/ground_state.jl:4-29) is evaluated once, at step 10.
+sbec_status sbec_batch_ground_state(sbec_batch* b, int64_t n_steps, double tol, int64_t check_every,
+                                    sbec_gs_result* out) {
+  SBEC_API_BEGIN
+  need(b, "batch");
+  need(out, "out");
+  if (n_steps <= 0 || check_every <= 0) fail(SBEC_ERR_INVALID, "n_steps and check_every must be positive");
+  EngineBase& e = *b->eng;
+  const int n = e.n_solves();
+  std::vector<int> active(n);
+  for (int i = 0; i < n; ++i) active[i] = i;
+  e.batch_set_active(active);
+  std::vector<double> E_prev(n), E(n), pmax(n), dmax(n);
+  e.batch_energies(E_prev.data());
+  e.batch_save_prev();
+  for (int i = 0; i < n; ++i) out[i] = sbec_gs_result{0, NAN, NAN, NAN, n_steps};
+  int64_t step = 0;
+  while (step < n_steps && !active.empty()) {
+    int64_t nxt = std::min(n_steps, (step / check_every + 1) * check_every);
+    if (step < 10) nxt = std::min<int64_t>(nxt, 10);
+    e.batch_itp_steps(nxt - step, e.dt);
+    step = nxt;
+    if (step == std::min<int64_t>(10, n_steps) && e.batch_has_nan())
+      fail(SBEC_ERR_NUMERIC, "NaN detected in ITP within the first 10 steps. Likely potential overflow. Reduce dt.");
+    if (step % check_every == 0) {
+      e.batch_energies(E.data());
+      e.batch_max_abs(pmax.data(), dmax.data());
+      std::vector<int> keep;
+      for (int s : active) {
+        const double dE = std::fabs(E[s] - E_prev[s]);
+        const double dpsi = pmax[s] > 0 ? dmax[s] / pmax[s] : 0.0;
+        out[s].dE = dE;
+        out[s].dpsi = dpsi;
+        if (dE < tol && dpsi < tol) {
+          out[s].converged = 1;
+          out[s].energy = E[s];
+          out[s].steps = step;
+        } else {
+          E_prev[s] = E[s];
+          keep.push_back(s);
+        }
+      }
+      active = keep;
+      e.batch_set_active(active);
+      e.batch_save_prev();
+    }
+  }
+  if (!active.empty()) {
+    e.batch_energies(E.data());
+    for (int s : active) {
+      out[s].energy = E[s];
+      out[s].steps = step;
+    }
+  }
+  e.sync();
   SBEC_API_END
 }
 

@@ -84,24 +84,28 @@ __device__ __forceinline__ float2 cmul_comp(float2 x, float2 wh, float2 wl) {
 }
 __device__ __forceinline__ double2 cmul_comp(double2 x, double2 wh, double2) { return x * wh; }
 
-// Twiddle / phase table: head values and (FP32 only) tails.
+// Twiddle / phase table: head values; FP32 tables store (head, tail) pairs
+// interleaved, entry e at hi[2e], hi[2e+1].
 template <typename R>
 struct Tw {
   const cplx<R>* hi;
   const cplx<R>* lo;
 };
 
+// x * w (or conj w) for a table twiddle.  FP32 tables interleave head and tail
+// (one 16-byte load) and use the compensated product.
 template <typename R>
 __device__ __forceinline__ cplx<R> tw_mul(cplx<R> x, const Tw<R>& t, int idx, bool conj_w) {
-  cplx<R> w = __ldg(t.hi + idx);
   if constexpr (sizeof(R) == 4) {
-    cplx<R> wl = __ldg(t.lo + idx);
+    const float4 w4 = __ldg(reinterpret_cast<const float4*>(t.hi) + idx);
+    float2 wh = mk<float>(w4.x, w4.y), wl = mk<float>(w4.z, w4.w);
     if (conj_w) {
-      w.y = -w.y;
+      wh.y = -wh.y;
       wl.y = -wl.y;
     }
-    return cmul_comp(x, w, wl);
+    return cmul_comp(x, wh, wl);
   } else {
+    cplx<R> w = __ldg(t.hi + idx);
     if (conj_w) w.y = -w.y;
     return x * w;
   }
@@ -115,6 +119,16 @@ __device__ __forceinline__ cplx<R> ldg(const cplx<R>* p) {
 template <typename R>
 __device__ __forceinline__ R ldg_r(const R* p) {
   return __ldg(p);
+}
+
+// Programmatic dependent launch: let the next kernel in the stream be scheduled
+// now, and wait until the previous grid has completed (and its writes are
+// visible) before touching its outputs.  No-ops when launched without the attribute.
+__device__ __forceinline__ void pdl_begin() {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
+  cudaTriggerProgrammaticLaunchCompletion();
+  cudaGridDependencySynchronize();
+#endif
 }
 
 constexpr int kMaxD = 13;      // F <= 6

@@ -143,6 +143,17 @@ class EngineBase {
   virtual void fused_split_steps(long long n, double dt, double kin_dt, bool kin_itp, bool itp,
                                  bool normalize) = 0;
 
+  // Batches of independent solves sharing grid, F, V, dt and Zeeman (per-solve c0, c1, psi).
+  virtual int n_solves() const = 0;
+  virtual void batch_init(int n, const double* c0, const double* c1, const double* psi_all) = 0;
+  virtual void batch_set_active(const std::vector<int>& active) = 0;
+  virtual void batch_itp_steps(long long n, double dt) = 0;    // fused ITP split_step! x n, renormalised
+  virtual void batch_energies(double* E) = 0;                  // total_energy per solve (all solves)
+  virtual void batch_max_abs(double* pmax, double* dmax) = 0;  // vs the saved previous psi (active solves)
+  virtual void batch_save_prev() = 0;
+  virtual bool batch_has_nan() = 0;
+  virtual void batch_get_psi(int solve, double* host) = 0;
+
  protected:
   Setup s_;
   cudaStream_t stream_ = nullptr;

@@ -32,9 +32,9 @@ constexpr int x_lines_per_block() {
 template <typename R, int N>
 constexpr int strided_width() {
   constexpr int tpl = N / PlanOf<R, N>::E;
-  constexpr int sector = 32 / (int)sizeof(cplx<R>);
+  constexpr int seg = 16 / (int)sizeof(cplx<R>);  // at least 16 contiguous bytes per row segment
   int w = 64 / tpl;
-  if (w < sector) w = sector;
+  if (w < seg) w = seg;
   while (w > 1 && (w * tpl > 1024 || (long)w * N * (int)sizeof(cplx<R>) > 96 * 1024)) w /= 2;
   return w;
 }
@@ -121,11 +121,12 @@ class Engine final : public EngineBase {
     V_ = alloc<R>(N_);
     cuda_check(cudaMemsetAsync(V_, 0, sizeof(R) * N_, stream_), "memset V");
     for (int a = 0; a < s_.ndim; ++a) {
-      ptab_[a] = alloc<cplx<R>>(s_.n[a]);
-      ptab_lo_[a] = sizeof(R) == 4 ? alloc<cplx<R>>(s_.n[a]) : nullptr;
+      ptab_[a] = alloc<cplx<R>>((size_t)s_.n[a] * (sizeof(R) == 4 ? 2 : 1));
+      ptab_lo_[a] = nullptr;
     }
     for (int a = 0; a < s_.ndim; ++a) twiddle(s_.n[a]);
-    partials_ = alloc<double>((size_t)kMaxBlocks * 16);
+    partials_n_ = (size_t)kMaxBlocks * 16;
+    partials_ = alloc<double>(partials_n_);
     results_ = alloc<double>(64);
     cuda_check(cudaMallocHost(&host_res_, 64 * sizeof(double)), "cudaMallocHost");
     cuda_check(cudaMallocHost(&host_psi_, sizeof(double) * 2 * nc_), "cudaMallocHost psi");
@@ -485,7 +486,8 @@ class Engine final : public EngineBase {
     }
     if (pending) {
       pb();
-      k_normalize_apply<R><<<grid_for(nc_), 256, 0, stream_>>>(psi_[kPsi], N_ * s_.D, 1, results_ + 40, s_.dV);
+      launch_pdl(k_normalize_apply<R>, dim3(grid_for(nc_)), dim3(256), 0, psi_[kPsi], (int64_t)(N_ * s_.D), 1,
+                 (const double*)(results_ + 40), s_.dV);
       done("normalize", 2.0 * (double)sizeof(cplx<R>) * nc_);
     }
     graph_end(key);
@@ -544,6 +546,195 @@ class Engine final : public EngineBase {
     prof.add_launches(g.launches);
   }
 
+  // ---------------- batches of independent solves ----------------
+  int n_solves() const override { return nsolve_; }
+
+  void batch_init(int n, const double* c0, const double* c1, const double* psi_all) override {
+    if (!fused_path()) fail(SBEC_ERR_UNSUPPORTED, "batched solves need the fused path (no DDI / tensor, D in {1,3,5})");
+    if (n < 1) fail(SBEC_ERR_INVALID, "n_solves must be >= 1");
+    nsolve_ = n;
+    const size_t tot = (size_t)n * nc_;
+    bpsi_ = alloc<cplx<R>>(tot);
+    bprev_ = alloc<cplx<R>>(tot);
+    c0s_ = alloc<R>(n);
+    c1s_ = alloc<R>(n);
+    active_ = alloc<int>(n);
+    bnorm_ = alloc<double>(n);
+    bres_ = alloc<double>((size_t)n * 16);
+    std::vector<R> h0(n), h1(n);
+    for (int i = 0; i < n; ++i) {
+      h0[i] = (R)c0[i];
+      h1[i] = (R)c1[i];
+    }
+    upload(c0s_, h0.data(), n);
+    upload(c1s_, h1.data(), n);
+    // psi: host doubles -> device (converted per solve through the staging buffer)
+    for (int i = 0; i < n; ++i) {
+      std::memcpy(host_psi_, psi_all + (size_t)i * 2 * nc_, sizeof(double) * 2 * nc_);
+      if (sizeof(R) == 8) {
+        cuda_check(cudaMemcpyAsync(bpsi_ + (size_t)i * nc_, host_psi_, sizeof(double) * 2 * nc_,
+                                   cudaMemcpyHostToDevice, stream_), "batch psi upload");
+      } else {
+        cuda_check(cudaMemcpyAsync(stage_, host_psi_, sizeof(double) * 2 * nc_, cudaMemcpyHostToDevice, stream_),
+                   "batch psi upload");
+        pb();
+        k_from_f64<R><<<grid_for(nc_), 256, 0, stream_>>>(stage_, bpsi_ + (size_t)i * nc_, nc_);
+        done("convert", (16.0 + sizeof(cplx<R>)) * nc_);
+      }
+      sync();
+    }
+    const int bps = row_blocks_per_solve();
+    const size_t need = std::max((size_t)n * bps, (size_t)n * 64 * 16) + 64;
+    if (need > partials_n_) {
+      partials_n_ = need;
+      partials_ = alloc<double>(partials_n_);
+    }
+    std::vector<int> all(n);
+    for (int i = 0; i < n; ++i) all[i] = i;
+    batch_set_active(all);
+  }
+
+  void batch_set_active(const std::vector<int>& act) override {
+    n_active_ = (int)act.size();
+    if (n_active_ > 0) upload(active_, act.data(), act.size());
+  }
+
+  void batch_itp_steps(long long n, double dtv) override {
+    if (n <= 0 || n_active_ == 0) return;
+    update_phase(dtv, true);
+    const GraphKey key{3, n, dtv, (double)n_active_, zeeman_p, zeeman_q, active_version_};
+    if (graph_replay(key)) return;
+    graph_begin(key);
+    omap_ = active_;
+    oper_ = s_.D;
+    bool pending = false;
+    for (long long i = 0; i < n; ++i) {
+      // spin mixing is decided per solve from c1[b] inside the pass
+      PotArgs<R> pot = pot_full(dtv / 2, true);
+      pot.rot_a = pot.rot_b = s_.D > 1;
+      if (s_.ndim == 1) {
+        RowArgs<R> a = batch_row_args(pending);
+        a.p1 = pot;
+        a.p2 = pot;
+        a.flags |= RP_POT1 | RP_KIN_X | RP_POT2 | RP_NORM;
+        launch_row(a);
+      } else {
+        RowArgs<R> a = batch_row_args(pending);
+        a.p1 = pot;
+        a.flags |= RP_POT1 | RP_FWD_X;
+        launch_row(a);
+        last_axes_kinetic_on(bpsi_, n_active_);
+        RowArgs<R> b = batch_row_args(false);
+        b.p1 = pot;
+        b.flags |= RP_INV_X | RP_POT1 | RP_NORM;
+        launch_row(b);
+      }
+      pb();
+      launch_pdl(k_seg_finish_rows<R>, dim3((n_active_ + 127) / 128), dim3(128), 0, (const double*)partials_,
+                 row_blocks_per_solve(), n_active_, (const int*)active_, bnorm_);
+      done("reduce_finish", 8.0 * row_blocks_per_solve() * n_active_);
+      pending = true;
+    }
+    pb();
+    launch_pdl(k_batch_normalize<R>, dim3(grid_for(nc_ * n_active_)), dim3(256), 0, bpsi_, (int64_t)nc_,
+               (const int*)active_, n_active_, (const double*)bnorm_, s_.dV);
+    done("normalize", 2.0 * sizeof(cplx<R>) * nc_ * n_active_);
+    omap_ = nullptr;
+    oper_ = 1;
+    graph_end(key);
+  }
+
+  void batch_energies(double* E) override {
+    const int na = n_active_;
+    for (int i = 0; i < nsolve_; ++i) E[i] = NAN;
+    if (na == 0) return;
+    cplx<R>* scr = batch_scratch();
+    pb();
+    k_batch_gather<R><<<grid_for(nc_ * na), 256, 0, stream_>>>(bpsi_, scr, nc_, active_, na, 1);
+    done("elementwise", 2.0 * sizeof(cplx<R>) * nc_ * na);
+    fft_forward_batch(scr, na);
+    const int bpe = (int)std::min<int64_t>(64, (N_ + kRedThreads - 1) / kRedThreads);
+    PhaseTableArgs g = phase_geom(0.0, false);
+    pb();
+    k_batch_kinetic_sum<R><<<dim3(bpe, na), kRedThreads, 0, stream_>>>(scr, N_, s_.D, g, partials_);
+    done("reduce", sizeof(cplx<R>) * (double)nc_ * na);
+    pb();
+    k_seg_finish<1><<<(na + 127) / 128, 128, 0, stream_>>>(partials_, bpe, na, active_, 0, bres_, 16);
+    done("reduce_finish", 8.0 * bpe * na);
+    SBEC_SWITCH_D(s_.D, launch_batch_energy_local_d, bpe, na);
+    std::vector<double> h((size_t)nsolve_ * 16);
+    cuda_check(cudaMemcpyAsync(h.data(), bres_, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, stream_), "fetch");
+    sync();
+    std::vector<int> act(na);
+    cuda_check(cudaMemcpy(act.data(), active_, sizeof(int) * na, cudaMemcpyDeviceToHost), "active");
+    std::vector<R> c0h(nsolve_), c1h(nsolve_);
+    cuda_check(cudaMemcpy(c0h.data(), c0s_, sizeof(R) * nsolve_, cudaMemcpyDeviceToHost), "c0");
+    cuda_check(cudaMemcpy(c1h.data(), c1s_, sizeof(R) * nsolve_, cudaMemcpyDeviceToHost), "c1");
+    const double dV = s_.dV, N = (double)N_;
+    for (int b : act) {
+      const double* r = &h[(size_t)b * 16];
+      double ez = 0.0;
+      for (int c = 0; c < s_.D; ++c) {
+        const double m = (double)(s_.F - c);
+        ez += (-zeeman_p * m + zeeman_q * m * m) * r[1 + c] * dV;
+      }
+      const int o = 1 + s_.D;
+      double e = 0.5 * (r[0] * dV / N) + r[o] * dV + ez + 0.5 * (double)c0h[b] * r[o + 1] * dV +
+                 0.5 * (double)c1h[b] * r[o + 2] * dV;
+      if (s_.c_lhy != 0.0) e += (2.0 / 5.0) * s_.c_lhy * r[o + 3] * dV;
+      E[b] = e;
+    }
+  }
+
+  void batch_max_abs(double* pmax, double* dmax) override {
+    const int na = n_active_;
+    if (na == 0) return;
+    const int bpe = (int)std::min<int64_t>(64, (nc_ + kRedThreads - 1) / kRedThreads);
+    pb();
+    k_batch_max_abs<R><<<dim3(bpe, na), kRedThreads, 0, stream_>>>(bpsi_, bprev_, nc_, nc_, active_, partials_);
+    done("reduce", 2.0 * sizeof(cplx<R>) * (double)nc_ * na);
+    pb();
+    k_seg_finish<2><<<(na + 127) / 128, 128, 0, stream_>>>(partials_, bpe, na, active_, 1, bres_, 16);
+    done("reduce_finish", 16.0 * bpe * na);
+    std::vector<double> h((size_t)nsolve_ * 16);
+    cuda_check(cudaMemcpyAsync(h.data(), bres_, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, stream_), "fetch");
+    sync();
+    for (int b = 0; b < nsolve_; ++b) {
+      pmax[b] = h[(size_t)b * 16];
+      dmax[b] = h[(size_t)b * 16 + 1];
+    }
+  }
+
+  void batch_save_prev() override {
+    cuda_check(cudaMemcpyAsync(bprev_, bpsi_, sizeof(cplx<R>) * nc_ * nsolve_, cudaMemcpyDeviceToDevice, stream_),
+               "prev copy");
+  }
+
+  bool batch_has_nan() override {
+    const int nb = red_blocks(nc_ * nsolve_);
+    pb();
+    k_comp_norms<R, 1><<<nb, kRedThreads, 0, stream_>>>(bpsi_, nc_ * nsolve_, partials_);
+    done("reduce", sizeof(cplx<R>) * (double)nc_ * nsolve_);
+    finish<2>(nb, false, 1);
+    fetch(3);
+    return host_res_[2] > 0;
+  }
+
+  void batch_get_psi(int solve, double* host) override {
+    if (solve < 0 || solve >= nsolve_) fail(SBEC_ERR_INVALID, "solve index out of range");
+    const cplx<R>* src = bpsi_ + (size_t)solve * nc_;
+    if (sizeof(R) == 8) {
+      cuda_check(cudaMemcpyAsync(host_psi_, src, sizeof(double) * 2 * nc_, cudaMemcpyDeviceToHost, stream_), "get");
+    } else {
+      pb();
+      k_to_f64<R><<<grid_for(nc_), 256, 0, stream_>>>(src, stage_, nc_);
+      done("convert", (16.0 + sizeof(cplx<R>)) * nc_);
+      cuda_check(cudaMemcpyAsync(host_psi_, stage_, sizeof(double) * 2 * nc_, cudaMemcpyDeviceToHost, stream_), "get");
+    }
+    sync();
+    std::memcpy(host, host_psi_, sizeof(double) * 2 * nc_);
+  }
+
   void sync() override { cuda_check(cudaStreamSynchronize(stream_), "stream sync"); }
 
  private:
@@ -568,6 +759,22 @@ class Engine final : public EngineBase {
   }
 
   void launch_check(const char* what) { cuda_check(cudaGetLastError(), what); }
+
+  // Launch with programmatic stream serialisation (the kernel calls pdl_begin()).
+  template <typename... KArgs, typename... Args>
+  void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream_;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = use_pdl_ ? 1 : 0;
+    cuda_check(cudaLaunchKernelEx(&cfg, kern, args...), "cudaLaunchKernelEx");
+  }
   void pb() { prof.begin(stream_); }
   void done(const char* name, double bytes) {
     cuda_check(cudaGetLastError(), name);
@@ -586,7 +793,8 @@ class Engine final : public EngineBase {
   template <int K>
   void finish(int nb, bool is_max, int out_off) {
     pb();
-    k_reduce_finish<K><<<1, 32, 0, stream_>>>(partials_, nb, is_max ? 1 : 0, results_ + out_off);
+    launch_pdl(k_reduce_finish<K>, dim3(1), dim3(32), 0, (const double*)partials_, nb, is_max ? 1 : 0,
+               results_ + out_off);
     done("reduce_finish", 8.0 * K * nb);
   }
 
@@ -666,22 +874,21 @@ class Engine final : public EngineBase {
     auto it = tw_.find(n);
     if (it != tw_.end()) return it->second;
     std::vector<cplx<R>> h(n), l(n);
+    const int per = sizeof(R) == 4 ? 2 : 1;  // FP32: (head, tail) interleaved
+    std::vector<cplx<R>> tab((size_t)n * per);
     for (int e = 0; e < n; ++e) {
       const long double ang = -2.0L * 3.141592653589793238462643383279502884L * (long double)e / (long double)n;
       const long double c = std::cos(ang), sn = std::sin(ang);
       h[e] = mk<R>((R)c, (R)sn);
-      l[e] = mk<R>((R)(c - (long double)h[e].x), (R)(sn - (long double)h[e].y));
+      tab[(size_t)e * per] = h[e];
+      if (per == 2) tab[(size_t)e * 2 + 1] = mk<R>((R)(c - (long double)h[e].x), (R)(sn - (long double)h[e].y));
     }
+    (void)l;
     Tw<R> t{};
-    cplx<R>* dh = alloc<cplx<R>>(n);
-    upload(dh, h.data(), n);
+    cplx<R>* dh = alloc<cplx<R>>(tab.size());
+    upload(dh, tab.data(), tab.size());
     t.hi = dh;
     t.lo = nullptr;
-    if (sizeof(R) == 4) {
-      cplx<R>* dl = alloc<cplx<R>>(n);
-      upload(dl, l.data(), n);
-      t.lo = dl;
-    }
     tw_[n] = t;
     return t;
   }
@@ -737,7 +944,7 @@ class Engine final : public EngineBase {
     (void)once;
     const int64_t blocks = (n_lines + LPB - 1) / LPB;
     pb();
-    kern<<<(unsigned)blocks, LPB * TPL, smem, stream_>>>(data, n_lines, mode, phase_ref(), twiddle(NN));
+    launch_pdl(kern, dim3((unsigned)blocks), dim3(LPB * TPL), smem, data, n_lines, mode, phase_ref(), twiddle(NN));
     done(mode == 2 ? "fft_x_kinetic" : "fft_x", 2.0 * (double)sizeof(cplx<R>) * (double)n_lines * NN);
   }
 
@@ -752,8 +959,8 @@ class Engine final : public EngineBase {
     (void)once;
     dim3 grid((unsigned)((inner + W - 1) / W), (unsigned)outer);
     pb();
-    kern<<<grid, W * TPL, smem, stream_>>>(data, S, inner, outer_stride, n_in, n_out, mode, phase_ref(),
-                                           twiddle(NN));
+    launch_pdl(kern, grid, dim3(W * TPL), smem, data, S, inner, outer_stride, n_in, n_out, mode, phase_ref(),
+               twiddle(NN), omap_, oper_);
     done(mode == 2 ? "fft_last_kinetic" : "fft_strided", (double)sizeof(cplx<R>) * (double)(n_in + n_out) * (double)inner * (double)outer);
   }
 
@@ -780,6 +987,78 @@ class Engine final : public EngineBase {
                                  (int64_t)nx * ny, ny, ny, 1);
     }
     if (kinetic) SBEC_SWITCH_POW2(nx, launch_fft_x, buf, (int64_t)ny * nz * D, 1);
+  }
+
+  // ---- batch helpers
+  int row_blocks_per_solve() const {
+    const int nx = s_.n[0];
+    const int tpl = nx / plan_radix_host(sizeof(R) == 4, nx);
+    int rpb = 64 / (s_.D * std::max(tpl, 1));
+    if (rpb < 1) rpb = 1;
+    const int64_t rows = N_ / nx;
+    return (int)((rows + rpb - 1) / rpb);
+  }
+
+  RowArgs<R> batch_row_args(bool scale) {
+    RowArgs<R> a = row_args(scale);
+    a.psi = bpsi_;
+    a.active = active_;
+    a.blocks_per_solve = row_blocks_per_solve();
+    a.solve_stride = nc_;
+    a.c0s = c0s_;
+    a.c1s = c1s_;
+    a.n_slots = n_active_;
+    a.norm_total = bnorm_;
+    return a;
+  }
+
+  cplx<R>* batch_scratch() {
+    if (!bscratch_) bscratch_ = alloc<cplx<R>>((size_t)nc_ * nsolve_);
+    return bscratch_;
+  }
+
+  // kinetic passes above x for n_slots solves addressed through omap_
+  void last_axes_kinetic_on(cplx<R>* buf, int n_slots) {
+    const int nx = s_.n[0], ny = s_.n[1], nz = s_.n[2];
+    const int64_t D = s_.D;
+    if (s_.ndim == 2) {
+      oper_ = (int)D;
+      SBEC_SWITCH_POW2_STRIDED(ny, launch_fft_strided, buf, (int64_t)nx, (int64_t)nx, D * n_slots, N_, ny, ny, 2);
+    } else {
+      oper_ = (int)(nz * D);
+      SBEC_SWITCH_POW2_STRIDED(ny, launch_fft_strided, buf, (int64_t)nx, (int64_t)nx, (int64_t)nz * D * n_slots,
+                               (int64_t)nx * ny, ny, ny, 0);
+      oper_ = (int)D;
+      SBEC_SWITCH_POW2_STRIDED(nz, launch_fft_strided, buf, (int64_t)nx * ny, (int64_t)nx * ny, D * n_slots, N_, nz,
+                               nz, 2);
+      oper_ = (int)(nz * D);
+      SBEC_SWITCH_POW2_STRIDED(ny, launch_fft_strided, buf, (int64_t)nx, (int64_t)nx, (int64_t)nz * D * n_slots,
+                               (int64_t)nx * ny, ny, ny, 1);
+      oper_ = (int)D;
+    }
+  }
+
+  // forward FFT of n_slots compact solves (energy)
+  void fft_forward_batch(cplx<R>* buf, int n_slots) {
+    const int nx = s_.n[0], ny = s_.n[1], nz = s_.n[2];
+    const int64_t D = s_.D;
+    SBEC_SWITCH_POW2(nx, launch_fft_x, buf, (int64_t)ny * nz * D * n_slots, 0);
+    if (s_.ndim >= 2)
+      SBEC_SWITCH_POW2_STRIDED(ny, launch_fft_strided, buf, (int64_t)nx, (int64_t)nx, (int64_t)nz * D * n_slots,
+                               (int64_t)nx * ny, ny, ny, 0);
+    if (s_.ndim >= 3)
+      SBEC_SWITCH_POW2_STRIDED(nz, launch_fft_strided, buf, (int64_t)nx * ny, (int64_t)nx * ny, D * n_slots, N_, nz,
+                               nz, 0);
+  }
+
+  template <int D>
+  void launch_batch_energy_local_d(int bpe, int na) {
+    pb();
+    k_batch_energy_local<R, D><<<dim3(bpe, na), kRedThreads, 0, stream_>>>(bpsi_, N_, nc_, active_, V_, st_, partials_);
+    done("reduce", (sizeof(cplx<R>) * D + sizeof(R)) * (double)N_ * na);
+    pb();
+    k_seg_finish<D + 4><<<(na + 127) / 128, 128, 0, stream_>>>(partials_, bpe, na, active_, 0, bres_ + 1, 16);
+    done("reduce_finish", 8.0 * (D + 4) * bpe * na);
   }
 
   // ---- fused row pass launchers
@@ -829,9 +1108,11 @@ class Engine final : public EngineBase {
     auto kern = k_row_pass<R, NN, D, RPB>;
     static const bool once = (set_smem(kern, smem), true);
     (void)once;
-    const int nb = (int)((a.n_rows + RPB - 1) / RPB);
+    const int bps = (int)((a.n_rows + RPB - 1) / RPB);
+    const int nb = a.active ? bps * a.n_slots : bps;
+    if (a.active && a.blocks_per_solve != bps) fail(SBEC_ERR_INVALID, "row pass blocks per solve mismatch");
     pb();
-    kern<<<nb, D * RPB * TPL, smem, stream_>>>(a, st_, phase_ref(), twiddle(NN));
+    launch_pdl(kern, dim3(nb), dim3(D * RPB * TPL), smem, a, st_, phase_ref(), twiddle(NN));
     done("row_pass", 2.0 * (double)sizeof(cplx<R>) * nc_ + (double)sizeof(R) * N_ * ((a.flags & RP_POT1) ? 1 : 0));
     return nb;
   }
@@ -848,7 +1129,7 @@ class Engine final : public EngineBase {
 
   int launch_row(const RowArgs<R>& a) {
     if (a.flags & RP_NORM) {
-      if ((a.n_rows + 0) > (int64_t)kMaxBlocks * 64) fail(SBEC_ERR_UNSUPPORTED, "too many rows for the norm partials");
+      if ((size_t)a.n_rows * std::max(a.n_slots, 1) > partials_n_) fail(SBEC_ERR_UNSUPPORTED, "too many rows for the norm partials");
     }
     switch (s_.n[0]) {
       case 16: return launch_row_n<16>(a);
@@ -865,9 +1146,9 @@ class Engine final : public EngineBase {
   }
 
   void finish_row_norm(int nb) {
-    if (nb > kMaxBlocks * 16) fail(SBEC_ERR_UNSUPPORTED, "too many row blocks");
+    if ((size_t)nb > partials_n_) fail(SBEC_ERR_UNSUPPORTED, "too many row blocks");
     pb();
-    k_reduce_finish<1><<<1, 32, 0, stream_>>>(partials_, nb, 0, results_ + 40);
+    launch_pdl(k_reduce_finish<1>, dim3(1), dim3(32), 0, (const double*)partials_, nb, 0, results_ + 40);
     done("reduce_finish", 8.0 * nb);
   }
 
@@ -1104,6 +1385,7 @@ class Engine final : public EngineBase {
   cplx<R>* ptab_lo_[3] = {nullptr, nullptr, nullptr};
   std::map<int, Tw<R>> tw_;
   double* partials_ = nullptr;
+  size_t partials_n_ = 0;
   double* results_ = nullptr;
   double* host_res_ = nullptr;
   double* host_psi_ = nullptr;
@@ -1120,7 +1402,19 @@ class Engine final : public EngineBase {
   R* phi_per_ = nullptr;
   cplx<R>* spec_[2] = {nullptr, nullptr};
   std::map<GraphKey, GraphEntry> graphs_;
+  const int* omap_ = nullptr;  // outer-index map for batched strided passes (null: identity)
+  int nsolve_ = 1, n_active_ = 0, active_version_ = 0;
+  cplx<R>* bpsi_ = nullptr;
+  cplx<R>* bprev_ = nullptr;
+  cplx<R>* bscratch_ = nullptr;
+  R* c0s_ = nullptr;
+  R* c1s_ = nullptr;
+  int* active_ = nullptr;
+  double* bnorm_ = nullptr;
+  double* bres_ = nullptr;
+  int oper_ = 1;
   bool use_graphs_ = true;
+  bool use_pdl_ = true;
   bool capturing_ = false;
   long long cap_launch0_ = 0;
   double phase_dt_ = NAN;

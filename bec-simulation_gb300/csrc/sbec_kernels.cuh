@@ -53,8 +53,13 @@ __global__ void k_phase_tables(PhaseOut<R> out, PhaseTableArgs a) {
       im *= a.scale;
     }
     const cplx<R> h = mk<R>((R)re, (R)im);
-    tab[m] = h;
-    if (tlo) tlo[m] = mk<R>((R)(re - (double)h.x), (R)(im - (double)h.y));
+    if constexpr (sizeof(R) == 4) {
+      tab[2 * m] = h;
+      tab[2 * m + 1] = mk<R>((R)(re - (double)h.x), (R)(im - (double)h.y));
+    } else {
+      tab[m] = h;
+    }
+    (void)tlo;
   }
 }
 
@@ -72,6 +77,7 @@ struct PhaseRef {
 template <typename R, int N, int LPB>
 __global__ void __launch_bounds__(LPB * (N / PlanOf<R, N>::E))
 k_fft_x(cplx<R>* __restrict__ data, int64_t n_lines, int mode, PhaseRef<R> ph, Tw<R> tw) {
+  pdl_begin();
   constexpr int TPL = N / PlanOf<R, N>::E;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);
@@ -105,7 +111,8 @@ k_fft_x(cplx<R>* __restrict__ data, int64_t n_lines, int mode, PhaseRef<R> ph, T
 template <typename R, int N, int W>
 __global__ void __launch_bounds__(W * (N / PlanOf<R, N>::E))
 k_fft_strided(cplx<R>* __restrict__ data, int64_t S, int64_t inner, int64_t outer_stride, int n_in,
-              int n_out, int mode, PhaseRef<R> ph, Tw<R> tw) {
+              int n_out, int mode, PhaseRef<R> ph, Tw<R> tw, const int* __restrict__ omap, int oper) {
+  pdl_begin();
   constexpr int TPL = N / PlanOf<R, N>::E;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);
@@ -114,7 +121,8 @@ k_fft_strided(cplx<R>* __restrict__ data, int64_t S, int64_t inner, int64_t oute
   const int tid = threadIdx.x;
   const int64_t i0 = (int64_t)blockIdx.x * W;
   const int nw = (int)min((int64_t)W, inner - i0);
-  cplx<R>* g = data + (int64_t)blockIdx.y * outer_stride + i0;
+  const int64_t o = omap ? (int64_t)omap[blockIdx.y / oper] * oper + blockIdx.y % oper : (int64_t)blockIdx.y;
+  cplx<R>* g = data + o * outer_stride + i0;
   for (int f = tid; f < W * N; f += blockDim.x) {
     const int i = f / W, w = f % W;
     s[f] = (i < n_in && w < nw) ? g[(int64_t)i * S + w] : mk<R>(0, 0);
@@ -465,11 +473,11 @@ __device__ __forceinline__ void diag_apply(cplx<R> (&v)[D], R veff, R tau, int i
 }
 
 template <typename R, int D>
-__device__ __forceinline__ void diag_point(cplx<R> (&v)[D], R Vp, const PotArgs<R>& a) {
+__device__ __forceinline__ void diag_point(cplx<R> (&v)[D], R Vp, const PotArgs<R>& a, R c0) {
   R n = 0;
 #pragma unroll
   for (int c = 0; c < D; ++c) n += abs2(v[c]);
-  const R Vint = a.c0 * n + a.c_lhy * n * sqrt(n);
+  const R Vint = c0 * n + a.c_lhy * n * sqrt(n);
   diag_apply<R, D>(v, Vp + Vint, a.tau_d, a.itp, a.zee, a.zee_lo);
 }
 
@@ -681,13 +689,13 @@ __global__ void __launch_bounds__(256) k_potential(PotArgs<R> a, SpinTabs<R> st)
 #pragma unroll
   for (int c = 0; c < D; ++c) v[c] = a.psi[c * a.N + p];
   const R Vp = a.V[p];
-  if (a.pre_diag) diag_point<R, D>(v, Vp, a);
+  if (a.pre_diag) diag_point<R, D>(v, Vp, a, a.c0);
   if (a.rot_a) spin_mixing_point<R, D>(v, a.c1, a.tau_s, a.itp, st);
   if (a.ddi_rot) {
     spin_rotate<R, D>(v, a.phi[p], a.phi[a.N + p], a.phi[2 * a.N + p], a.tau_ddi, a.itp, st);
   }
   if (a.rot_b) spin_mixing_point<R, D>(v, a.c1, a.tau_s, a.itp, st);
-  if (a.post_diag) diag_point<R, D>(v, Vp, a);
+  if (a.post_diag) diag_point<R, D>(v, Vp, a, a.c0);
 #pragma unroll
   for (int c = 0; c < D; ++c) a.psi[c * a.N + p] = v[c];
   if (a.spin_out) {
@@ -725,37 +733,53 @@ struct RowArgs {
   int64_t n_rows;     // N / nx
   int flags;
   PotArgs<R> p1, p2;  // potential stages (diag, spin mixing)
-  const double* norm_total;  // sum |psi|^2 of the previous pass (RP_SCALE)
+  const double* norm_total;  // per-solve sum |psi|^2 of the previous pass (RP_SCALE)
   double dV;
   double* partials;   // RP_NORM: one double per block
+  // batches of independent solves (null active: a single solve)
+  const int* active;        // slot -> solve index
+  int blocks_per_solve;
+  int64_t solve_stride;     // D*N elements between solves
+  const R* c0s;             // per-solve couplings (null: p1/p2 values)
+  const R* c1s;
+  int n_slots;              // launch size: active slots (host side)
 };
 
 template <typename R, int D>
-__device__ __forceinline__ void pot_stage(cplx<R> (&v)[D], R Vp, const PotArgs<R>& a, const SpinTabs<R>& st) {
-  if (a.pre_diag) diag_point<R, D>(v, Vp, a);
-  if (a.rot_a) spin_mixing_point<R, D>(v, a.c1, a.tau_s, a.itp, st);
-  if (a.rot_b) spin_mixing_point<R, D>(v, a.c1, a.tau_s, a.itp, st);
-  if (a.post_diag) diag_point<R, D>(v, Vp, a);
+__device__ __forceinline__ void pot_stage(cplx<R> (&v)[D], R Vp, const PotArgs<R>& a, const SpinTabs<R>& st, R c0,
+                                          R c1) {
+  const bool sm = a.rot_a && fabs(c1) >= (R)1e-30;
+  if (a.pre_diag) diag_point<R, D>(v, Vp, a, c0);
+  if (sm) spin_mixing_point<R, D>(v, c1, a.tau_s, a.itp, st);
+  if (sm) spin_mixing_point<R, D>(v, c1, a.tau_s, a.itp, st);
+  if (a.post_diag) diag_point<R, D>(v, Vp, a, c0);
 }
 
 template <typename R, int N, int D, int RPB>
 __global__ void __launch_bounds__(D * RPB * (N / PlanOf<R, N>::E))
 k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
+  pdl_begin();
   constexpr int TPL = N / PlanOf<R, N>::E;
   constexpr int NL = D * RPB;  // line = c*RPB + r
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);
   __shared__ double red[32];
   const int tid = threadIdx.x;
-  const int64_t row0 = (int64_t)blockIdx.x * RPB;
+  const int slot = a.active ? (int)(blockIdx.x / a.blocks_per_solve) : 0;
+  const int lblk = a.active ? (int)(blockIdx.x % a.blocks_per_solve) : (int)blockIdx.x;
+  const int b = a.active ? a.active[slot] : 0;
+  cplx<R>* psi = a.psi + (int64_t)b * a.solve_stride;
+  const R c0 = a.c0s ? a.c0s[b] : a.p1.c0;
+  const R c1 = a.c1s ? a.c1s[b] : a.p1.c1;
+  const int64_t row0 = (int64_t)lblk * RPB;
   const int nr = (int)min((int64_t)RPB, a.n_rows - row0);
   R scale = (R)1;
-  if (a.flags & RP_SCALE) scale = (R)(1.0 / sqrt(a.norm_total[0] * a.dV));
+  if (a.flags & RP_SCALE) scale = (R)(1.0 / sqrt(a.norm_total[b] * a.dV));
   for (int f = tid; f < NL * N; f += blockDim.x) {
     const int line = f / N, x = f % N;
     const int c = line / RPB, r = line % RPB;
     cplx<R> v = mk<R>(0, 0);
-    if (r < nr) v = a.psi[c * a.N + (row0 + r) * N + x];
+    if (r < nr) v = psi[c * a.N + (row0 + r) * N + x];
     if (a.flags & RP_SCALE) v = v * scale;
     s[f] = v;
   }
@@ -769,7 +793,7 @@ k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
       cplx<R> v[D];
 #pragma unroll
       for (int c = 0; c < D; ++c) v[c] = s[(c * RPB + r) * N + x];
-      pot_stage<R, D>(v, a.p1.V[(row0 + r) * N + x], a.p1, st);
+      pot_stage<R, D>(v, a.p1.V[(row0 + r) * N + x], a.p1, st, c0, c1);
 #pragma unroll
       for (int c = 0; c < D; ++c) s[(c * RPB + r) * N + x] = v[c];
     }
@@ -790,7 +814,7 @@ k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
 #pragma unroll
       for (int c = 0; c < D; ++c) v[c] = s[(c * RPB + r) * N + x];
       if (a.flags & RP_POT2) {
-        pot_stage<R, D>(v, a.p2.V[(row0 + r) * N + x], a.p2, st);
+        pot_stage<R, D>(v, a.p2.V[(row0 + r) * N + x], a.p2, st, c0, c1);
 #pragma unroll
         for (int c = 0; c < D; ++c) s[(c * RPB + r) * N + x] = v[c];
       }
@@ -802,7 +826,7 @@ k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
   for (int f = tid; f < NL * N; f += blockDim.x) {
     const int line = f / N, x = f % N;
     const int c = line / RPB, r = line % RPB;
-    if (r < nr) a.psi[c * a.N + (row0 + r) * N + x] = s[f];
+    if (r < nr) psi[c * a.N + (row0 + r) * N + x] = s[f];
   }
   if (a.flags & RP_NORM) {
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
@@ -990,6 +1014,7 @@ __device__ __forceinline__ void block_reduce_store(double (&vals)[K], double* pa
 // Sum (or max) K values over nb partial blocks into out[k].
 template <int K>
 __global__ void k_reduce_finish(const double* __restrict__ partials, int nb, int is_max, double* __restrict__ out) {
+  pdl_begin();
   const int k = threadIdx.x;
   if (k >= K) return;
   double x = is_max ? 0.0 : 0.0;
@@ -1159,6 +1184,149 @@ __global__ void __launch_bounds__(kRedThreads) k_max_abs_real(const R* __restric
 }
 
 // ---------------------------------------------------------------------------
+// Batched-solve reductions: grid (blocks per solve, active slots); per-block
+// partials [slot][blk][K], then a per-solve fixed-order finish into out[solve][K].
+// ---------------------------------------------------------------------------
+template <int K>
+__device__ __forceinline__ void block_reduce_store_2d(double (&vals)[K], double* partials, bool is_max) {
+  __shared__ double red[K][kRedThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    double x = vals[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double y = __shfl_down_sync(0xffffffffu, x, o);
+      x = is_max ? fmax(x, y) : x + y;
+    }
+    if (lane == 0) red[k][warp] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < K) {
+    const int k = threadIdx.x;
+    double x = red[k][0];
+    for (int w = 1; w < kRedThreads / 32; ++w) x = is_max ? fmax(x, red[k][w]) : x + red[k][w];
+    partials[((size_t)blockIdx.y * gridDim.x + blockIdx.x) * K + k] = x;
+  }
+}
+
+template <int K>
+__global__ void k_seg_finish(const double* __restrict__ partials, int nb, int n_slots, const int* __restrict__ active,
+                             int is_max, double* __restrict__ out, int out_stride) {
+  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= n_slots) return;
+  const int b = active ? active[slot] : slot;
+  for (int k = 0; k < K; ++k) {
+    double x = 0.0;
+    for (int i = 0; i < nb; ++i) {
+      const double y = partials[((size_t)slot * nb + i) * K + k];
+      x = is_max ? fmax(x, y) : x + y;
+    }
+    out[(size_t)b * out_stride + k] = x;
+  }
+}
+
+// Row-pass norm partials: one per block, blocks grouped by slot.
+template <typename R>
+__global__ void k_seg_finish_rows(const double* __restrict__ partials, int bps, int n_slots,
+                                  const int* __restrict__ active, double* __restrict__ out) {
+  pdl_begin();
+  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= n_slots) return;
+  double x = 0.0;
+  for (int i = 0; i < bps; ++i) x += partials[(size_t)slot * bps + i];
+  out[active ? active[slot] : slot] = x;
+}
+
+// Per-solve [sum n^2... ] energy terms and component sums: K = D + 4 values
+// [comp sums(D), trap, n^2, |f|^2, n^{5/2}] for solve active[blockIdx.y].
+template <typename R, int D>
+__global__ void __launch_bounds__(kRedThreads) k_batch_energy_local(const cplx<R>* __restrict__ psi, int64_t N,
+                                                                    int64_t solve_stride,
+                                                                    const int* __restrict__ active,
+                                                                    const R* __restrict__ V, SpinTabs<R> st,
+                                                                    double* partials) {
+  double acc[D + 4];
+#pragma unroll
+  for (int k = 0; k < D + 4; ++k) acc[k] = 0.0;
+  const cplx<R>* base = psi + (int64_t)active[blockIdx.y] * solve_stride;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (int64_t)gridDim.x * blockDim.x) {
+    double n = 0.0, fz = 0.0, fre = 0.0, fim = 0.0;
+    cplx<R> prev = mk<R>(0, 0);
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      const cplx<R> z = base[c * N + p];
+      const double a2 = (double)z.x * z.x + (double)z.y * z.y;
+      acc[c] += a2;
+      n += a2;
+      fz += (double)st.m[c] * a2;
+      if (c >= 1) {
+        fre += (double)st.fp[c] * ((double)prev.x * z.x + (double)prev.y * z.y);
+        fim += (double)st.fp[c] * ((double)prev.x * z.y - (double)prev.y * z.x);
+      }
+      prev = z;
+    }
+    acc[D] += (double)V[p] * n;
+    acc[D + 1] += n * n;
+    acc[D + 2] += fre * fre + fim * fim + fz * fz;
+    acc[D + 3] += n * n * sqrt(n);
+  }
+  block_reduce_store_2d<D + 4>(acc, partials, false);
+}
+
+// Per-solve kinetic sum over a compact (slot-ordered) transformed scratch buffer.
+template <typename R>
+__global__ void __launch_bounds__(kRedThreads) k_batch_kinetic_sum(const cplx<R>* __restrict__ a, int64_t N, int D,
+                                                                   PhaseTableArgs g, double* partials) {
+  double acc[1] = {0.0};
+  const cplx<R>* base = a + (int64_t)blockIdx.y * N * D;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < N * D; q += (int64_t)gridDim.x * blockDim.x) {
+    int64_t p = q % N;
+    double k2 = 0.0;
+    for (int ax = 0; ax < g.ndim; ++ax) {
+      const int n = g.n[ax];
+      const int m = (int)(p % n);
+      p /= n;
+      const double k = (double)freq_index(m, n) * g.kmult[ax];
+      k2 += k * k;
+    }
+    const cplx<R> z = base[q];
+    acc[0] += k2 * ((double)z.x * z.x + (double)z.y * z.y);
+  }
+  block_reduce_store_2d<1>(acc, partials, false);
+}
+
+// Per-solve [max |psi|, max |psi - prev|].
+template <typename R>
+__global__ void __launch_bounds__(kRedThreads) k_batch_max_abs(const cplx<R>* __restrict__ a,
+                                                               const cplx<R>* __restrict__ b, int64_t n,
+                                                               int64_t solve_stride, const int* __restrict__ active,
+                                                               double* partials) {
+  double acc[2] = {0.0, 0.0};
+  const int64_t off = (int64_t)active[blockIdx.y] * solve_stride;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+    const cplx<R> x = a[off + q], y = b[off + q];
+    acc[0] = fmax(acc[0], hypot((double)x.x, (double)x.y));
+    acc[1] = fmax(acc[1], hypot((double)x.x - (double)y.x, (double)x.y - (double)y.y));
+  }
+  block_reduce_store_2d<2>(acc, partials, true);
+}
+
+// Copy the active solves (slot order) between a strided batch buffer and a compact one.
+template <typename R>
+__global__ void k_batch_gather(const cplx<R>* __restrict__ src, cplx<R>* __restrict__ dst, int64_t per_solve,
+                               const int* __restrict__ active, int n_slots, int to_compact) {
+  const int64_t total = per_solve * n_slots;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+    const int slot = (int)(q / per_solve);
+    const int64_t r = q % per_solve;
+    const int64_t sidx = (int64_t)active[slot] * per_solve + r;
+    if (to_compact) dst[q] = src[sidx];
+    else dst[sidx] = src[q];
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Elementwise helpers
 // ---------------------------------------------------------------------------
 template <typename R>
@@ -1170,11 +1338,25 @@ __global__ void k_scale(cplx<R>* a, int64_t n, double s) {
 // psi /= sqrt(sum_c sums[c]*dV) with the sums already on the device (src/split_step.jl:185-195).
 template <typename R>
 __global__ void k_normalize_apply(cplx<R>* a, int64_t N, int D, const double* __restrict__ sums, double dV) {
+  pdl_begin();
   double ns = 0.0;
   for (int c = 0; c < D; ++c) ns += sums[c] * dV;
   const R s = (R)(1.0 / sqrt(ns));
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < N * D; q += (int64_t)gridDim.x * blockDim.x)
     a[q] = a[q] * s;
+}
+
+// psi_b /= sqrt(norm[b]*dV) for the active solves of a batch.
+template <typename R>
+__global__ void k_batch_normalize(cplx<R>* a, int64_t per_solve, const int* __restrict__ active, int n_slots,
+                                  const double* __restrict__ norm, double dV) {
+  pdl_begin();
+  const int64_t total = per_solve * n_slots;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+    const int b = active[q / per_solve];
+    const R s = (R)(1.0 / sqrt(norm[b] * dV));
+    a[(int64_t)b * per_solve + q % per_solve] = a[(int64_t)b * per_solve + q % per_solve] * s;
+  }
 }
 
 // Per-component scale psi_c *= w[c] (constrained normalisation, src/ground_state.jl:312-317).

@@ -493,4 +493,94 @@ def scan_continuation(*, param_values, make_interactions: Callable, grid, atom, 
     return results
 
 
+def _config(grid: Grid, F: int, zeeman, sim_params: SimParams, precision: str, interactions=None) -> _lib.sbec_config:
+    cfg = _lib.sbec_config()
+    cfg.ndim = grid.config.ndim
+    for d in range(grid.config.ndim):
+        cfg.n[d] = grid.config.n_points[d]
+        cfg.L[d] = grid.config.box_size[d]
+    cfg.F = F
+    if interactions is not None:
+        cfg.c0, cfg.c1, cfg.c_lhy = interactions.c0, interactions.c1, interactions.c_lhy
+    z = zeeman(0.0) if callable(zeeman) else zeeman
+    cfg.zeeman_p, cfg.zeeman_q = z.p, z.q
+    cfg.dt = sim_params.dt
+    cfg.imaginary_time = int(bool(sim_params.imaginary_time))
+    cfg.normalize_every = int(sim_params.normalize_every)
+    if precision not in PRECISIONS:
+        raise _lib.ArgumentError(f"unknown precision {precision!r}")
+    cfg.precision = PRECISIONS[precision]
+    return cfg
+
+
+class GroundStateBatch:
+    """Independent ITP solves that share grid, F, V, dt and Zeeman, stepped together.
+
+    Each solve follows ``find_ground_state``'s loop and convergence test
+    (src/ground_state.jl:116-169) with its own c0, c1 and initial psi; solves leave
+    the batch at the check where they converge.
+    """
+
+    def __init__(self, *, grid: Grid, atom: AtomSpecies, c0s, c1s, psi_inits, zeeman=None, potential=None,
+                 dt: float = 0.005, c_lhy: float = 0.0, precision: str = "fp32"):
+        lib = load()
+        self.grid, self.F, self.D = grid, atom.F, 2 * atom.F + 1
+        self.n = len(psi_inits)
+        if len(c0s) != self.n or len(c1s) != self.n:
+            raise _lib.ArgumentError("c0s, c1s and psi_inits must have the same length")
+        zeeman = ZeemanParams() if zeeman is None else zeeman
+        cfg = _config(grid, atom.F, zeeman, SimParams(dt, 1, True, 1, 1), precision,
+                      InteractionParams(0.0, 0.0, c_lhy))
+        psi = np.concatenate([to_interleaved(p) for p in psi_inits])
+        V = np.ascontiguousarray(evaluate_potential(potential, grid).ravel(order="F"))
+        c0 = np.ascontiguousarray(c0s, dtype=np.float64)
+        c1 = np.ascontiguousarray(c1s, dtype=np.float64)
+        h = C.c_void_p()
+        check(lib.sbec_batch_create(C.byref(cfg), self.n, dptr(c0), dptr(c1), dptr(psi), dptr(V), C.byref(h)))
+        self._h = h
+        self._lib = lib
+
+    def close(self) -> None:
+        if self._h is not None:
+            check(self._lib.sbec_batch_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def ground_state(self, n_steps: int, tol: float, check_every: Optional[int] = None) -> list:
+        out = (_lib.sbec_gs_result * self.n)()
+        ce = max(1, n_steps // 10) if check_every is None else check_every
+        check(self._lib.sbec_batch_ground_state(self._h, int(n_steps), float(tol), int(ce), out))
+        return [dict(converged=bool(r.converged), energy=r.energy, dE=r.dE, dpsi=r.dpsi, steps=r.steps) for r in out]
+
+    def psi(self, i: int) -> np.ndarray:
+        n = int(np.prod(self.grid.config.n_points)) * self.D
+        buf = np.empty(2 * n)
+        check(self._lib.sbec_batch_get_psi(self._h, int(i), dptr(buf)))
+        return from_interleaved(buf, self.grid.config.n_points, self.D)
+
+    def energies(self) -> np.ndarray:
+        E = np.empty(self.n)
+        check(self._lib.sbec_batch_energies(self._h, dptr(E)))
+        return E
+
+
+def find_ground_states_batched(*, grid: Grid, atom: AtomSpecies, interactions: list, psi_inits: list, zeeman=None,
+                               potential=None, dt: float = 0.005, n_steps: int = 10000, tol: float = 1e-10,
+                               precision: str = "fp32") -> list:
+    """``find_ground_state`` for many (interactions, psi0) pairs at once; one result per pair."""
+    b = GroundStateBatch(grid=grid, atom=atom, c0s=[ip.c0 for ip in interactions], c1s=[ip.c1 for ip in interactions],
+                         psi_inits=psi_inits, zeeman=zeeman, potential=potential, dt=dt,
+                         c_lhy=interactions[0].c_lhy if interactions else 0.0, precision=precision)
+    res = b.ground_state(n_steps, tol)
+    for i, r in enumerate(res):
+        r["psi"] = b.psi(i)
+    b.close()
+    return res
+
+
 __all__ = [n for n in dir() if not n.startswith("_")]

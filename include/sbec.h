@@ -187,6 +187,23 @@ sbec_status sbec_spin_density(sbec_ws* ws, double* out);
  * src/ddi_padded.jl:55-85); padded selects the zero-padded convolution. */
 sbec_status sbec_ddi_potential(sbec_ws* ws, int32_t padded, double* out);
 
+/* ---- batches of independent ground-state solves ---------------------------
+ * The multistart / continuation / phase-boundary callers of find_ground_state
+ * (src/ground_state.jl:239-378, src/phase_boundary.jl:9) run many independent ITP
+ * solves; a batch steps all solves that share grid, F, V, dt and Zeeman in the same
+ * kernels (per-solve c0, c1 and psi), each with the find_ground_state convergence
+ * test of src/ground_state.jl:138-159.  cfg: imaginary_time=1, normalize_every=1,
+ * contact couplings only (no c_extra/DDI); cfg->c0/c1 are ignored.
+ * psi: n_solves consecutive host psi buffers (reference layout). */
+typedef struct sbec_batch sbec_batch;
+sbec_status sbec_batch_create(const sbec_config* cfg, int32_t n_solves, const double* c0, const double* c1,
+                              const double* psi, const double* V, sbec_batch** out);
+sbec_status sbec_batch_destroy(sbec_batch* b);
+sbec_status sbec_batch_ground_state(sbec_batch* b, int64_t n_steps, double tol, int64_t check_every,
+                                    sbec_gs_result* out);
+sbec_status sbec_batch_get_psi(sbec_batch* b, int32_t solve, double* psi);
+sbec_status sbec_batch_energies(sbec_batch* b, double* E);
+
 /* ---- tracing (the reference's @timeit_debug substep timers, src/split_step.jl:15-131) ---- */
 typedef struct sbec_kernel_stat {
   char name[32];             /* kernel category: fft_x, fft_last_kinetic, potential, tensor, ddi_*, reduce, ... */

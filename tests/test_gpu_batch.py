@@ -1,0 +1,56 @@
+"""Batched ground states (multistart / continuation callers of find_ground_state):
+every solve of a batch must give the same result as its own find_ground_state
+run on the oracle (FP64), and stay within 1e-6 in energy in the FP32-bulk form."""
+
+import numpy as np
+import pytest
+
+import oracle as O
+import spinorbec as S
+from parity_util import ENERGY_TOL_FP64, PSI_TOL_FP64, rel_psi_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _starts(og, F, c1s):
+    states = ["polar", "ferromagnetic", "uniform", "antiferromagnetic", "random"]
+    psis, inter = [], []
+    for i, c1 in enumerate(c1s):
+        st = states[i % len(states)]
+        psis.append(O.init_psi(og, F, st, seed=100 + i))
+        inter.append((10.0, c1))
+    return psis, inter
+
+
+@pytest.mark.parametrize("n,L", [((64,), (16.0,)), ((32, 32), (16.0, 16.0))])
+def test_batch_matches_individual_fp64(gpu, n, L):
+    og = O.make_grid(O.GridConfig(n, L))
+    hg = S.make_grid(S.GridConfig(n, L))
+    c1s = [-1.0, -0.5, -0.1, 0.0, 0.3, 0.7, 1.0]
+    psis, inter = _starts(og, 1, c1s)
+    kw = dict(dt=0.005, n_steps=600, tol=1e-9)
+    res = S.find_ground_states_batched(grid=hg, atom=S.Rb87, interactions=[S.InteractionParams(a, b) for a, b in inter],
+                                       psi_inits=psis, zeeman=S.ZeemanParams(0.2, 0.05), potential=S.HarmonicTrap(*([1.0] * len(n))),
+                                       precision="fp64", **kw)
+    for (c0, c1), p0, r in zip(inter, psis, res):
+        ro = O.find_ground_state(grid=og, atom=O.Rb87, interactions=O.InteractionParams(c0, c1),
+                                 zeeman=O.ZeemanParams(0.2, 0.05), V=O.harmonic_potential(og, (1.0,) * len(n)),
+                                 psi_init=p0, **kw)
+        assert r["converged"] == ro["converged"] and r["steps"] == ro["steps"]
+        assert abs(r["energy"] - ro["energy"]) <= ENERGY_TOL_FP64 * abs(ro["energy"]) * 10
+        assert rel_psi_err(r["psi"], ro["workspace"].psi) < PSI_TOL_FP64
+
+
+def test_batch_fp32_energy(gpu):
+    n, L = (64, 64), (20.0, 20.0)
+    og = O.make_grid(O.GridConfig(n, L))
+    hg = S.make_grid(S.GridConfig(n, L))
+    c1s = [-0.5, 0.5]
+    psis, inter = _starts(og, 1, c1s)
+    kw = dict(dt=0.005, n_steps=1000, tol=1e-8)
+    res = S.find_ground_states_batched(grid=hg, atom=S.Rb87, interactions=[S.InteractionParams(a, b) for a, b in inter],
+                                       psi_inits=psis, potential=S.HarmonicTrap(1.0, 1.0), precision="fp32", **kw)
+    for (c0, c1), p0, r in zip(inter, psis, res):
+        ro = O.find_ground_state(grid=og, atom=O.Rb87, interactions=O.InteractionParams(c0, c1),
+                                 V=O.harmonic_potential(og, (1.0, 1.0)), psi_init=p0, **kw)
+        assert abs(r["energy"] - ro["energy"]) / abs(ro["energy"]) < 1e-6
