@@ -5,6 +5,7 @@
 
 #include <cmath>
 #include <complex>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <tuple>
@@ -114,6 +115,9 @@ class Engine final : public EngineBase {
  public:
   explicit Engine(const Setup& s) : EngineBase(s) {
     cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+    // SBEC_GRAPHS=0 / SBEC_PDL=0 turn off graph replay / programmatic dependent launch.
+    if (const char* g = std::getenv("SBEC_GRAPHS")) use_graphs_ = std::atoi(g) != 0;
+    if (const char* p = std::getenv("SBEC_PDL")) use_pdl_ = std::atoi(p) != 0;
     const int D = s_.D;
     N_ = s_.N;
     nc_ = N_ * D;
