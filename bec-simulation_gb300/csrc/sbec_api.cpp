@@ -44,6 +44,14 @@ namespace {
 
 thread_local std::string g_err;
 
+}  // namespace
+
+namespace sbec {
+void set_last_error(const std::string& msg) { g_err = msg; }
+}  // namespace sbec
+
+namespace {
+
 #define SBEC_API_BEGIN try {
 #define SBEC_API_END                                      \
   }                                                       \

@@ -13,6 +13,8 @@
 namespace sbec {
 
 void cuda_check(cudaError_t e, const char* what);
+// Message returned by sbec_last_error() on the calling thread.
+void set_last_error(const std::string& msg);
 
 // Per-kernel-category launch counts and (when enabled) CUDA-event durations on
 // the workspace stream; the counterpart of the reference's @timeit_debug

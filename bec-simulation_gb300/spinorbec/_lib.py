@@ -155,6 +155,7 @@ _PROTOS = {
     "sbec_batch_ground_state": (C.c_int, [_P, C.c_int64, C.c_double, C.c_int64, C.POINTER(sbec_gs_result)]),
     "sbec_batch_get_psi": (C.c_int, [_P, C.c_int32, _D]),
     "sbec_batch_energies": (C.c_int, [_P, _D]),
+    "sbec_component_norms_noalloc": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_void_p]),
 }
 
 _lib = None

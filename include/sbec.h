@@ -220,6 +220,28 @@ sbec_status sbec_launch_count(sbec_ws* ws, int64_t* n);
 /* The workspace's CUDA stream (cudaStream_t), for callers that order or time work on it. */
 sbec_status sbec_ws_stream(sbec_ws* ws, void** stream);
 
+/* ---- allocation-free reduction --------------------------------------------
+ * No counterpart in the reference: an extra entry point for callers that cannot
+ * allocate GPU memory at the time of the call -- code running while a stream is
+ * captured into a CUDA graph, or hosts whose device memory belongs to another
+ * allocator (e.g. a Julia CUDA.jl pool) that must not see cudaMalloc/cudaFree.
+ * Computes sums_dev[c] = sum_x |psi_c(x)|^2 for c < n_components and writes the
+ * number of NaN entries to sums_dev[n_components], for a device wavefunction in
+ * the reference layout (interleaved complex FP64, planar per component).  The
+ * norm and <Fz> of total_norm / magnetization follow as dV*sum_c sums_dev[c] and
+ * dV*sum_c (F-c)*sums_dev[c].  psi_dev and sums_dev are device pointers owned by
+ * the caller; the work is queued on `stream` (a cudaStream_t, NULL = default).
+ * Scratch lives in a fixed device array (256 KiB per device, kept until exit), so
+ * the call performs no allocation.  The first call on a device resolves that
+ * array's address (no allocation, but make it before any stream capture).  All
+ * calls on a device share the array: calls whose kernels overlap on the GPU race.
+ * Limits: 1 <= n_components <= SBEC_NOALLOC_MAX_COMPONENTS,
+ * 1 <= n_points <= SBEC_NOALLOC_MAX_POINTS; otherwise SBEC_ERR_INVALID. */
+#define SBEC_NOALLOC_MAX_COMPONENTS 16
+#define SBEC_NOALLOC_MAX_POINTS (1LL << 31)
+sbec_status sbec_component_norms_noalloc(const double* psi_dev, int64_t n_points, int32_t n_components,
+                                         double* sums_dev, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
