@@ -168,12 +168,18 @@ int snapshot(sbec_ws* ws, sbec_callback cb, void* user) {
   sbec_snapshot sn{};
   sn.t = e.t;
   sn.step = e.step;
-  sn.energy = total_energy(e);
-  norm_and_mz(e, &sn.norm, &sn.magnetization);
   const Setup& s = e.setup();
-  ws->host_psi.resize((size_t)2 * s.N * s.D);
-  e.get_psi(ws->host_psi.data());
-  sn.psi = ws->host_psi.data();
+  std::vector<double> sums(s.D);
+  const sbec_energy_terms t = e.energy_terms_and_norms(sums.data());
+  sn.energy = t.kinetic + t.trap + t.zeeman + t.c0 + t.c1 + t.ddi + t.lhy + t.tensor;
+  double n = 0.0, m = 0.0;
+  for (int c = 0; c < s.D; ++c) {
+    n += sums[c];
+    m += (double)(s.F - c) * sums[c] * s.dV;
+  }
+  sn.norm = n * s.dV;
+  sn.magnetization = m;
+  sn.psi = e.psi_to_pinned();
   return cb(user, &sn);
 }
 

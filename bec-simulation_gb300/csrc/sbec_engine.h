@@ -128,6 +128,10 @@ class EngineBase {
   // reductions (synchronise the stream)
   virtual void comp_norms(double* sums, double* nan_count) = 0;  // sum |psi_c|^2 per component
   virtual sbec_energy_terms energy_terms() = 0;
+  // total_energy terms plus the component sums of the same psi (one device->host fetch)
+  virtual sbec_energy_terms energy_terms_and_norms(double* comp_sums) = 0;
+  // psi downloaded into the workspace's pinned staging buffer (valid until the next call)
+  virtual const double* psi_to_pinned() = 0;
   virtual double l2_change(int a, int b) = 0;                      // ||a-b||^2/||b||^2
   virtual void max_abs(int a, int b, double* max_a, double* max_diff) = 0;
   virtual double ddi_phi_max() = 0;                                // last periodic Φ (ITP check)

@@ -300,7 +300,15 @@ class Engine final : public EngineBase {
     if (nan_count) *nan_count = host_res_[1 + s_.D];
   }
 
-  sbec_energy_terms energy_terms() override {
+  sbec_energy_terms energy_terms() override { return energy_terms_and_norms(nullptr); }
+
+  const double* psi_to_pinned() override {
+    download_psi_to_pinned();
+    sync();
+    return host_psi_;
+  }
+
+  sbec_energy_terms energy_terms_and_norms(double* comp_sums) override {
     sbec_energy_terms e{};
     const double dV = s_.dV;
     // kinetic: forward FFT of a copy, sum k^2 |psi_hat|^2 dV / N (src/energy.jl:56-65)
@@ -353,6 +361,8 @@ class Engine final : public EngineBase {
     if (s_.ddi) e.ddi = 0.5 * host_res_[31] * dV;
     if (s_.c_lhy != 0.0) e.lhy = (2.0 / 5.0) * s_.c_lhy * host_res_[23] * dV;
     if (s_.tensor) e.tensor = host_res_[30] * dV;
+    if (comp_sums)
+      for (int c = 0; c < s_.D; ++c) comp_sums[c] = host_res_[1 + c];
     return e;
   }
 
@@ -1418,7 +1428,7 @@ class Engine final : public EngineBase {
   double* bres_ = nullptr;
   int oper_ = 1;
   bool use_graphs_ = true;
-  bool use_pdl_ = true;
+  bool use_pdl_ = false;  // SBEC_PDL=1 enables; measured slower for these short kernels
   bool capturing_ = false;
   long long cap_launch0_ = 0;
   double phase_dt_ = NAN;
