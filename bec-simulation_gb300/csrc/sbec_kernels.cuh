@@ -619,7 +619,11 @@ __device__ __forceinline__ void euler_point(cplx<R> (&v)[D], R px, R py, R pz, R
 
 // exp(-i tau phi·F) v (or exp(-tau phi·F) v in imaginary time) by a Taylor series
 // of the tridiagonal phi·F, with sub-steps so each has ||tau phi·F|| <= 1/2 and the
-// series cut once the bound of the next term is below eps.  Used by the FP32 form
+// series cut once the bound of the next term is below eps.  The series is summed by
+// Horner's scheme, v + (X/1)(v + (X/2)(v + ...)): adding the terms largest-first drops
+// every term below half an ulp of the running sum, a truncation whose norm error has
+// one sign (about -1e-7 per unit rotation angle in FP32), while the nested form adds
+// each correction to a value of its own size.  Used by the FP32 form
 // in place of the Euler-angle phases, whose FP32 recurrences carry a systematic
 // magnitude error; the operator is the same exp(-i dt phi·F) as
 // src/spinor_utils.jl:82-166 and the skip threshold |phi||dt| < 1e-14 is kept.
@@ -642,21 +646,18 @@ __device__ __forceinline__ void rotate_taylor(cplx<R> (&v)[D], R px, R py, R pz,
   }
   const R dt = tau / (R)nsub;
   for (int sub = 0; sub < nsub; ++sub) {
-    cplx<R> term[D], acc[D];
+    cplx<R> y[D];
 #pragma unroll
-    for (int c = 0; c < D; ++c) term[c] = acc[c] = v[c];
-    for (int k = 1; k <= K; ++k) {
-      cplx<R> y[D];
-      nF_apply<R, D>(term, px, py, pz, st, y);
+    for (int c = 0; c < D; ++c) y[c] = v[c];
+    for (int k = K; k >= 1; --k) {
+      cplx<R> t[D];
+      nF_apply<R, D>(y, px, py, pz, st, t);
       const R f = dt / (R)k;
 #pragma unroll
-      for (int c = 0; c < D; ++c) {
-        term[c] = itp ? (-f) * y[c] : mul_mi(f * y[c]);
-        acc[c] += term[c];
-      }
+      for (int c = 0; c < D; ++c) y[c] = v[c] + (itp ? (-f) * t[c] : mul_mi(f * t[c]));
     }
 #pragma unroll
-    for (int c = 0; c < D; ++c) v[c] = acc[c];
+    for (int c = 0; c < D; ++c) v[c] = y[c];
   }
 }
 
@@ -914,38 +915,33 @@ __device__ __forceinline__ void tensor_point(cplx<R> (&v)[D], const TensorArgs<R
     }
     K = K + 1;
   }
+  // Horner's scheme (as in rotate_taylor): y <- v + (-i dtau / k) h y for k = K..1.
   const R dtau = a.tau / (R)nsub;
   for (int sub = 0; sub < nsub; ++sub) {
-    cplx<R> term[D], acc[D];
+    cplx<R> y[D];
 #pragma unroll
-    for (int c = 0; c < D; ++c) {
-      term[c] = v[c];
-      acc[c] = v[c];
-    }
-    for (int k = 1; k <= K; ++k) {
-      cplx<R> y[D];
+    for (int c = 0; c < D; ++c) y[c] = v[c];
+    for (int k = K; k >= 1; --k) {
+      cplx<R> t[D];
 #pragma unroll
-      for (int c = 0; c < D; ++c) y[c] = mk<R>(0, 0);
+      for (int c = 0; c < D; ++c) t[c] = mk<R>(0, 0);
       int idx = 0;
 #pragma unroll
       for (int c = 0; c < D; ++c) {
 #pragma unroll
         for (int cp = c; cp < D; ++cp) {
           const cplx<R> h = hs[idx * hstride];
-          y[c] += h * term[cp];
-          if (cp != c) y[cp] += cmulc(h, term[c]);
+          t[c] += h * y[cp];
+          if (cp != c) t[cp] += cmulc(h, y[c]);
           ++idx;
         }
       }
       const R f = dtau / (R)k;
 #pragma unroll
-      for (int c = 0; c < D; ++c) {
-        term[c] = a.itp ? (-f) * y[c] : mul_mi(f * y[c]);
-        acc[c] += term[c];
-      }
+      for (int c = 0; c < D; ++c) y[c] = v[c] + (a.itp ? (-f) * t[c] : mul_mi(f * t[c]));
     }
 #pragma unroll
-    for (int c = 0; c < D; ++c) v[c] = acc[c];
+    for (int c = 0; c < D; ++c) v[c] = y[c];
   }
   (void)F;
 }
