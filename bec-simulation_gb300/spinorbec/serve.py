@@ -1,0 +1,224 @@
+"""Continuous-batching request server for ground-state and dynamics solves.
+
+Requests arrive over time (e.g. a seeded Poisson stream).  A request is admitted
+as soon as its device footprint fits the HBM budget and a slot is free; each
+admitted request gets a resident workspace with its own CUDA stream and runs in a
+worker thread (the C calls release the GIL), so the work of requests that are in
+flight together overlaps on the GPU.  When a request finishes, its workspace is
+freed and the next waiting requests are admitted.  Every kernel and reduction of
+the engine is deterministic, so a request's result does not depend on what else
+is in flight.
+
+Per request the server records queueing, service and end-to-end latency; run()
+returns them with throughput and p50/p99.
+"""
+
+from __future__ import annotations
+
+import math
+import threading
+import time
+from concurrent.futures import ThreadPoolExecutor
+from dataclasses import dataclass
+from typing import Callable, Optional
+
+import numpy as np
+
+from . import api
+from .host import (AtomSpecies, GridConfig, HarmonicTrap, InteractionParams, SimParams, ZeemanParams, init_psi,
+                   make_grid)
+
+
+@dataclass
+class SolveRequest:
+    """One solve: a ground state (find_ground_state) or a real-time run (run_simulation!)."""
+
+    rid: int
+    kind: str                 # "ground_state" | "dynamics"
+    n_points: tuple
+    box_size: tuple
+    F: int
+    c0: float
+    c1: float
+    steps: int
+    dt: float = 0.005
+    enable_ddi: bool = False
+    c_dd: float = 0.0
+    tol: float = 1e-8
+    arrival: float = 0.0      # seconds after the start of the stream
+    precision: str = "fp32"
+    omega: float = 1.0
+
+
+@dataclass
+class SolveResult:
+    rid: int
+    kind: str
+    energy: float
+    norm: float
+    converged: Optional[bool]
+    steps: int
+    arrival: float
+    admitted: float
+    finished: float
+    footprint: int
+
+    @property
+    def latency(self) -> float:
+        return self.finished - self.arrival
+
+    @property
+    def queueing(self) -> float:
+        return self.admitted - self.arrival
+
+
+def footprint_bytes(req: SolveRequest, ddi_padding: bool = False) -> int:
+    """Upper bound of the device memory one request's workspace allocates: four psi slots
+    and a scratch copy, V and a 3-field temporary, the FP64 staging buffer of the FP32 form,
+    and for DDI the spin density, two phi fields and the half-spectrum of three fields
+    (periodic, plus the zero-padded one when enabled); 10 % and 8 MiB on top for tables,
+    reduction partials and allocation granularity."""
+    N = int(np.prod(req.n_points))
+    nc = N * (2 * req.F + 1)
+    s = 8 if req.precision.startswith("fp32") else 16   # bytes per complex element
+    r = s // 2
+    total = 5 * nc * s + 4 * N * r
+    if s == 8:
+        total += nc * 16
+    if req.enable_ddi:
+        total += 9 * N * r + (3 * N * s) // 2
+        if ddi_padding:
+            total += 6 * N * s
+    return int(total * 1.1) + (8 << 20)
+
+
+def run_request(req: SolveRequest) -> dict:
+    """Run one request to completion on its own workspace (and stream); returns its results."""
+    grid = make_grid(GridConfig(req.n_points, req.box_size))
+    atom = AtomSpecies("req", req.F)
+    inter = InteractionParams(req.c0, req.c1)
+    trap = HarmonicTrap(*([req.omega] * len(req.n_points)))
+    if req.kind == "ground_state":
+        r = api.find_ground_state(grid=grid, atom=atom, interactions=inter, potential=trap, dt=req.dt,
+                                  n_steps=req.steps, tol=req.tol, initial_state="polar",
+                                  enable_ddi=req.enable_ddi, c_dd=req.c_dd if req.enable_ddi else float("nan"),
+                                  precision=req.precision)
+        ws = r["workspace"]
+        out = dict(energy=r["energy"], norm=api.total_norm(ws), converged=r["converged"], steps=r["steps"])
+        ws.close()
+        return out
+    psi = init_psi(grid, req.F, "ferromagnetic" if req.F > 1 else "polar")
+    ws = api.make_workspace(grid=grid, atom=atom, interactions=inter, potential=trap,
+                            zeeman=ZeemanParams(0.0, 0.1),
+                            sim_params=SimParams(req.dt, req.steps, False, None, req.steps), psi_init=psi,
+                            enable_ddi=req.enable_ddi, c_dd=req.c_dd, precision=req.precision)
+    res = api.run_simulation(ws, keep_psi=False)
+    out = dict(energy=res.energies[-1], norm=res.norms[-1], converged=None, steps=req.steps)
+    ws.close()
+    return out
+
+
+class Server:
+    """Admission by HBM budget and slots; concurrent resident workspaces."""
+
+    def __init__(self, hbm_budget_bytes: float = 150e9, max_slots: int = 32,
+                 runner: Callable[[SolveRequest], dict] = run_request):
+        self.budget = float(hbm_budget_bytes)
+        self.max_slots = int(max_slots)
+        self.runner = runner
+        self._used = 0.0
+        self._active = 0
+        self.peak_used = 0.0
+        self.peak_active = 0
+        self._cv = threading.Condition()
+
+    def _admit(self, fp: int) -> None:
+        with self._cv:
+            while self._active >= self.max_slots or (self._used + fp > self.budget and self._active > 0):
+                self._cv.wait()
+            self._used += fp
+            self._active += 1
+            self.peak_used = max(self.peak_used, self._used)
+            self.peak_active = max(self.peak_active, self._active)
+
+    def _release(self, fp: int) -> None:
+        with self._cv:
+            self._used -= fp
+            self._active -= 1
+            self._cv.notify_all()
+
+    def run(self, requests: list, realtime: bool = True) -> dict:
+        """Serve `requests`; returns per-request results and stats.
+
+        With realtime=True each request is submitted at its arrival time (seconds from
+        the call); otherwise all are submitted at once and queue by arrival order."""
+        t0 = time.perf_counter()
+        results: list = []
+        lock = threading.Lock()
+
+        def serve(req: SolveRequest):
+            fp = footprint_bytes(req)
+            if fp > self.budget:
+                raise MemoryError(f"request {req.rid} needs {fp / 1e9:.1f} GB > budget")
+            self._admit(fp)
+            admitted = time.perf_counter() - t0
+            try:
+                out = self.runner(req)
+            finally:
+                self._release(fp)
+            fin = time.perf_counter() - t0
+            with lock:
+                results.append(SolveResult(req.rid, req.kind, out["energy"], out["norm"], out["converged"],
+                                           out["steps"], req.arrival, admitted, fin, fp))
+
+        order = sorted(requests, key=lambda r: r.arrival)
+        with ThreadPoolExecutor(max_workers=self.max_slots + 4) as ex:
+            futs = []
+            for req in order:
+                if realtime:
+                    wait = req.arrival - (time.perf_counter() - t0)
+                    if wait > 0:
+                        time.sleep(wait)
+                futs.append(ex.submit(serve, req))
+            for f in futs:
+                f.result()
+        wall = time.perf_counter() - t0
+        lat = np.array([r.latency for r in results])
+        return dict(results=sorted(results, key=lambda r: r.rid), wall_s=wall,
+                    solves_per_s=len(results) / wall if wall > 0 else float("nan"),
+                    p50_latency_s=float(np.percentile(lat, 50)) if len(lat) else float("nan"),
+                    p99_latency_s=float(np.percentile(lat, 99)) if len(lat) else float("nan"))
+
+
+def poisson_requests(n: int, rate: float = 200.0, seed: int = 5, *, max_points_3d: int = 128,
+                     max_steps: int = 5000, min_steps: int = 500, precision: str = "fp32") -> list:
+    """Seeded request stream: dimension uniform over 1-D/2-D/3-D with power-of-two sizes drawn
+    log-uniformly (1-D 256..4096, 2-D 64^2..512^2, 3-D 32^3..max^3), F in {1, 2, 6}, c0 ~ U[5, 20],
+    c1 ~ U[-1, 1], DDI on for F = 6, steps ~ U{min..max}, half ground states, half dynamics."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    t = 0.0
+    reqs = []
+    for i in range(n):
+        t += rng.exponential(1.0 / rate)
+        dim = int(rng.integers(1, 4))
+        if dim == 1:
+            e = int(rng.integers(8, 13))
+            npts = (2 ** e,)
+            box = (40.0,)
+        elif dim == 2:
+            e = int(rng.integers(6, 10))
+            npts = (2 ** e, 2 ** e)
+            box = (20.0, 20.0)
+        else:
+            hi = int(round(math.log2(max_points_3d)))
+            e = int(rng.integers(5, hi + 1))
+            npts = (2 ** e,) * 3
+            box = (16.0,) * 3
+        F = int(rng.choice([1, 2, 6]))
+        kind = "ground_state" if rng.random() < 0.5 else "dynamics"
+        reqs.append(SolveRequest(rid=i, kind=kind, n_points=npts, box_size=box, F=F,
+                                 c0=float(rng.uniform(5.0, 20.0)), c1=float(rng.uniform(-1.0, 1.0)),
+                                 steps=int(rng.integers(min_steps, max_steps + 1)),
+                                 dt=0.005 if kind == "ground_state" else 1e-3,
+                                 enable_ddi=(F == 6), c_dd=20.0 if F == 6 else 0.0, arrival=t, precision=precision))
+    return reqs
