@@ -218,6 +218,183 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+# ----------------------------------------------------------------------------- batched ground states
+def batched_workload(S, n_solves: int = 512, seed: int = 4242):
+    """The 512-solve batch: c1 on 64 values in [-1, 1] x 8 starts (polar, ferromagnetic,
+    uniform, antiferromagnetic, 4 seeded random), grid 64^2 / 128^2 / 256^2 drawn per solve."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    c1s = np.linspace(-1.0, 1.0, 64)
+    starts = ["polar", "ferromagnetic", "uniform", "antiferromagnetic", "random", "random", "random", "random"]
+    sizes = rng.choice([64, 128, 256], size=n_solves)
+    jobs = []
+    for i in range(n_solves):
+        c1 = float(c1s[i // 8 % 64])
+        st = starts[i % 8]
+        jobs.append(dict(idx=i, n=int(sizes[i]), c1=c1, state=st, seed=1000 + i))
+    return jobs
+
+
+def run_batched(S, jobs, precision: str, n_steps: int, tol: float) -> tuple:
+    """Runs every job through GroundStateBatch grouped by grid size; returns (seconds, results by idx)."""
+    import time as _t
+    res = {}
+    total = 0.0
+    for n in sorted({j["n"] for j in jobs}):
+        group = [j for j in jobs if j["n"] == n]
+        g = S.make_grid(S.GridConfig((n, n), (20.0, 20.0)))
+        psis = [S.init_psi(g, 1, j["state"], seed=j["seed"]) for j in group]
+        b = S.GroundStateBatch(grid=g, atom=S.Rb87, c0s=[10.0] * len(group), c1s=[j["c1"] for j in group],
+                               psi_inits=psis, potential=S.HarmonicTrap(1.0, 1.0), dt=0.005, precision=precision)
+        t0 = _t.perf_counter()
+        r = b.ground_state(n_steps, tol, max(1, n_steps // 10))
+        total += _t.perf_counter() - t0
+        b.close()
+        for j, x in zip(group, r):
+            res[j["idx"]] = x
+    return total, res
+
+
+def bench_batched(S, sample: int = 6, n_steps: int = 10000, tol: float = 1e-8) -> dict:
+    jobs = batched_workload(S)
+    secs32, r32 = run_batched(S, jobs, "fp32", n_steps, tol)
+    # plain FP64 form, one solve at a time (find_ground_state per solve), on a seeded sample
+    rng = np.random.Generator(np.random.PCG64(7))
+    pick = [int(i) for i in rng.choice(len(jobs), size=sample, replace=False)]
+    secs64 = 0.0
+    errs = []
+    by_size = {}
+    for i in pick:
+        j = jobs[i]
+        g = S.make_grid(S.GridConfig((j["n"], j["n"]), (20.0, 20.0)))
+        psi0 = S.init_psi(g, 1, j["state"], seed=j["seed"])
+        t0 = time.perf_counter()
+        r = S.find_ground_state(grid=g, atom=S.Rb87, interactions=S.InteractionParams(10.0, j["c1"]),
+                                potential=S.HarmonicTrap(1.0, 1.0), dt=0.005, n_steps=n_steps, tol=tol,
+                                psi_init=psi0, precision="fp64")
+        dt = time.perf_counter() - t0
+        r["workspace"].close()
+        secs64 += dt
+        by_size.setdefault(j["n"], []).append(dt)
+        errs.append(abs(r32[i]["energy"] - r["energy"]) / abs(r["energy"]))
+    # one-at-a-time FP64 time for all 512 solves, from the per-size mean of the sample
+    mean = {n: float(np.mean(v)) for n, v in by_size.items()}
+    overall = float(np.mean([x for v in by_size.values() for x in v]))
+    est64 = sum(mean.get(j["n"], overall) for j in jobs)
+    conv = sum(1 for x in r32.values() if x["converged"])
+    return {"workload": "512 ITP solves, 2D spin-1, c1 in 64 values of [-1,1] x 8 starts, grids 64^2/128^2/256^2, "
+                        "dt=0.005, tol=1e-8, check every 1000 of 10000 steps",
+            "fp32_batched_solves_per_s": len(jobs) / secs32, "fp32_batched_seconds": secs32,
+            "fp64_one_at_a_time_solves_per_s": len(jobs) / est64,
+            "fp64_sample": f"{sample} solves timed one at a time ({secs64:.2f} s), extrapolated per grid size",
+            "speedup_vs_fp64_one_at_a_time": est64 / secs32,
+            "energy_rel_err_fp32_vs_fp64_max": max(errs), "converged": conv}
+
+
+# ----------------------------------------------------------------------------- serving
+def bench_serving(S, n_requests: int, fp64_probe_steps: int = 20) -> dict:
+    """Poisson request stream (seeded, mean 200 req/s) served with continuous batching in the
+    FP32-bulk form under a 150 GB HBM budget; the plain FP64 form one request at a time is
+    estimated per request from a timed probe of the same grid (per-step time x the steps the
+    served solve took, plus its measured setup)."""
+    from spinorbec import serve
+
+    reqs = serve.poisson_requests(n_requests, rate=200.0, seed=5)
+    srv = serve.Server(hbm_budget_bytes=150e9, max_slots=32)
+    out = srv.run(reqs, realtime=True)
+    est64 = 0.0
+    probes = {}
+    for r, res in zip(reqs, out["results"]):
+        key = (r.n_points, r.F, r.enable_ddi, r.kind)
+        if key not in probes:
+            probes[key] = fp64_probe(S, r, fp64_probe_steps)
+        setup, per_step = probes[key]
+        est64 += setup + per_step * res.steps
+    return {"workload": f"{n_requests} requests of the seeded Poisson stream (mean 200 req/s): 1-D 256..4096, "
+                        "2-D 64^2..512^2, 3-D 32^3..128^3, F in {1,2,6}, DDI for F=6, 500-5000 steps, "
+                        "half ground states (tol 1e-8) half real-time runs",
+            "hbm_budget_gb": 150, "max_slots": 32, "peak_concurrent": srv.peak_active,
+            "peak_admitted_gb": srv.peak_used / 1e9,
+            "fp32_served_solves_per_s": out["solves_per_s"], "wall_s": out["wall_s"],
+            "p50_latency_s": out["p50_latency_s"], "p99_latency_s": out["p99_latency_s"],
+            "fp64_one_at_a_time_solves_per_s": len(reqs) / est64,
+            "fp64_estimate": f"per grid/F/kind: setup + {fp64_probe_steps}-step timed probe x steps of the served solve",
+            "speedup_vs_fp64_one_at_a_time": est64 / out["wall_s"]}
+
+
+def fp64_probe(S, r, k: int) -> tuple:
+    """(setup seconds, seconds per step) of request r's grid in the plain FP64 form."""
+    from spinorbec import serve
+
+    g = S.make_grid(S.GridConfig(r.n_points, r.box_size))
+    t0 = time.perf_counter()
+    ws = S.make_workspace(grid=g, atom=S.AtomSpecies("req", r.F), interactions=S.InteractionParams(r.c0, r.c1),
+                          potential=S.HarmonicTrap(*([r.omega] * len(r.n_points))), zeeman=S.ZeemanParams(0.0, 0.1),
+                          sim_params=S.SimParams(r.dt, k, r.kind == "ground_state", 1 if r.kind == "ground_state"
+                                                 else None, k),
+                          psi_init=S.init_psi(g, r.F, "polar"), enable_ddi=r.enable_ddi, c_dd=r.c_dd,
+                          precision="fp64")
+    S.split_step(ws, 2)
+    S.total_energy(ws)
+    setup = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    S.split_step(ws, k)
+    S.total_energy(ws)
+    per_step = (time.perf_counter() - t0) / k
+    ws.close()
+    del serve
+    return setup, per_step
+
+
+# ----------------------------------------------------------------------------- 3D spin-6 dipolar
+def bench_3d_f6(S, n: int = 128, steps32: int = 20, steps64: int = 2) -> dict:
+    """3D spin-6 Eu151 (c_total 4689, c1/c0 1/36, tensor c_extra (0,0,50)), zero-padded DDI
+    c_dd=100, trap (1,1,1.2), polarised m=+6 with 0.01 rad seeded phase noise; adaptive
+    Yoshida from dt=1e-3.  A bounded sample of the 2000-step run: the first accepted steps
+    of each form, timed, and the FP32 energy against the FP64 one after fixed-dt steps."""
+    ip = S.interaction_params_from_constraint(c_total=4689.0, c1_ratio=1 / 36, F=6, c_extra=(0.0, 0.0, 50.0))
+    g = S.make_grid(S.GridConfig((n, n, n), (24.0, 24.0, 24.0)))
+    rng = np.random.Generator(np.random.PCG64(11))
+    psi = S.init_psi(g, 6, "ferromagnetic")
+    psi = psi * np.exp(1j * 0.01 * rng.standard_normal(psi.shape))
+    out = {"workload": f"3D spin-6 {n}^3, 13 components, tensor + zero-padded {2 * n}^3 DDI, adaptive Yoshida "
+                       "dt0=1e-3 (sample of the 2000-step run)"}
+
+    def make(prec):
+        return S.make_workspace(grid=g, atom=S.AtomSpecies("151Eu", 6), interactions=ip,
+                                potential=S.HarmonicTrap(1.0, 1.0, 1.2), sim_params=S.SimParams(1e-3, 10),
+                                psi_init=psi, enable_ddi=True, c_dd=100.0, ddi_padding=True, precision=prec)
+
+    units = n ** 3 * 13
+    for prec, k in (("fp32", steps32), ("fp64", steps64)):
+        ws = make(prec)
+        S.run_simulation_yoshida(ws, S.AdaptiveDtParams(dt_init=1e-3), t_end=1.0, save_interval=1.0,
+                                 keep_psi=False, max_accepted=1)
+        ws.close()
+        ws = make(prec)
+        t0 = time.perf_counter()
+        r = S.run_simulation_yoshida(ws, S.AdaptiveDtParams(dt_init=1e-3), t_end=1.0, save_interval=1.0,
+                                     keep_psi=False, max_accepted=k)
+        secs = time.perf_counter() - t0
+        acc = int(r["n_accepted"])
+        ws.close()
+        out[prec] = {"seconds": secs, "accepted_steps": acc, "rejected_steps": int(r["n_rejected"]),
+                     "steps_per_s": acc / secs, "value": units * acc / secs, "unit": UNIT,
+                     "est_2000_step_solves_per_s": acc / secs / 2000.0}
+    out["speedup_fp32_vs_fp64"] = out["fp32"]["steps_per_s"] / out["fp64"]["steps_per_s"]
+    # accuracy: same fixed-dt Yoshida steps in both forms
+    w32, w64 = make("fp32"), make("fp64")
+    for _ in range(steps64):
+        S.yoshida_core(w32, 1e-3)
+        S.yoshida_core(w64, 1e-3)
+    e32, e64 = S.total_energy(w32), S.total_energy(w64)
+    n32, n64 = S.total_norm(w32), S.total_norm(w64)
+    out["energy_rel_err_fp32_vs_fp64"] = abs(e32 - e64) / abs(e64)
+    out["norm_rel_err_fp32_vs_fp64"] = abs(n32 - n64) / abs(n64)
+    w32.close()
+    w64.close()
+    return out
+
+
 # ----------------------------------------------------------------------------- GPU arm
 def measured_peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
@@ -348,6 +525,16 @@ def main_gpu(args) -> None:
         v64 = dist.world * units_per_run(p_steps) * max(1, args.steps // 2) / (ms64 / 1e3)
         plain = {"value": v64, "unit": UNIT, "steps_per_run": p_steps}
 
+    batched = None
+    if not args.no_batched:
+        batched = bench_batched(S)
+    serving = None
+    if not args.no_serving:
+        serving = bench_serving(S, args.serve_requests)
+    dipolar = None
+    if not args.no_3d:
+        dipolar = bench_3d_f6(S)
+
     cpu = None
     if dist.rank == 0 and not args.no_cpu:
         cpu = cpu_calibrated(args.cpu_seconds, os.cpu_count() or 1)
@@ -362,6 +549,9 @@ def main_gpu(args) -> None:
                        "l2": "flushed (256 MB write) between timed runs; psi (1.5 MB) stays L2-resident within a run"},
             "e2e": e2e,
             "plain_fp64": plain,
+            "batched_ground_states": batched,
+            "serving": serving,
+            "dipolar_3d_f6": dipolar,
             "vs_plain_fp64": (value / plain["value"]) if plain else None,
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": traffic, "peak_source": peak_src,
@@ -375,6 +565,42 @@ def main_gpu(args) -> None:
     dist.close()
 
 
+def ncu_case(args) -> None:
+    """Short runs of each workload for ncu captures (a few steps; no timing)."""
+    import __graft_entry__
+
+    __graft_entry__.build()
+    import spinorbec as S
+
+    k = args.ncu_steps
+    case = args.ncu_case
+    if case in ("2d256_fp32", "2d256_fp64"):
+        g = S.make_grid(S.GridConfig(N_GRID, BOX))
+        ws = S.make_workspace(grid=g, atom=S.Na23, interactions=S.InteractionParams(C0, C1), zeeman=S.ZeemanParams(ZP, ZQ),
+                              potential=S.HarmonicTrap(*OMEGA), sim_params=S.SimParams(DT, k, False, None, k + 1),
+                              precision=case.split("_")[1])
+        S.run_simulation(ws, keep_psi=False)
+    elif case == "batch256_fp32":
+        g = S.make_grid(S.GridConfig((256, 256), (20.0, 20.0)))
+        nb = args.ncu_batch
+        psis = [S.init_psi(g, 1, "polar") for _ in range(nb)]
+        b = S.GroundStateBatch(grid=g, atom=S.Rb87, c0s=[10.0] * nb, c1s=list(np.linspace(-1, 1, nb)), psi_inits=psis,
+                               potential=S.HarmonicTrap(1.0, 1.0), dt=0.005, precision="fp32")
+        b.ground_state(k, 1e-30, k)
+    elif case in ("3d_f6_fp32", "3d_f6_fp64"):
+        ip = S.interaction_params_from_constraint(c_total=4689.0, c1_ratio=1 / 36, F=6, c_extra=(0.0, 0.0, 50.0))
+        n = args.ncu_grid
+        g = S.make_grid(S.GridConfig((n, n, n), (24.0, 24.0, 24.0)))
+        psi = S.init_psi(g, 6, "ferromagnetic")
+        ws = S.make_workspace(grid=g, atom=S.AtomSpecies("151Eu", 6), interactions=ip, potential=S.HarmonicTrap(1.0, 1.0, 1.2),
+                              sim_params=S.SimParams(1e-3, k, False, None, k + 1), psi_init=psi, enable_ddi=True,
+                              c_dd=100.0, ddi_padding=True, precision=case.split("_")[2])
+        S.split_step(ws, k)
+    else:
+        raise SystemExit(f"unknown --ncu-case {case}")
+    print(f"ncu case {case}: {k} steps done")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -386,7 +612,18 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-3d", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--ncu-case", default=None, help="short run for profiling: 2d256_fp32|2d256_fp64|batch256_fp32|3d_f6_fp32|3d_f6_fp64")
+    ap.add_argument("--ncu-steps", type=int, default=4)
+    ap.add_argument("--ncu-grid", type=int, default=32)
+    ap.add_argument("--ncu-batch", type=int, default=170, help="solves in the batch256_fp32 case (the 256^2 group)")
     args = ap.parse_args()
+    if args.ncu_case:
+        ncu_case(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
