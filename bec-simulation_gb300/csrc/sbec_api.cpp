@@ -888,4 +888,26 @@ sbec_status sbec_ws_stream(sbec_ws* ws, void** stream) {
   SBEC_API_END
 }
 
+static void copy_report(const std::string& r, char* buf, int64_t cap, int64_t* len) {
+  if (len) *len = (int64_t)r.size();
+  if (buf && cap > 0) {
+    const size_t n = std::min<size_t>(r.size(), (size_t)cap - 1);
+    std::memcpy(buf, r.data(), n);
+    buf[n] = 0;
+  }
+}
+
+sbec_status sbec_tuning_report(sbec_ws* ws, char* buf, int64_t cap, int64_t* len) {
+  SBEC_API_BEGIN
+  copy_report(E(ws).tuning_report(), buf, cap, len);
+  SBEC_API_END
+}
+
+sbec_status sbec_batch_tuning_report(sbec_batch* b, char* buf, int64_t cap, int64_t* len) {
+  SBEC_API_BEGIN
+  need(b, "batch");
+  copy_report(b->eng->tuning_report(), buf, cap, len);
+  SBEC_API_END
+}
+
 }  // extern "C"

@@ -143,6 +143,7 @@ class EngineBase {
   // row pass plus the last-axis pass; an ITP split_step defers its renormalisation
   // into the next row pass.
   virtual bool fused_path() const = 0;
+  virtual std::string tuning_report() const = 0;  // autotuner decisions of this engine
   virtual void lf_open(double dt) = 0;               // V(dt/2), forward x
   virtual void lf_steps(long long n, double dt) = 0;  // n x [K(dt) with merged V(dt)]
   virtual void lf_close(double dt) = 0;              // K(dt), V(dt/2)

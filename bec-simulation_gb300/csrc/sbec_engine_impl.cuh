@@ -7,13 +7,17 @@
 #include <complex>
 #include <cstdlib>
 #include <cstring>
+#include <algorithm>
 #include <map>
+#include <mutex>
 #include <tuple>
+#include <type_traits>
 #include <string>
 #include <vector>
 
 #include "sbec_engine.h"
 #include "sbec_kernels.cuh"
+#include "sbec_lines.h"
 
 namespace sbec {
 
@@ -23,23 +27,6 @@ namespace sbec {
 // Tiles are kept small (about 64 threads) so that the 2-D grids of a single solve
 // (e.g. 768 lines of 256) still spread over all 152 SMs; strided tiles are at
 // least one 32-byte sector wide so every global access moves whole sectors.
-template <typename R, int N>
-constexpr int x_lines_per_block() {
-  constexpr int tpl = N / PlanOf<R, N>::E;
-  constexpr int lpb = 64 / tpl;
-  return lpb < 1 ? 1 : lpb;
-}
-
-template <typename R, int N>
-constexpr int strided_width() {
-  constexpr int tpl = N / PlanOf<R, N>::E;
-  constexpr int seg = 16 / (int)sizeof(cplx<R>);  // at least 16 contiguous bytes per row segment
-  int w = 64 / tpl;
-  if (w < seg) w = seg;
-  while (w > 1 && (w * tpl > 1024 || (long)w * N * (int)sizeof(cplx<R>) > 96 * 1024)) w /= 2;
-  return w;
-}
-
 template <typename R, int MH>
 constexpr int ddi_x_rows_per_block() {
   constexpr int tpl = MH / PlanOf<R, MH>::E;
@@ -118,6 +105,8 @@ class Engine final : public EngineBase {
     // SBEC_GRAPHS=0 / SBEC_PDL=0 turn off graph replay / programmatic dependent launch.
     if (const char* g = std::getenv("SBEC_GRAPHS")) use_graphs_ = std::atoi(g) != 0;
     if (const char* p = std::getenv("SBEC_PDL")) use_pdl_ = std::atoi(p) != 0;
+    if (const char* t = std::getenv("SBEC_TUNE")) tune_on_ = std::atoi(t) != 0;
+    if (const char* f = std::getenv("SBEC_TUNE_FORCE")) tune_force_ = std::atoi(f);
     const int D = s_.D;
     N_ = s_.N;
     nc_ = N_ * D;
@@ -418,11 +407,12 @@ class Engine final : public EngineBase {
     if (!(s_.D == 1 || s_.D == 3 || s_.D == 5)) return false;
     const int nx = s_.n[0];
     if (nx < 16 || nx > 4096) return false;
-    return row_smem_bytes(nx) <= 200 * 1024;
+    return row_variant_ok(sizeof(R) == 4, nx, s_.D, 0);
   }
 
   void lf_open(double dtv) override {
     update_phase(dtv, false);
+    ensure_row_tuned(dtv, false, false);
     RowArgs<R> a = row_args(false);
     a.p1 = pot_full(dtv / 2, false);
     a.flags = RP_POT1 | (s_.ndim > 1 ? RP_FWD_X : 0);
@@ -431,6 +421,7 @@ class Engine final : public EngineBase {
 
   void lf_steps(long long n, double dtv) override {
     update_phase(dtv, false);
+    ensure_row_tuned(dtv, false, false);
     if (n <= 0) return;
     const GraphKey key{1, n, dtv, 0.0, zeeman_p, zeeman_q, 0};
     if (graph_replay(key)) return;
@@ -454,6 +445,7 @@ class Engine final : public EngineBase {
 
   void lf_close(double dtv) override {
     update_phase(dtv, false);
+    ensure_row_tuned(dtv, false, false);
     RowArgs<R> a = row_args(false);
     if (s_.ndim == 1) {
       a.p2 = pot_full(dtv / 2, false);
@@ -471,6 +463,7 @@ class Engine final : public EngineBase {
   // the end), using the |psi|^2 sums the closing pass of step k accumulated.
   void fused_split_steps(long long n, double dtv, double kin_dt, bool kin_itp, bool it, bool normalize) override {
     update_phase(kin_dt, kin_itp);
+    ensure_row_tuned(dtv, it, false);
     if (n <= 0) return;
     const GraphKey key{2, n, dtv, kin_dt, zeeman_p, zeeman_q, (kin_itp ? 1 : 0) | (it ? 2 : 0) | (normalize ? 4 : 0)};
     if (graph_replay(key)) return;
@@ -616,6 +609,7 @@ class Engine final : public EngineBase {
   void batch_itp_steps(long long n, double dtv) override {
     if (n <= 0 || n_active_ == 0) return;
     update_phase(dtv, true);
+    ensure_row_tuned(dtv, true, true);
     const GraphKey key{3, n, dtv, (double)n_active_, zeeman_p, zeeman_q, active_version_};
     if (graph_replay(key)) return;
     graph_begin(key);
@@ -948,34 +942,190 @@ class Engine final : public EngineBase {
   }
 
   // ---- FFT launchers
-  template <int NN>
-  void launch_fft_x(cplx<R>* data, int64_t n_lines, int mode) {
-    constexpr int LPB = x_lines_per_block<R, NN>();
-    constexpr int TPL = NN / PlanOf<R, NN>::E;
-    const size_t smem = sizeof(cplx<R>) * LPB * NN;
-    auto kern = k_fft_x<R, NN, LPB>;
-    static const bool once = (set_smem(kern, smem), true);
-    (void)once;
-    const int64_t blocks = (n_lines + LPB - 1) / LPB;
-    pb();
-    launch_pdl(kern, dim3((unsigned)blocks), dim3(LPB * TPL), smem, data, n_lines, mode, phase_ref(), twiddle(NN));
-    done(mode == 2 ? "fft_x_kinetic" : "fft_x", 2.0 * (double)sizeof(cplx<R>) * (double)n_lines * NN);
+  LineCtx<R> line_ctx() const { return LineCtx<R>{stream_, use_pdl_, phase_ref(), st_}; }
+
+  // Calls f(std::integral_constant<int, V>) for the compiled variant V of a line kind.
+  template <typename F>
+  void with_variant(int n, int v, F&& f) {
+    if constexpr (sizeof(R) == 8) {
+      (void)n;
+      (void)v;
+      f(std::integral_constant<int, 0>{});
+    } else {
+      switch (line_variant(true, n, v)) {
+        case 1: f(std::integral_constant<int, 1>{}); break;
+        case 2: f(std::integral_constant<int, 2>{}); break;
+        case 3: f(std::integral_constant<int, 3>{}); break;
+        default: f(std::integral_constant<int, 0>{}); break;
+      }
+    }
   }
 
-  template <int NN>
-  void launch_fft_strided(cplx<R>* data, int64_t S, int64_t inner, int64_t outer, int64_t outer_stride, int n_in,
-                          int n_out, int mode) {
-    constexpr int W = strided_width<R, NN>();
-    constexpr int TPL = NN / PlanOf<R, NN>::E;
-    const size_t smem = sizeof(cplx<R>) * W * NN;
-    auto kern = k_fft_strided<R, NN, W>;
-    static const bool once = (set_smem(kern, smem), true);
-    (void)once;
-    dim3 grid((unsigned)((inner + W - 1) / W), (unsigned)outer);
+  // ---- autotuner.  The first time a line-kernel call shape is met (outside a graph
+  // capture) every compiled variant is timed on a copy of the data it would touch:
+  // one warm-up launch, then the median of three CUDA-event timings, each on a
+  // fresh copy.  The fastest is kept in a table shared by all workspaces of the
+  // process, so every solve of one shape runs the same kernels (the variants agree
+  // to FP32 rounding, not bit for bit).
+  static std::mutex& tune_mutex() {
+    static std::mutex m;
+    return m;
+  }
+  static std::map<std::string, int>& tune_table() {
+    static std::map<std::string, int> t;
+    return t;
+  }
+
+  bool capturing() const {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    cuda_check(cudaStreamIsCapturing(stream_, &st), "cudaStreamIsCapturing");
+    return st != cudaStreamCaptureStatusNone;
+  }
+
+  std::vector<int> line_candidates(int n, bool row) const {
+    std::vector<int> c;
+    for (int v = 0; v < kLineVariants; ++v) {
+      if (line_variant(sizeof(R) == 4, n, v) != v) continue;
+      if (row && !row_variant_ok(sizeof(R) == 4, n, s_.D, v)) continue;
+      c.push_back(v);
+    }
+    return c;
+  }
+
+  // Variant for a call shape: forced, cached, or measured now.  launch(v, buf)
+  // runs variant v on buf, a copy of the `extent` elements at src.
+  template <typename Launch>
+  int line_tune(const std::string& shape, int n, bool row, const cplx<R>* src, size_t extent, Launch&& launch) {
+    const std::vector<int> cands = line_candidates(n, row);
+    if (cands.empty()) return 0;
+    if (tune_force_ >= 0) {
+      for (int v : cands)
+        if (v == tune_force_) return v;
+      return 0;
+    }
+    if (!tune_on_ || cands.size() == 1) return cands[0];
+    const std::string key = std::string(sizeof(R) == 4 ? "fp32 " : "fp64 ") + shape + " D=" + std::to_string(s_.D) +
+                            " grid=" + std::to_string(s_.n[0]) + "x" + std::to_string(s_.n[1]) + "x" +
+                            std::to_string(s_.n[2]) + " solves=" + std::to_string(std::max(nsolve_, 1));
+    auto mine = tuned_.find(key);
+    if (mine != tuned_.end()) return mine->second;
+    std::lock_guard<std::mutex> lock(tune_mutex());
+    auto it = tune_table().find(key);
+    if (it != tune_table().end()) return tuned_[key] = it->second;
+    if (capturing()) return 0;  // never reached: shapes are first met in an eager run
+    if (extent > tune_buf_n_) {
+      tune_buf_ = alloc<cplx<R>>(extent);
+      tune_buf_n_ = extent;
+    }
+    cudaEvent_t e0, e1;
+    cuda_check(cudaEventCreate(&e0), "cudaEventCreate");
+    cuda_check(cudaEventCreate(&e1), "cudaEventCreate");
+    const size_t bytes = sizeof(cplx<R>) * extent;
+    std::string line = key + " ->";
+    float best = 0.0f;
+    int bv = cands[0];
+    for (int v : cands) {
+      cuda_check(cudaMemcpyAsync(tune_buf_, src, bytes, cudaMemcpyDeviceToDevice, stream_), "cudaMemcpyAsync");
+      launch(v, tune_buf_);
+      float t[3];
+      for (float& ti : t) {
+        cuda_check(cudaMemcpyAsync(tune_buf_, src, bytes, cudaMemcpyDeviceToDevice, stream_), "cudaMemcpyAsync");
+        cuda_check(cudaEventRecord(e0, stream_), "cudaEventRecord");
+        launch(v, tune_buf_);
+        cuda_check(cudaEventRecord(e1, stream_), "cudaEventRecord");
+        cuda_check(cudaEventSynchronize(e1), "cudaEventSynchronize");
+        cuda_check(cudaEventElapsedTime(&ti, e0, e1), "cudaEventElapsedTime");
+      }
+      std::sort(t, t + 3);
+      line += " v" + std::to_string(v) + "=" + std::to_string(t[1] * 1000.0f).substr(0, 7) + "us";
+      if (v == cands[0] || t[1] < best) {
+        best = t[1];
+        bv = v;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cuda_check(cudaGetLastError(), "autotune");
+    tune_log_.push_back(line + " chosen v" + std::to_string(bv));
+    tune_table()[key] = bv;
+    return tuned_[key] = bv;
+  }
+
+  // Row-pass variant, fixed once per engine before any row arguments are built
+  // (the tile height sets how many norm partials a pass writes).
+  void ensure_row_tuned(double dtv, bool itp, bool batch) {
+    if (row_tuned_ || !fused_path()) return;
+    row_tuned_ = true;
+    const int nx = s_.n[0];
+    RowArgs<R> a = batch ? batch_row_args(false) : row_args(false);
+    PotArgs<R> pot = pot_full(dtv / 2, itp);
+    if (batch) pot.rot_a = pot.rot_b = s_.D > 1;
+    a.p1 = pot;
+    a.p2 = pot;
+    a.flags = s_.ndim > 1 ? (RP_INV_X | RP_POT1 | RP_FWD_X) : (RP_POT1 | RP_KIN_X);
+    const LineCtx<R> c = line_ctx();
+    const Tw<R> tw = twiddle(nx);
+    const int D = s_.D;
+    const size_t extent = batch ? (size_t)nc_ * nsolve_ : (size_t)nc_;
+    const cplx<R>* src = batch ? bpsi_ : psi_[kPsi];
+    v_row_ = line_tune("row flags=" + std::to_string(a.flags) + (batch ? " batched" : ""), nx, true, src, extent,
+                       [&](int v, cplx<R>* buf) {
+                         RowArgs<R> b = a;
+                         b.psi = buf;
+                         const int rpb = row_rpb_host(sizeof(R) == 4, nx, D, v);
+                         const int bps = (int)((a.n_rows + rpb - 1) / rpb);
+                         b.blocks_per_solve = bps;
+                         const int nb = b.active ? bps * b.n_slots : bps;
+                         with_variant(nx, v, [&](auto vv) { LineKernels<R, decltype(vv)::value>::row(c, tw, nx, D, b, nb); });
+                       });
+  }
+
+  std::string tuning_report() const override {
+    std::string r;
+    for (const auto& l : tune_log_) r += l + "\n";
+    r += "row variant " + std::to_string(v_row_) + (tune_force_ >= 0 ? " (forced)" : (tune_on_ ? "" : " (tuning off)"));
+    return r;
+  }
+
+  void fft_x_n(int n, cplx<R>* data, int64_t n_lines, int mode) {
+    const LineCtx<R> c = line_ctx();
+    const Tw<R> tw = twiddle(n);
+    const int vx = line_tune(
+        "x n=" + std::to_string(n) + " lines=" + std::to_string(n_lines) + " mode=" + std::to_string(mode), n,
+        false, data, (size_t)n_lines * n, [&](int v, cplx<R>* buf) {
+          with_variant(n, v, [&](auto vv) { LineKernels<R, decltype(vv)::value>::fft_x(c, tw, n, buf, n_lines, mode); });
+        });
     pb();
-    launch_pdl(kern, grid, dim3(W * TPL), smem, data, S, inner, outer_stride, n_in, n_out, mode, phase_ref(),
-               twiddle(NN), omap_, oper_);
-    done(mode == 2 ? "fft_last_kinetic" : "fft_strided", (double)sizeof(cplx<R>) * (double)(n_in + n_out) * (double)inner * (double)outer);
+    with_variant(n, vx, [&](auto v) { LineKernels<R, decltype(v)::value>::fft_x(c, tw, n, data, n_lines, mode); });
+    done(mode == 2 ? "fft_x_kinetic" : "fft_x", 2.0 * (double)sizeof(cplx<R>) * (double)n_lines * n);
+  }
+
+  void fft_strided_n(int n, cplx<R>* data, int64_t S, int64_t inner, int64_t outer, int64_t outer_stride, int n_in,
+                     int n_out, int mode) {
+    const LineCtx<R> c = line_ctx();
+    const Tw<R> tw = twiddle(n);
+    const int* om = omap_;
+    const int op = oper_;
+    // elements the launch touches from `data`: all outer lines, or every solve slot through omap
+    const size_t extent = (size_t)(om ? (int64_t)std::max(nsolve_, 1) * op : outer) * (size_t)outer_stride;
+    const int vs = line_tune("strided n=" + std::to_string(n) + " S=" + std::to_string(S) + " inner=" +
+                                 std::to_string(inner) + " outer=" + std::to_string(outer) + " in/out=" +
+                                 std::to_string(n_in) + "/" + std::to_string(n_out) + " mode=" + std::to_string(mode) +
+                                 (om ? " batched" : ""),
+                             n, false, data, extent, [&](int v, cplx<R>* buf) {
+                               with_variant(n, v, [&](auto vv) {
+                                 LineKernels<R, decltype(vv)::value>::fft_strided(c, tw, n, buf, S, inner, outer,
+                                                                                  outer_stride, n_in, n_out, mode, om,
+                                                                                  op);
+                               });
+                             });
+    pb();
+    with_variant(n, vs, [&](auto v) {
+      LineKernels<R, decltype(v)::value>::fft_strided(c, tw, n, data, S, inner, outer, outer_stride, n_in, n_out,
+                                                      mode, om, op);
+    });
+    done(mode == 2 ? "fft_last_kinetic" : "fft_strided",
+         (double)sizeof(cplx<R>) * (double)(n_in + n_out) * (double)inner * (double)outer);
   }
 
   // Full spatial FFT of a D-component buffer: forward only (kinetic=false), or the
@@ -985,30 +1135,28 @@ class Engine final : public EngineBase {
     const int nx = s_.n[0], ny = s_.n[1], nz = s_.n[2];
     const int64_t D = s_.D;
     if (nd == 1) {
-      SBEC_SWITCH_POW2(nx, launch_fft_x, buf, D, kinetic ? 2 : 0);
+      fft_x_n(nx, buf, D, kinetic ? 2 : 0);
       return;
     }
-    SBEC_SWITCH_POW2(nx, launch_fft_x, buf, (int64_t)ny * nz * D, 0);
+    fft_x_n(nx, buf, (int64_t)ny * nz * D, 0);
     if (nd == 2) {
-      SBEC_SWITCH_POW2_STRIDED(ny, launch_fft_strided, buf, (int64_t)nx, (int64_t)nx, D, N_, ny, ny, kinetic ? 2 : 0);
+      fft_strided_n(ny, buf, (int64_t)nx, (int64_t)nx, D, N_, ny, ny, kinetic ? 2 : 0);
     } else {
-      SBEC_SWITCH_POW2_STRIDED(ny, launch_fft_strided, buf, (int64_t)nx, (int64_t)nx, (int64_t)nz * D,
+      fft_strided_n(ny, buf, (int64_t)nx, (int64_t)nx, (int64_t)nz * D,
                                (int64_t)nx * ny, ny, ny, 0);
-      SBEC_SWITCH_POW2_STRIDED(nz, launch_fft_strided, buf, (int64_t)nx * ny, (int64_t)nx * ny, D, N_, nz, nz,
+      fft_strided_n(nz, buf, (int64_t)nx * ny, (int64_t)nx * ny, D, N_, nz, nz,
                                kinetic ? 2 : 0);
       if (kinetic)
-        SBEC_SWITCH_POW2_STRIDED(ny, launch_fft_strided, buf, (int64_t)nx, (int64_t)nx, (int64_t)nz * D,
+        fft_strided_n(ny, buf, (int64_t)nx, (int64_t)nx, (int64_t)nz * D,
                                  (int64_t)nx * ny, ny, ny, 1);
     }
-    if (kinetic) SBEC_SWITCH_POW2(nx, launch_fft_x, buf, (int64_t)ny * nz * D, 1);
+    if (kinetic) fft_x_n(nx, buf, (int64_t)ny * nz * D, 1);
   }
 
   // ---- batch helpers
   int row_blocks_per_solve() const {
     const int nx = s_.n[0];
-    const int tpl = nx / plan_radix_host(sizeof(R) == 4, nx);
-    int rpb = 64 / (s_.D * std::max(tpl, 1));
-    if (rpb < 1) rpb = 1;
+    const int rpb = row_rpb_host(sizeof(R) == 4, nx, s_.D, v_row_);
     const int64_t rows = N_ / nx;
     return (int)((rows + rpb - 1) / rpb);
   }
@@ -1037,16 +1185,16 @@ class Engine final : public EngineBase {
     const int64_t D = s_.D;
     if (s_.ndim == 2) {
       oper_ = (int)D;
-      SBEC_SWITCH_POW2_STRIDED(ny, launch_fft_strided, buf, (int64_t)nx, (int64_t)nx, D * n_slots, N_, ny, ny, 2);
+      fft_strided_n(ny, buf, (int64_t)nx, (int64_t)nx, D * n_slots, N_, ny, ny, 2);
     } else {
       oper_ = (int)(nz * D);
-      SBEC_SWITCH_POW2_STRIDED(ny, launch_fft_strided, buf, (int64_t)nx, (int64_t)nx, (int64_t)nz * D * n_slots,
+      fft_strided_n(ny, buf, (int64_t)nx, (int64_t)nx, (int64_t)nz * D * n_slots,
                                (int64_t)nx * ny, ny, ny, 0);
       oper_ = (int)D;
-      SBEC_SWITCH_POW2_STRIDED(nz, launch_fft_strided, buf, (int64_t)nx * ny, (int64_t)nx * ny, D * n_slots, N_, nz,
+      fft_strided_n(nz, buf, (int64_t)nx * ny, (int64_t)nx * ny, D * n_slots, N_, nz,
                                nz, 2);
       oper_ = (int)(nz * D);
-      SBEC_SWITCH_POW2_STRIDED(ny, launch_fft_strided, buf, (int64_t)nx, (int64_t)nx, (int64_t)nz * D * n_slots,
+      fft_strided_n(ny, buf, (int64_t)nx, (int64_t)nx, (int64_t)nz * D * n_slots,
                                (int64_t)nx * ny, ny, ny, 1);
       oper_ = (int)D;
     }
@@ -1056,12 +1204,12 @@ class Engine final : public EngineBase {
   void fft_forward_batch(cplx<R>* buf, int n_slots) {
     const int nx = s_.n[0], ny = s_.n[1], nz = s_.n[2];
     const int64_t D = s_.D;
-    SBEC_SWITCH_POW2(nx, launch_fft_x, buf, (int64_t)ny * nz * D * n_slots, 0);
+    fft_x_n(nx, buf, (int64_t)ny * nz * D * n_slots, 0);
     if (s_.ndim >= 2)
-      SBEC_SWITCH_POW2_STRIDED(ny, launch_fft_strided, buf, (int64_t)nx, (int64_t)nx, (int64_t)nz * D * n_slots,
+      fft_strided_n(ny, buf, (int64_t)nx, (int64_t)nx, (int64_t)nz * D * n_slots,
                                (int64_t)nx * ny, ny, ny, 0);
     if (s_.ndim >= 3)
-      SBEC_SWITCH_POW2_STRIDED(nz, launch_fft_strided, buf, (int64_t)nx * ny, (int64_t)nx * ny, D * n_slots, N_, nz,
+      fft_strided_n(nz, buf, (int64_t)nx * ny, (int64_t)nx * ny, D * n_slots, N_, nz,
                                nz, 0);
   }
 
@@ -1075,21 +1223,7 @@ class Engine final : public EngineBase {
     done("reduce_finish", 8.0 * (D + 4) * bpe * na);
   }
 
-  // ---- fused row pass launchers
-  template <int NN, int D>
-  static constexpr int row_rpb() {
-    constexpr int tpl = NN / PlanOf<R, NN>::E;
-    constexpr int r = 64 / (D * tpl);
-    return r < 1 ? 1 : r;
-  }
-
-  size_t row_smem_bytes(int nx) const {
-    const int tpl = nx / plan_radix_host(sizeof(R) == 4, nx);
-    int rpb = 64 / (s_.D * std::max(tpl, 1));
-    if (rpb < 1) rpb = 1;
-    return sizeof(cplx<R>) * (size_t)s_.D * rpb * nx;
-  }
-
+  // ---- fused row pass
   PotArgs<R> pot_full(double tau_half, bool it) const {
     // the half-potential stage without DDI/tensor: diag(tau/2) SM(tau/2) SM(tau/2) diag(tau/2)
     PotArgs<R> a = pot_args(tau_half / 2, it);
@@ -1114,49 +1248,22 @@ class Engine final : public EngineBase {
     return a;
   }
 
-  template <int NN, int D>
-  int launch_row_nd(const RowArgs<R>& a) {
-    constexpr int RPB = row_rpb<NN, D>();
-    constexpr int TPL = NN / PlanOf<R, NN>::E;
-    const size_t smem = sizeof(cplx<R>) * D * RPB * NN;
-    auto kern = k_row_pass<R, NN, D, RPB>;
-    static const bool once = (set_smem(kern, smem), true);
-    (void)once;
-    const int bps = (int)((a.n_rows + RPB - 1) / RPB);
-    const int nb = a.active ? bps * a.n_slots : bps;
-    if (a.active && a.blocks_per_solve != bps) fail(SBEC_ERR_INVALID, "row pass blocks per solve mismatch");
-    pb();
-    launch_pdl(kern, dim3(nb), dim3(D * RPB * TPL), smem, a, st_, phase_ref(), twiddle(NN));
-    done("row_pass", 2.0 * (double)sizeof(cplx<R>) * nc_ + (double)sizeof(R) * N_ * ((a.flags & RP_POT1) ? 1 : 0));
-    return nb;
-  }
-
-  template <int NN>
-  int launch_row_n(const RowArgs<R>& a) {
-    switch (s_.D) {
-      case 1: return launch_row_nd<NN, 1>(a);
-      case 3: return launch_row_nd<NN, 3>(a);
-      case 5: return launch_row_nd<NN, 5>(a);
-      default: fail(SBEC_ERR_UNSUPPORTED, "fused path needs D in {1,3,5}");
-    }
-  }
-
   int launch_row(const RowArgs<R>& a) {
     if (a.flags & RP_NORM) {
       if ((size_t)a.n_rows * std::max(a.n_slots, 1) > partials_n_) fail(SBEC_ERR_UNSUPPORTED, "too many rows for the norm partials");
     }
-    switch (s_.n[0]) {
-      case 16: return launch_row_n<16>(a);
-      case 32: return launch_row_n<32>(a);
-      case 64: return launch_row_n<64>(a);
-      case 128: return launch_row_n<128>(a);
-      case 256: return launch_row_n<256>(a);
-      case 512: return launch_row_n<512>(a);
-      case 1024: return launch_row_n<1024>(a);
-      case 2048: return launch_row_n<2048>(a);
-      case 4096: return launch_row_n<4096>(a);
-      default: fail(SBEC_ERR_UNSUPPORTED, "fused path line length");
-    }
+    const int nx = s_.n[0];
+    const int rpb = row_rpb_host(sizeof(R) == 4, nx, s_.D, v_row_);
+    const int bps = (int)((a.n_rows + rpb - 1) / rpb);
+    const int nb = a.active ? bps * a.n_slots : bps;
+    if (a.active && a.blocks_per_solve != bps) fail(SBEC_ERR_INVALID, "row pass blocks per solve mismatch");
+    const LineCtx<R> c = line_ctx();
+    const Tw<R> tw = twiddle(nx);
+    const int D = s_.D;
+    pb();
+    with_variant(nx, v_row_, [&](auto v) { LineKernels<R, decltype(v)::value>::row(c, tw, nx, D, a, nb); });
+    done("row_pass", 2.0 * (double)sizeof(cplx<R>) * nc_ + (double)sizeof(R) * N_ * ((a.flags & RP_POT1) ? 1 : 0));
+    return nb;
   }
 
   void finish_row_norm(int nb) {
@@ -1172,12 +1279,12 @@ class Engine final : public EngineBase {
     const int nx = s_.n[0], ny = s_.n[1], nz = s_.n[2];
     const int64_t D = s_.D;
     if (s_.ndim == 2) {
-      SBEC_SWITCH_POW2_STRIDED(ny, launch_fft_strided, psi_[kPsi], (int64_t)nx, (int64_t)nx, D, N_, ny, ny, 2);
+      fft_strided_n(ny, psi_[kPsi], (int64_t)nx, (int64_t)nx, D, N_, ny, ny, 2);
     } else {
-      SBEC_SWITCH_POW2_STRIDED(ny, launch_fft_strided, psi_[kPsi], (int64_t)nx, (int64_t)nx, (int64_t)nz * D,
+      fft_strided_n(ny, psi_[kPsi], (int64_t)nx, (int64_t)nx, (int64_t)nz * D,
                                (int64_t)nx * ny, ny, ny, 0);
-      SBEC_SWITCH_POW2_STRIDED(nz, launch_fft_strided, psi_[kPsi], (int64_t)nx * ny, (int64_t)nx * ny, D, N_, nz, nz, 2);
-      SBEC_SWITCH_POW2_STRIDED(ny, launch_fft_strided, psi_[kPsi], (int64_t)nx, (int64_t)nx, (int64_t)nz * D,
+      fft_strided_n(nz, psi_[kPsi], (int64_t)nx * ny, (int64_t)nx * ny, D, N_, nz, nz, 2);
+      fft_strided_n(ny, psi_[kPsi], (int64_t)nx, (int64_t)nx, (int64_t)nz * D,
                                (int64_t)nx * ny, ny, ny, 1);
     }
   }
@@ -1259,10 +1366,10 @@ class Engine final : public EngineBase {
       SBEC_SWITCH_POW2_STRIDED(g.My, launch_ddi_last, spec, g, (int64_t)g.Hx, (int64_t)g.Hx, g.ny, g.ny);
     } else {
       const int64_t plane = (int64_t)g.Hx * g.My;
-      SBEC_SWITCH_POW2_STRIDED(g.My, launch_fft_strided, spec, (int64_t)g.Hx, (int64_t)g.Hx, (int64_t)3 * g.nz,
+      fft_strided_n(g.My, spec, (int64_t)g.Hx, (int64_t)g.Hx, (int64_t)3 * g.nz,
                                plane, g.ny, g.My, 0);
       SBEC_SWITCH_POW2_STRIDED(g.Mz, launch_ddi_last, spec, g, plane, plane, g.nz, g.nz);
-      SBEC_SWITCH_POW2_STRIDED(g.My, launch_fft_strided, spec, (int64_t)g.Hx, (int64_t)g.Hx, (int64_t)3 * g.nz,
+      fft_strided_n(g.My, spec, (int64_t)g.Hx, (int64_t)g.Hx, (int64_t)3 * g.nz,
                                plane, g.My, g.ny, 1);
     }
     SBEC_SWITCH_POW2(MH, launch_ddi_c2r, spec, g, phi3);
@@ -1429,6 +1536,15 @@ class Engine final : public EngineBase {
   int oper_ = 1;
   bool use_graphs_ = true;
   bool use_pdl_ = false;  // SBEC_PDL=1 enables; measured slower for these short kernels
+  // line-kernel variants in use (see sbec_lines.h); chosen by the autotuner
+  int v_row_ = 0, v_str_ = 0, v_x_ = 0;
+  bool tune_on_ = true;       // SBEC_TUNE=0: variant 0 everywhere
+  int tune_force_ = -1;       // SBEC_TUNE_FORCE=v: variant v wherever it is compiled
+  bool row_tuned_ = false;
+  std::map<std::string, int> tuned_;  // this engine's strided / x decisions by call shape
+  std::vector<std::string> tune_log_;
+  cplx<R>* tune_buf_ = nullptr;
+  size_t tune_buf_n_ = 0;
   bool capturing_ = false;
   long long cap_launch0_ = 0;
   double phase_dt_ = NAN;

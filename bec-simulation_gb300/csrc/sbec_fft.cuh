@@ -100,20 +100,12 @@ __device__ __forceinline__ void dft(cplx<R>* v) {
   }
 }
 
-// One Stockham stage.  tw holds W_N^e = exp(-2*pi*i*e/N), e = 0..N-1 (forward sign).
+// Twiddle, butterfly and store of one Stockham stage for the values v a thread loaded.
 template <typename R, int N, int E, int RAD, int SIGN>
-__device__ __forceinline__ void fft_stage(cplx<R>* s, int SI, int SL, int l, int t, int Ns, const Tw<R>& tw) {
+__device__ __forceinline__ void fft_stage_store(cplx<R>* s, int SI, int SL, int l, int t, int Ns, const Tw<R>& tw,
+                                                cplx<R> (&v)[E]) {
   constexpr int TPL = N / E;
   constexpr int NBT = E / RAD;
-  constexpr int STRIDE = N / RAD;
-  cplx<R> v[E];
-#pragma unroll
-  for (int b = 0; b < NBT; ++b) {
-    const int j = t + b * TPL;
-#pragma unroll
-    for (int r = 0; r < RAD; ++r) v[b * RAD + r] = s[(j + r * STRIDE) * SI + l * SL];
-  }
-  __syncthreads();
 #pragma unroll
   for (int b = 0; b < NBT; ++b) {
     const int j = t + b * TPL;
@@ -128,13 +120,38 @@ __device__ __forceinline__ void fft_stage(cplx<R>* s, int SI, int SL, int l, int
 #pragma unroll
     for (int r = 0; r < RAD; ++r) s[(base + r * Ns) * SI + l * SL] = v[b * RAD + r];
   }
+}
+
+// One Stockham stage.  tw holds W_N^e = exp(-2*pi*i*e/N), e = 0..N-1 (forward sign).
+// Threads with act == false (the spare threads of a block sized for a per-point
+// stage) skip the work but reach the same two barriers as every other thread:
+// __syncthreads is an aligned barrier, and a warp whose threads split between two
+// barrier call sites never completes.
+template <typename R, int N, int E, int RAD, int SIGN>
+__device__ __forceinline__ void fft_stage(cplx<R>* s, int SI, int SL, int l, int t, int Ns, const Tw<R>& tw,
+                                          bool act) {
+  constexpr int TPL = N / E;
+  constexpr int NBT = E / RAD;
+  constexpr int STRIDE = N / RAD;
+  cplx<R> v[E];
+  if (act) {
+#pragma unroll
+    for (int b = 0; b < NBT; ++b) {
+      const int j = t + b * TPL;
+#pragma unroll
+      for (int r = 0; r < RAD; ++r) v[b * RAD + r] = s[(j + r * STRIDE) * SI + l * SL];
+    }
+  }
+  __syncthreads();
+  if (act) fft_stage_store<R, N, E, RAD, SIGN>(s, SI, SL, l, t, Ns, tw, v);
   __syncthreads();
 }
 
 template <typename R, int N, int E, int SIGN, int RAD, int... REST>
-__device__ __forceinline__ void run_stages(cplx<R>* s, int SI, int SL, int l, int t, int Ns, const Tw<R>& tw) {
-  fft_stage<R, N, E, RAD, SIGN>(s, SI, SL, l, t, Ns, tw);
-  if constexpr (sizeof...(REST) > 0) run_stages<R, N, E, SIGN, REST...>(s, SI, SL, l, t, Ns * RAD, tw);
+__device__ __forceinline__ void run_stages(cplx<R>* s, int SI, int SL, int l, int t, int Ns, const Tw<R>& tw,
+                                           bool act) {
+  fft_stage<R, N, E, RAD, SIGN>(s, SI, SL, l, t, Ns, tw, act);
+  if constexpr (sizeof...(REST) > 0) run_stages<R, N, E, SIGN, REST...>(s, SI, SL, l, t, Ns * RAD, tw, act);
 }
 
 // Radix plans per line length: E = largest radix; stages run in the listed order.
@@ -148,8 +165,8 @@ template <int N> struct FftPlan32;
     static constexpr int E = EE;                                                                 \
     template <typename R, int SIGN>                                                              \
     static __device__ __forceinline__ void run(cplx<R>* s, int SI, int SL, int l, int t,        \
-                                               const Tw<R>& tw) {                                \
-      run_stages<R, NN, EE, SIGN, __VA_ARGS__>(s, SI, SL, l, t, 1, tw);                          \
+                                               const Tw<R>& tw, bool act) {                      \
+      run_stages<R, NN, EE, SIGN, __VA_ARGS__>(s, SI, SL, l, t, 1, tw, act);                     \
     }                                                                                            \
   };
 SBEC_PLAN(FftPlan, 2, 2, 2)
@@ -178,20 +195,33 @@ SBEC_PLAN(FftPlan32, 2048, 8, 8, 8, 8, 4)
 SBEC_PLAN(FftPlan32, 4096, 8, 8, 8, 8, 8)
 #undef SBEC_PLAN
 
-template <typename R, int N>
-struct PlanSel {
+// Plan family P of a line kernel: 0 = the precision's default (radix-16 for FP64,
+// radix-4/8 for FP32), 1 = the other one.  The autotuner picks per shape.
+template <typename R, int N, int P>
+struct PlanSel;
+template <int N>
+struct PlanSel<double, N, 0> {
   using type = FftPlan<N>;
 };
 template <int N>
-struct PlanSel<float, N> {
+struct PlanSel<double, N, 1> {
   using type = FftPlan32<N>;
 };
-template <typename R, int N>
-using PlanOf = typename PlanSel<R, N>::type;
+template <int N>
+struct PlanSel<float, N, 0> {
+  using type = FftPlan32<N>;
+};
+template <int N>
+struct PlanSel<float, N, 1> {
+  using type = FftPlan<N>;
+};
+template <typename R, int N, int P = 0>
+using PlanOf = typename PlanSel<R, N, P>::type;
 
-// host-side mirror of PlanOf<R, N>::E
-inline int plan_radix_host(bool fp32, int n) {
-  if (fp32) return n <= 4 ? n : (n <= 256 ? 4 : 8);
+// host-side mirror of PlanOf<R, N, P>::E
+inline int plan_radix_host(bool fp32, int n, int P = 0) {
+  const bool deep = fp32 ? (P == 1) : (P == 0);
+  if (!deep) return n <= 4 ? n : (n <= 256 ? 4 : 8);
   switch (n) {
     case 32: case 64: case 512: return 8;
     case 2: case 4: case 8: return n;
@@ -201,9 +231,10 @@ inline int plan_radix_host(bool fp32, int n) {
 
 // Transform every line of a shared-memory tile (all threads of the block participate).
 // Caller must __syncthreads() after filling the tile; the function ends synchronised.
-template <typename R, int N, int SIGN>
-__device__ __forceinline__ void fft_tile(cplx<R>* s, int SI, int SL, int l, int t, const Tw<R>& tw) {
-  PlanOf<R, N>::template run<R, SIGN>(s, SI, SL, l, t, tw);
+template <typename R, int N, int SIGN, int P = 0>
+__device__ __forceinline__ void fft_tile(cplx<R>* s, int SI, int SL, int l, int t, const Tw<R>& tw,
+                                         bool act = true) {
+  PlanOf<R, N, P>::template run<R, SIGN>(s, SI, SL, l, t, tw, act);
 }
 
 }  // namespace sbec

@@ -74,11 +74,11 @@ struct PhaseRef {
 // FFT along x (contiguous lines).  mode 0: forward, 1: inverse,
 // 2: forward, x phase (1-D kinetic step), inverse.
 // ---------------------------------------------------------------------------
-template <typename R, int N, int LPB>
-__global__ void __launch_bounds__(LPB * (N / PlanOf<R, N>::E))
+template <typename R, int N, int LPB, int P = 0>
+__global__ void __launch_bounds__(LPB * (N / PlanOf<R, N, P>::E))
 k_fft_x(cplx<R>* __restrict__ data, int64_t n_lines, int mode, PhaseRef<R> ph, Tw<R> tw) {
   pdl_begin();
-  constexpr int TPL = N / PlanOf<R, N>::E;
+  constexpr int TPL = N / PlanOf<R, N, P>::E;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);
   const int tid = threadIdx.x;
@@ -89,13 +89,13 @@ k_fft_x(cplx<R>* __restrict__ data, int64_t n_lines, int mode, PhaseRef<R> ph, T
   __syncthreads();
   const int t = tid % TPL, l = tid / TPL;
   if (mode == 1) {
-    fft_tile<R, N, +1>(s, 1, N, l, t, tw);
+    fft_tile<R, N, +1, P>(s, 1, N, l, t, tw);
   } else {
-    fft_tile<R, N, -1>(s, 1, N, l, t, tw);
+    fft_tile<R, N, -1, P>(s, 1, N, l, t, tw);
     if (mode == 2) {
       for (int f = tid; f < LPB * N; f += blockDim.x) s[f] = tw_mul<R>(s[f], ph.tab[0], f % N, false);
       __syncthreads();
-      fft_tile<R, N, +1>(s, 1, N, l, t, tw);
+      fft_tile<R, N, +1, P>(s, 1, N, l, t, tw);
     }
   }
   for (int f = tid; f < nl * N; f += blockDim.x) g[f] = s[f];
@@ -108,12 +108,12 @@ k_fft_x(cplx<R>* __restrict__ data, int64_t n_lines, int mode, PhaseRef<R> ph, T
 // mode 0 forward, 1 inverse, 2 forward, x phase, inverse (last axis of the
 // kinetic step; the line's lower-axis coordinates come from i0 + w).
 // ---------------------------------------------------------------------------
-template <typename R, int N, int W>
-__global__ void __launch_bounds__(W * (N / PlanOf<R, N>::E))
+template <typename R, int N, int W, int P = 0>
+__global__ void __launch_bounds__(W * (N / PlanOf<R, N, P>::E))
 k_fft_strided(cplx<R>* __restrict__ data, int64_t S, int64_t inner, int64_t outer_stride, int n_in,
               int n_out, int mode, PhaseRef<R> ph, Tw<R> tw, const int* __restrict__ omap, int oper) {
   pdl_begin();
-  constexpr int TPL = N / PlanOf<R, N>::E;
+  constexpr int TPL = N / PlanOf<R, N, P>::E;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);
   __shared__ cplx<R> inner_ph[W];
@@ -143,9 +143,9 @@ k_fft_strided(cplx<R>* __restrict__ data, int64_t S, int64_t inner, int64_t oute
   __syncthreads();
   const int w = tid % W, t = tid / W;
   if (mode == 1) {
-    fft_tile<R, N, +1>(s, W, 1, w, t, tw);
+    fft_tile<R, N, +1, P>(s, W, 1, w, t, tw);
   } else {
-    fft_tile<R, N, -1>(s, W, 1, w, t, tw);
+    fft_tile<R, N, -1, P>(s, W, 1, w, t, tw);
     if (mode == 2) {
       const Tw<R> last = ph.tab[ph.ndim - 1];
       for (int f = tid; f < W * N; f += blockDim.x) {
@@ -160,7 +160,7 @@ k_fft_strided(cplx<R>* __restrict__ data, int64_t S, int64_t inner, int64_t oute
         }
       }
       __syncthreads();
-      fft_tile<R, N, +1>(s, W, 1, w, t, tw);
+      fft_tile<R, N, +1, P>(s, W, 1, w, t, tw);
     }
   }
   for (int f = tid; f < W * N; f += blockDim.x) {
@@ -439,9 +439,32 @@ struct PotArgs {
   cplx<R> zee_lo[kMaxD];       // FP32 tails of the Zeeman factors
 };
 
+// sin x and cos x - 1 in FP32.  For |x| <= 1/2 (the usual case: the phase angles of
+// one split step are small) both come from their Taylor series, summed by Horner's
+// rule in x^2 through the x^9 and x^10 terms (the first omitted term is below 3e-11
+// of the result at |x| = 1/2); cos x - 1 is formed directly, so it keeps full relative
+// precision for small x.  Larger angles use one sincosf of x/2:
+// sin x = 2 sin(x/2) cos(x/2), cos x - 1 = -2 sin^2(x/2).
+__device__ __forceinline__ void sin_cosm1(float x, float& sn, float& cm1) {
+  if (fabsf(x) <= 0.5f) {
+    const float x2 = x * x;
+    const float ps = fmaf(x2, fmaf(x2, fmaf(x2, 1.0f / 362880.0f, -1.0f / 5040.0f), 1.0f / 120.0f), -1.0f / 6.0f);
+    sn = fmaf(x * x2, ps, x);
+    const float pc = fmaf(x2, fmaf(x2, fmaf(x2, fmaf(x2, -1.0f / 3628800.0f, 1.0f / 40320.0f), -1.0f / 720.0f),
+                                   1.0f / 24.0f),
+                          -0.5f);
+    cm1 = x2 * pc;
+  } else {
+    float sh, ch;
+    sincosf(0.5f * x, &sh, &ch);
+    sn = 2.0f * sh * ch;
+    cm1 = -2.0f * sh * sh;
+  }
+}
+
 // psi_c *= exp(-i Veff tau) * zee_c  (real time) or exp(-Veff tau) * zee_c (imaginary time),
 // src/propagators.jl:95-116.  FP64 keeps the reference's product order; FP32 applies
-// the potential phase as psi + psi*(cos x - 1, -sin x) with cos x - 1 = -2 sin^2(x/2):
+// the potential phase as psi + psi*(cos x - 1, -sin x) with cos x - 1 from sin_cosm1:
 // for the small angles of the trap centre cosf(x) rounds to 1 while sinf(x) does not,
 // and a plain product would change |psi| systematically every step.
 template <typename R, int D>
@@ -461,9 +484,9 @@ __device__ __forceinline__ void diag_apply(cplx<R> (&v)[D], R veff, R tau, int i
 #pragma unroll
     for (int c = 0; c < D; ++c) v[c] = v[c] * (base * zee[c]);
   } else {
-    const float x = veff * tau;
-    const float sn = sinf(x), sh = sinf(0.5f * x);
-    const float2 w1 = mk<float>(-2.0f * sh * sh, -sn);
+    float sn, cm1;
+    sin_cosm1(veff * tau, sn, cm1);
+    const float2 w1 = mk<float>(cm1, -sn);
 #pragma unroll
     for (int c = 0; c < D; ++c) {
       const float2 z = cmul_comp(v[c], zee[c], zee_lo[c]);
@@ -477,7 +500,8 @@ __device__ __forceinline__ void diag_point(cplx<R> (&v)[D], R Vp, const PotArgs<
   R n = 0;
 #pragma unroll
   for (int c = 0; c < D; ++c) n += abs2(v[c]);
-  const R Vint = c0 * n + a.c_lhy * n * sqrt(n);
+  R Vint = c0 * n;
+  if (a.c_lhy != (R)0) Vint += a.c_lhy * n * sqrt(n);
   diag_apply<R, D>(v, Vp + Vint, a.tau_d, a.itp, a.zee, a.zee_lo);
 }
 
@@ -519,9 +543,18 @@ template <typename R, int D>
 __device__ __forceinline__ void rodrigues_point(cplx<R> (&v)[D], R c1, R tau, int itp, const SpinTabs<R>& st) {
   R fx, fy, fz;
   spin_vector<R, D>(v, st, fx, fy, fz);
-  const R fm = sqrt(fx * fx + fy * fy + fz * fz);
-  if (fm < (R)1e-30) return;
-  const R inv = (R)1 / fm;
+  R fm, inv;
+  if constexpr (sizeof(R) == 8) {
+    fm = sqrt(fx * fx + fy * fy + fz * fz);
+    if (fm < (R)1e-30) return;
+    inv = (R)1 / fm;
+  } else {
+    // |<F>| below ~1e-19 (|<F>|^2 under the FP32 normal range) rotates by less than an ulp
+    const float f2 = fx * fx + fy * fy + fz * fz;
+    if (!(f2 > 1e-37f)) return;
+    inv = rsqrtf(f2);
+    fm = f2 * inv;
+  }
   cplx<R> w[D], w2[D];
   nF_apply<R, D>(v, fx * inv, fy * inv, fz * inv, st, w);
   nF_apply<R, D>(w, fx * inv, fy * inv, fz * inv, st, w2);
@@ -531,9 +564,14 @@ __device__ __forceinline__ void rodrigues_point(cplx<R> (&v)[D], R c1, R tau, in
 #pragma unroll
     for (int c = 0; c < D; ++c) v[c] = v[c] - sh * w[c] + chm1 * w2[c];
   } else {
-    R sn, sh;
-    if constexpr (sizeof(R) == 8) sn = sin(th), sh = sin(th * (R)0.5); else sn = sinf(th), sh = sinf(th * 0.5f);
-    const R cm1 = (R)-2 * sh * sh;  // cos(th) - 1 without cancellation
+    R sn, cm1;  // sin th and cos th - 1 (without cancellation)
+    if constexpr (sizeof(R) == 8) {
+      sn = sin(th);
+      const R sh = sin(th * (R)0.5);
+      cm1 = (R)-2 * sh * sh;
+    } else {
+      sin_cosm1(th, sn, cm1);
+    }
 #pragma unroll
     for (int c = 0; c < D; ++c) v[c] = v[c] + mul_mi(sn * w[c]) + cm1 * w2[c];
   }
@@ -756,11 +794,21 @@ __device__ __forceinline__ void pot_stage(cplx<R> (&v)[D], R Vp, const PotArgs<R
   if (a.post_diag) diag_point<R, D>(v, Vp, a, c0);
 }
 
-template <typename R, int N, int D, int RPB>
-__global__ void __launch_bounds__(D * RPB * (N / PlanOf<R, N>::E))
+// Threads of a row-pass block: enough for the FFTs (D*RPB lines of TPL threads) and
+// for one point per thread in the potential stage, whichever is more.
+template <typename R, int N, int D, int RPB, int P = 0>
+constexpr int row_threads() {
+  constexpr int fft = D * RPB * (N / PlanOf<R, N, P>::E);
+  constexpr int pts = RPB * N;
+  constexpr int t = fft > pts ? fft : (pts > 1024 ? 1024 : pts);
+  return (t + 31) / 32 * 32;
+}
+
+template <typename R, int N, int D, int RPB, int P = 0>
+__global__ void __launch_bounds__(row_threads<R, N, D, RPB, P>())
 k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
   pdl_begin();
-  constexpr int TPL = N / PlanOf<R, N>::E;
+  constexpr int TPL = N / PlanOf<R, N, P>::E;
   constexpr int NL = D * RPB;  // line = c*RPB + r
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);
@@ -786,7 +834,8 @@ k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
   }
   __syncthreads();
   const int t = tid % TPL, l = tid / TPL;
-  if (a.flags & RP_INV_X) fft_tile<R, N, +1>(s, 1, N, l, t, tw);
+  const bool fa = l < NL;  // this thread works on an FFT line
+  if (a.flags & RP_INV_X) fft_tile<R, N, +1, P>(s, 1, N, l, t, tw, fa);
   if (a.flags & RP_POT1) {
     for (int p = tid; p < RPB * N; p += blockDim.x) {
       const int r = p / N, x = p % N;
@@ -800,11 +849,11 @@ k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
     }
     __syncthreads();
   }
-  if (a.flags & (RP_FWD_X | RP_KIN_X)) fft_tile<R, N, -1>(s, 1, N, l, t, tw);
+  if (a.flags & (RP_FWD_X | RP_KIN_X)) fft_tile<R, N, -1, P>(s, 1, N, l, t, tw, fa);
   if (a.flags & RP_KIN_X) {
     for (int f = tid; f < NL * N; f += blockDim.x) s[f] = tw_mul<R>(s[f], ph.tab[0], f % N, false);
     __syncthreads();
-    fft_tile<R, N, +1>(s, 1, N, l, t, tw);
+    fft_tile<R, N, +1, P>(s, 1, N, l, t, tw, fa);
   }
   double acc = 0.0;
   if (a.flags & (RP_POT2 | RP_NORM)) {
@@ -873,7 +922,8 @@ __device__ __forceinline__ void diag_point_t(cplx<R> (&v)[D], R Vp, const Tensor
   R n = 0;
 #pragma unroll
   for (int c = 0; c < D; ++c) n += abs2(v[c]);
-  const R Vint = a.c0 * n + a.c_lhy * n * sqrt(n);
+  R Vint = a.c0 * n;
+  if (a.c_lhy != (R)0) Vint += a.c_lhy * n * sqrt(n);
   diag_apply<R, D>(v, Vp + Vint, a.tau_d, a.itp, a.zee, a.zee_lo);
 }
 

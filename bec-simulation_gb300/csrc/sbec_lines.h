@@ -1,0 +1,71 @@
+// FFT line kernels (contiguous x lines, strided lines, the fused row pass) in the
+// variants the autotuner chooses between.  A variant V combines
+//   plan family  V & 1:  0 = the precision's default radix set (FP64 radix-16,
+//                            FP32 radix-4/8), 1 = the other one;
+//   tile scale   V >> 1: 0 = ~64-thread tiles (spread a single small solve over
+//                            all SMs), 1 = wider tiles (x lines / row pass 2x
+//                            the lines per block, strided 4x the columns, i.e.
+//                            64-128 contiguous bytes per row segment).
+// FP32 lines of kMinTunedLine points or more have all four variants, each compiled
+// in its own translation unit (sbec_lines_f32_v<V>.cu); FP64 and shorter lines
+// have variant 0 only.
+#pragma once
+
+#include <algorithm>
+
+#include "sbec_engine.h"
+#include "sbec_kernels.cuh"
+
+namespace sbec {
+
+constexpr int kLineVariants = 4;
+constexpr int kMinTunedLine = 32;
+
+template <typename R>
+struct LineCtx {
+  cudaStream_t stream;
+  bool pdl;
+  PhaseRef<R> ph;
+  SpinTabs<R> st;
+};
+
+template <typename R, int V>
+struct LineKernels {
+  static void fft_x(const LineCtx<R>& c, const Tw<R>& tw, int n, cplx<R>* data, int64_t n_lines, int mode);
+  static void fft_strided(const LineCtx<R>& c, const Tw<R>& tw, int n, cplx<R>* data, int64_t S, int64_t inner,
+                          int64_t outer, int64_t outer_stride, int n_in, int n_out, int mode, const int* omap,
+                          int oper);
+  static void row(const LineCtx<R>& c, const Tw<R>& tw, int n, int D, const RowArgs<R>& a, int blocks);
+};
+
+// The variant actually compiled for a line of n points.
+inline int line_variant(bool fp32, int n, int V) { return (fp32 && n >= kMinTunedLine) ? V : 0; }
+
+// ---- host mirrors of the tile shapes (must match sbec_lines_impl.cuh)
+inline int line_tpl(bool fp32, int n, int V) { return std::max(1, n / plan_radix_host(fp32, n, V & 1)); }
+
+inline int row_rpb_host(bool fp32, int n, int D, int V) {
+  V = line_variant(fp32, n, V);
+  int r = 64 / (D * line_tpl(fp32, n, V));
+  if (r < 1) r = 1;
+  return r << (V >> 1);
+}
+
+inline int row_threads_host(bool fp32, int n, int D, int V) {
+  V = line_variant(fp32, n, V);
+  const int rpb = row_rpb_host(fp32, n, D, V);
+  const int fft = D * rpb * line_tpl(fp32, n, V);
+  const int pts = std::min(rpb * n, 1024);
+  return (std::max(fft, pts) + 31) / 32 * 32;
+}
+
+inline size_t row_smem_host(bool fp32, int n, int D, int V) {
+  return (size_t)(fp32 ? 8 : 16) * D * row_rpb_host(fp32, n, D, V) * n;
+}
+
+// A row-pass variant can run: at most 1024 threads and 200 KB of shared memory.
+inline bool row_variant_ok(bool fp32, int n, int D, int V) {
+  return row_threads_host(fp32, n, D, V) <= 1024 && row_smem_host(fp32, n, D, V) <= 200 * 1024;
+}
+
+}  // namespace sbec

@@ -120,6 +120,11 @@ class Workspace:
         return n.value
 
     @property
+    def tuning_report(self) -> str:
+        """Autotuner decisions (line-kernel variant per call shape, with every variant's time)."""
+        return _report(self._lib.sbec_tuning_report, self.handle)
+
+    @property
     def stream_ptr(self) -> int:
         p = C.c_void_p()
         check(self._lib.sbec_ws_stream(self.handle, C.byref(p)))
@@ -567,6 +572,18 @@ class GroundStateBatch:
         E = np.empty(self.n)
         check(self._lib.sbec_batch_energies(self._h, dptr(E)))
         return E
+
+    @property
+    def tuning_report(self) -> str:
+        return _report(self._lib.sbec_batch_tuning_report, self._h)
+
+
+def _report(fn, handle) -> str:
+    n = C.c_int64()
+    check(fn(handle, None, 0, C.byref(n)))
+    buf = C.create_string_buffer(n.value + 1)
+    check(fn(handle, buf, n.value + 1, C.byref(n)))
+    return buf.value.decode()
 
 
 def find_ground_states_batched(*, grid: Grid, atom: AtomSpecies, interactions: list, psi_inits: list, zeeman=None,

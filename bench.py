@@ -238,6 +238,7 @@ def run_batched(S, jobs, precision: str, n_steps: int, tol: float) -> tuple:
     """Runs every job through GroundStateBatch grouped by grid size; returns (seconds, results by idx)."""
     import time as _t
     res = {}
+    tune = {}
     total = 0.0
     for n in sorted({j["n"] for j in jobs}):
         group = [j for j in jobs if j["n"] == n]
@@ -248,9 +249,12 @@ def run_batched(S, jobs, precision: str, n_steps: int, tol: float) -> tuple:
         t0 = _t.perf_counter()
         r = b.ground_state(n_steps, tol, max(1, n_steps // 10))
         total += _t.perf_counter() - t0
+        log(f"batched {precision} {len(group)} x {n}^2: {_t.perf_counter() - t0:.2f} s")
+        tune[n] = b.tuning_report.splitlines()
         b.close()
         for j, x in zip(group, r):
             res[j["idx"]] = x
+    res["autotune"] = tune
     return total, res
 
 
@@ -280,6 +284,7 @@ def bench_batched(S, sample: int = 6, n_steps: int = 10000, tol: float = 1e-8) -
     mean = {n: float(np.mean(v)) for n, v in by_size.items()}
     overall = float(np.mean([x for v in by_size.values() for x in v]))
     est64 = sum(mean.get(j["n"], overall) for j in jobs)
+    tune = r32.pop("autotune")
     conv = sum(1 for x in r32.values() if x["converged"])
     return {"workload": "512 ITP solves, 2D spin-1, c1 in 64 values of [-1,1] x 8 starts, grids 64^2/128^2/256^2, "
                         "dt=0.005, tol=1e-8, check every 1000 of 10000 steps",
@@ -287,7 +292,15 @@ def bench_batched(S, sample: int = 6, n_steps: int = 10000, tol: float = 1e-8) -
             "fp64_one_at_a_time_solves_per_s": len(jobs) / est64,
             "fp64_sample": f"{sample} solves timed one at a time ({secs64:.2f} s), extrapolated per grid size",
             "speedup_vs_fp64_one_at_a_time": est64 / secs32,
-            "energy_rel_err_fp32_vs_fp64_max": max(errs), "converged": conv}
+            "energy_rel_err_fp32_vs_fp64_max": max(errs), "converged": conv, "autotune": tune}
+
+
+_T0 = time.perf_counter()
+
+
+def log(msg: str) -> None:
+    """Progress line on stderr (the JSON result stays alone on stdout)."""
+    print(f"[bench {time.perf_counter() - _T0:8.1f}s] {msg}", file=sys.stderr, flush=True)
 
 
 # ----------------------------------------------------------------------------- serving
@@ -299,8 +312,9 @@ def bench_serving(S, n_requests: int, fp64_probe_steps: int = 20) -> dict:
     from spinorbec import serve
 
     reqs = serve.poisson_requests(n_requests, rate=200.0, seed=5)
-    srv = serve.Server(hbm_budget_bytes=150e9, max_slots=32)
+    srv = serve.Server(hbm_budget_bytes=150e9, max_slots=32, runner=_logged(serve.run_request))
     out = srv.run(reqs, realtime=True)
+    log(f"serving: {len(reqs)} requests in {out['wall_s']:.1f} s")
     est64 = 0.0
     probes = {}
     for r, res in zip(reqs, out["results"]):
@@ -319,6 +333,16 @@ def bench_serving(S, n_requests: int, fp64_probe_steps: int = 20) -> dict:
             "fp64_one_at_a_time_solves_per_s": len(reqs) / est64,
             "fp64_estimate": f"per grid/F/kind: setup + {fp64_probe_steps}-step timed probe x steps of the served solve",
             "speedup_vs_fp64_one_at_a_time": est64 / out["wall_s"]}
+
+
+def _logged(runner):
+    def run(req):
+        t0 = time.perf_counter()
+        out = runner(req)
+        log(f"  request {req.rid}: {req.kind} {req.n_points} F={req.F} ddi={req.enable_ddi} {out['steps']} steps "
+            f"{time.perf_counter() - t0:.2f} s")
+        return out
+    return run
 
 
 def fp64_probe(S, r, k: int) -> tuple:
@@ -376,6 +400,7 @@ def bench_3d_f6(S, n: int = 128, steps32: int = 20, steps64: int = 2) -> dict:
                                      keep_psi=False, max_accepted=k)
         secs = time.perf_counter() - t0
         acc = int(r["n_accepted"])
+        log(f"3d f6 {prec}: {acc} accepted, {int(r['n_rejected'])} rejected in {secs:.2f} s")
         ws.close()
         out[prec] = {"seconds": secs, "accepted_steps": acc, "rejected_steps": int(r["n_rejected"]),
                      "steps_per_s": acc / secs, "value": units * acc / secs, "unit": UNIT,
@@ -428,6 +453,7 @@ def main_gpu(args) -> None:
                              n_steps=args.gs_steps, tol=1e-8, initial_state="polar")
     psi0 = noisy_polar(gs["workspace"].psi, dV)
     gs["workspace"].close()
+    log("initial state ready")
 
     flush = torch.empty(int(256e6) // 4, dtype=torch.float32, device="cuda")
 
@@ -488,6 +514,7 @@ def main_gpu(args) -> None:
         except Exception:
             traffic = None
     kernel_share = {k: round(v["ms"] / sum(x["ms"] for x in prof.values()), 4) for k, v in prof.items()}
+    autotune = ws32.tuning_report.splitlines()
     ws32.close()
 
     # ---- e2e through the C ABI: host psi in, 100 save points with host copies, psi out
@@ -525,15 +552,19 @@ def main_gpu(args) -> None:
         v64 = dist.world * units_per_run(p_steps) * max(1, args.steps // 2) / (ms64 / 1e3)
         plain = {"value": v64, "unit": UNIT, "steps_per_run": p_steps}
 
+    log("main workload done")
     batched = None
     if not args.no_batched:
         batched = bench_batched(S)
+        log("batched done")
     serving = None
     if not args.no_serving:
         serving = bench_serving(S, args.serve_requests)
+        log("serving done")
     dipolar = None
     if not args.no_3d:
-        dipolar = bench_3d_f6(S)
+        dipolar = bench_3d_f6(S, n=args.grid_3d)
+        log("3d f6 done")
 
     cpu = None
     if dist.rank == 0 and not args.no_cpu:
@@ -548,6 +579,7 @@ def main_gpu(args) -> None:
                        "precision": "fp32 bulk (FFTs, phases), fp64 reductions", "parallelism": "replicas",
                        "l2": "flushed (256 MB write) between timed runs; psi (1.5 MB) stays L2-resident within a run"},
             "e2e": e2e,
+            "autotune": autotune,
             "plain_fp64": plain,
             "batched_ground_states": batched,
             "serving": serving,
@@ -580,6 +612,7 @@ def ncu_case(args) -> None:
                               potential=S.HarmonicTrap(*OMEGA), sim_params=S.SimParams(DT, k, False, None, k + 1),
                               precision=case.split("_")[1])
         S.run_simulation(ws, keep_psi=False)
+        print(ws.tuning_report)
     elif case == "batch256_fp32":
         g = S.make_grid(S.GridConfig((256, 256), (20.0, 20.0)))
         nb = args.ncu_batch
@@ -587,6 +620,7 @@ def ncu_case(args) -> None:
         b = S.GroundStateBatch(grid=g, atom=S.Rb87, c0s=[10.0] * nb, c1s=list(np.linspace(-1, 1, nb)), psi_inits=psis,
                                potential=S.HarmonicTrap(1.0, 1.0), dt=0.005, precision="fp32")
         b.ground_state(k, 1e-30, k)
+        print(b.tuning_report)
     elif case in ("3d_f6_fp32", "3d_f6_fp64"):
         ip = S.interaction_params_from_constraint(c_total=4689.0, c1_ratio=1 / 36, F=6, c_extra=(0.0, 0.0, 50.0))
         n = args.ncu_grid
@@ -599,6 +633,22 @@ def ncu_case(args) -> None:
     else:
         raise SystemExit(f"unknown --ncu-case {case}")
     print(f"ncu case {case}: {k} steps done")
+
+
+def only_section(args) -> None:
+    """One optional section on its own (its JSON object on stdout)."""
+    import __graft_entry__
+
+    __graft_entry__.build()
+    import spinorbec as S
+
+    if args.only == "batched":
+        out = bench_batched(S)
+    elif args.only == "serving":
+        out = bench_serving(S, args.serve_requests)
+    else:
+        out = bench_3d_f6(S, n=args.grid_3d)
+    print(json.dumps({args.only: out}), flush=True)
 
 
 def main():
@@ -616,11 +666,17 @@ def main():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-3d", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--only", default=None, choices=["batched", "serving", "3d"],
+                    help="run one optional section alone and print its JSON")
+    ap.add_argument("--grid-3d", type=int, default=128)
     ap.add_argument("--ncu-case", default=None, help="short run for profiling: 2d256_fp32|2d256_fp64|batch256_fp32|3d_f6_fp32|3d_f6_fp64")
     ap.add_argument("--ncu-steps", type=int, default=4)
     ap.add_argument("--ncu-grid", type=int, default=32)
     ap.add_argument("--ncu-batch", type=int, default=170, help="solves in the batch256_fp32 case (the 256^2 group)")
     args = ap.parse_args()
+    if args.only:
+        only_section(args)
+        return
     if args.ncu_case:
         ncu_case(args)
         return

@@ -219,6 +219,11 @@ sbec_status sbec_profile_read(sbec_ws* ws, sbec_kernel_stat* out, int32_t max, i
 sbec_status sbec_launch_count(sbec_ws* ws, int64_t* n);
 /* The workspace's CUDA stream (cudaStream_t), for callers that order or time work on it. */
 sbec_status sbec_ws_stream(sbec_ws* ws, void** stream);
+/* Autotuner decisions of a workspace / batch (FFT line-kernel variant per call shape, with
+ * the measured time of every variant), as text; *len receives the full length.  No
+ * counterpart in the reference (FFTW plans are chosen inside FFTW). */
+sbec_status sbec_tuning_report(sbec_ws* ws, char* buf, int64_t cap, int64_t* len);
+sbec_status sbec_batch_tuning_report(sbec_batch* b, char* buf, int64_t cap, int64_t* len);
 
 /* ---- allocation-free reduction --------------------------------------------
  * No counterpart in the reference: an extra entry point for callers that cannot

@@ -1,0 +1,96 @@
+"""FFT line-kernel variants and their autotuner.
+
+Every compiled variant (plan family x tile scale) must give the FP32-form result
+on its own: each is forced in turn (SBEC_TUNE_FORCE, read when a workspace is
+created) and checked against the FP64 oracle on the fused row/column path, the
+batched ground state and the unfused x-line path (3-D with DDI).  With tuning on,
+the decisions are reported and two workspaces of one shape give identical
+results."""
+
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+import spinorbec as S
+from parity_util import make_pair, rel_psi_err
+
+pytestmark = pytest.mark.gpu
+
+VARIANTS = [0, 1, 2, 3]
+
+
+class _env:
+    def __init__(self, **kv):
+        self.kv = kv
+
+    def __enter__(self):
+        self.old = {k: os.environ.get(k) for k in self.kv}
+        os.environ.update({k: str(v) for k, v in self.kv.items()})
+
+    def __exit__(self, *a):
+        for k, v in self.old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+
+@pytest.mark.parametrize("v", VARIANTS)
+def test_forced_variant_fused_2d(gpu, v):
+    with _env(SBEC_TUNE_FORCE=v):
+        ws_o, ws_g = make_pair((64, 64), (20.0, 20.0), 1, c0=10.0, c1=0.5, omega=(1.0, 1.0), zeeman=(0.0, 0.1),
+                               dt=1e-3, precision="fp32", state="polar")
+    for _ in range(50):
+        O.split_step(ws_o)
+    S.split_step(ws_g, 50)
+    assert rel_psi_err(ws_g.psi, ws_o.psi) < 5e-5
+    assert "forced" in ws_g.tuning_report
+    ws_g.close()
+
+
+@pytest.mark.parametrize("v", VARIANTS)
+def test_forced_variant_batched_ground_state(gpu, v):
+    n, L = (128, 128), (20.0, 20.0)
+    og = O.make_grid(O.GridConfig(n, L))
+    hg = S.make_grid(S.GridConfig(n, L))
+    psis = [O.init_psi(og, 1, st, seed=3) for st in ("polar", "ferromagnetic", "random")]
+    c1s = [-0.5, 0.5, 0.2]
+    kw = dict(dt=0.005, n_steps=400, tol=1e-12)
+    with _env(SBEC_TUNE_FORCE=v):
+        res = S.find_ground_states_batched(grid=hg, atom=S.Rb87, interactions=[S.InteractionParams(10.0, c)
+                                                                               for c in c1s],
+                                           psi_inits=psis, potential=S.HarmonicTrap(1.0, 1.0), precision="fp32", **kw)
+    for c1, p0, r in zip(c1s, psis, res):
+        ro = O.find_ground_state(grid=og, atom=O.Rb87, interactions=O.InteractionParams(10.0, c1),
+                                 V=O.harmonic_potential(og, (1.0, 1.0)), psi_init=p0, **kw)
+        assert abs(r["energy"] - ro["energy"]) / abs(ro["energy"]) < 1e-6
+
+
+@pytest.mark.parametrize("v", VARIANTS)
+def test_forced_variant_unfused_3d_ddi(gpu, v):
+    with _env(SBEC_TUNE_FORCE=v):
+        ws_o, ws_g = make_pair((32, 32, 32), (16.0, 16.0, 16.0), 1, c0=5.0, c1=0.3, omega=(1.0, 1.0, 1.2),
+                               ddi=True, c_dd=2.0, dt=1e-3, precision="fp32", state="ferromagnetic")
+    for _ in range(5):
+        O.split_step(ws_o)
+    S.split_step(ws_g, 5)
+    assert rel_psi_err(ws_g.psi, ws_o.psi) < 5e-5
+    assert abs(S.total_energy(ws_g) - O.total_energy(ws_o)) / abs(O.total_energy(ws_o)) < 1e-5
+    ws_g.close()
+
+
+def test_tuning_reports_and_is_shared(gpu):
+    with _env(SBEC_TUNE=1):
+        # a shape no other test uses, so this process has not tuned it yet
+        ws = [make_pair((128, 32), (20.0, 10.0), 1, c0=10.0, c1=0.5, omega=(1.0, 1.0), dt=1e-3, precision="fp32",
+                        state="polar", seed=11)[1] for _ in range(2)]
+    for w in ws:
+        S.split_step(w, 20)
+    rep = ws[0].tuning_report + ws[1].tuning_report
+    assert "row" in rep and "chosen v" in rep
+    # the second workspace reuses the first one's decisions: same kernels, same result
+    assert np.array_equal(ws[0].psi, ws[1].psi)
+    for w in ws:
+        w.close()
