@@ -462,6 +462,25 @@ __device__ __forceinline__ void sin_cosm1(float x, float& sn, float& cm1) {
   }
 }
 
+// sinh x and cosh x - 1 in FP32 (the imaginary-time spin rotation): Taylor series
+// through the x^9 / x^10 terms for |x| <= 1/2, as in sin_cosm1 (cosh x - 1 then keeps
+// full relative precision, where coshf(x) - 1 cancels), otherwise from one expf.
+__device__ __forceinline__ void sinh_coshm1(float x, float& sh, float& chm1) {
+  if (fabsf(x) <= 0.5f) {
+    const float x2 = x * x;
+    const float ps = fmaf(x2, fmaf(x2, fmaf(x2, 1.0f / 362880.0f, 1.0f / 5040.0f), 1.0f / 120.0f), 1.0f / 6.0f);
+    sh = fmaf(x * x2, ps, x);
+    const float pc = fmaf(x2, fmaf(x2, fmaf(x2, fmaf(x2, 1.0f / 3628800.0f, 1.0f / 40320.0f), 1.0f / 720.0f),
+                                   1.0f / 24.0f),
+                          0.5f);
+    chm1 = x2 * pc;
+  } else {
+    const float e = expf(x), ei = 1.0f / e;
+    sh = 0.5f * (e - ei);
+    chm1 = 0.5f * (e + ei) - 1.0f;
+  }
+}
+
 // psi_c *= exp(-i Veff tau) * zee_c  (real time) or exp(-Veff tau) * zee_c (imaginary time),
 // src/propagators.jl:95-116.  FP64 keeps the reference's product order; FP32 applies
 // the potential phase as psi + psi*(cos x - 1, -sin x) with cos x - 1 from sin_cosm1:
@@ -475,7 +494,7 @@ __device__ __forceinline__ void diag_apply(cplx<R> (&v)[D], R veff, R tau, int i
 #pragma unroll
     for (int c = 0; c < D; ++c) {
       if constexpr (sizeof(R) == 8) v[c] = v[c] * (mk<R>(e, (R)0) * zee[c]);
-      else v[c] = cmul_comp(v[c], zee[c], zee_lo[c]) * e;
+      else v[c] = v[c] * (e * zee[c].x);  // imaginary-time Zeeman factors are real; renormalised each step
     }
     return;
   }
@@ -560,7 +579,13 @@ __device__ __forceinline__ void rodrigues_point(cplx<R> (&v)[D], R c1, R tau, in
   nF_apply<R, D>(w, fx * inv, fy * inv, fz * inv, st, w2);
   const R th = c1 * fm * tau;
   if (itp) {
-    const R sh = sinh(th), chm1 = cosh(th) - (R)1;
+    R sh, chm1;
+    if constexpr (sizeof(R) == 8) {
+      sh = sinh(th);
+      chm1 = cosh(th) - (R)1;
+    } else {
+      sinh_coshm1(th, sh, chm1);
+    }
 #pragma unroll
     for (int c = 0; c < D; ++c) v[c] = v[c] - sh * w[c] + chm1 * w2[c];
   } else {
