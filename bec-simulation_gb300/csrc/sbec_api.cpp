@@ -37,6 +37,7 @@ struct sbec_ws {
   std::unique_ptr<EngineBase> eng;
   double kin_dt = 0.0;    // parameters of the current kinetic phase (the batched kinetic cache)
   bool kin_itp = false;
+  bool pipelined_snapshots = false;  // sbec_set_snapshot_mode
   std::vector<double> host_psi;
 };
 
@@ -185,6 +186,69 @@ int snapshot(sbec_ws* ws, sbec_callback cb, void* user) {
 
 void check_cb(int rc) {
   if (rc != 0) fail(SBEC_ERR_CALLBACK, "callback requested stop");
+}
+
+// Leapfrog run with pipelined save points: the snapshot of save point j (energy
+// sums and FP64 psi into pinned slot j & 1) is enqueued behind segment j, segment
+// j + 1 is enqueued, and only then is save point j handed to the callback, so the
+// host-side callback overlaps the device work of the next segment.  A stop request
+// restores psi, t and step from the snapshot of that save point.
+void run_leapfrog_pipelined(sbec_ws* ws, int64_t n_steps, int64_t save_every, sbec_callback cb, void* user) {
+  EngineBase& e = *ws->eng;
+  const double dt = e.dt;
+  const Setup& s = e.setup();
+  struct Meta {
+    double t;
+    int64_t step;
+  } meta[2] = {};
+  auto deliver = [&](int k) {
+    sbec_snapshot sn{};
+    std::vector<double> sums(s.D);
+    sbec_energy_terms t{};
+    sn.psi = e.snapshot_wait(k, &t, sums.data());
+    sn.t = meta[k & 1].t;
+    sn.step = meta[k & 1].step;
+    sn.energy = t.kinetic + t.trap + t.zeeman + t.c0 + t.c1 + t.ddi + t.lhy + t.tensor;
+    double n = 0.0, m = 0.0;
+    for (int c = 0; c < s.D; ++c) {
+      n += sums[c];
+      m += (double)(s.F - c) * sums[c] * s.dV;
+    }
+    sn.norm = n * s.dV;
+    sn.magnetization = m;
+    if (cb(user, &sn) != 0) {
+      e.restore_snapshot(k);
+      e.t = meta[k & 1].t;
+      e.step = meta[k & 1].step;
+      fail(SBEC_ERR_CALLBACK, "callback requested stop");
+    }
+  };
+  check_cb(snapshot(ws, cb, user));
+  e.lf_open(dt);
+  int64_t step = 0;
+  int pending = -1, k = 0;
+  while (step < n_steps) {
+    const int64_t seg_end = std::min(n_steps, (step / save_every + 1) * save_every);
+    const int64_t nseg = seg_end - step;
+    e.lf_steps(nseg - 1, dt);
+    e.lf_close(dt);
+    for (int64_t i = 0; i < nseg; ++i) {
+      e.t += dt;
+      e.step += 1;
+    }
+    step = seg_end;
+    if (pending >= 0) {
+      deliver(pending);
+      pending = -1;
+    }
+    if (step % save_every == 0) {
+      e.snapshot_enqueue(k);
+      meta[k & 1] = {e.t, e.step};
+      pending = k++;
+    }
+    if (step < n_steps) e.lf_open(dt);
+  }
+  if (pending >= 0) deliver(pending);
 }
 
 // _normalize_psi_constrained! (src/ground_state.jl:279-320)
@@ -423,6 +487,8 @@ sbec_status sbec_run_simulation(sbec_ws* ws, int64_t n_steps, int64_t save_every
       step = nxt;
       if (step % save_every == 0) check_cb(snapshot(ws, cb, user));
     }
+  } else if (e.fused_path() && !ws->kin_itp && ws->kin_dt == e.dt && ws->pipelined_snapshots && cb) {
+    run_leapfrog_pipelined(ws, n_steps, save_every, cb, user);
   } else if (e.fused_path() && !ws->kin_itp && ws->kin_dt == e.dt) {
     // leapfrog with the fused row passes: identical operator sequence
     const double dt = e.dt;
@@ -895,6 +961,13 @@ static void copy_report(const std::string& r, char* buf, int64_t cap, int64_t* l
     std::memcpy(buf, r.data(), n);
     buf[n] = 0;
   }
+}
+
+sbec_status sbec_set_snapshot_mode(sbec_ws* ws, int32_t pipelined) {
+  SBEC_API_BEGIN
+  need(ws, "workspace");
+  ws->pipelined_snapshots = pipelined != 0;
+  SBEC_API_END
 }
 
 sbec_status sbec_tuning_report(sbec_ws* ws, char* buf, int64_t cap, int64_t* len) {

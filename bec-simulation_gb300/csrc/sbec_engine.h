@@ -132,6 +132,11 @@ class EngineBase {
   virtual sbec_energy_terms energy_terms_and_norms(double* comp_sums) = 0;
   // psi downloaded into the workspace's pinned staging buffer (valid until the next call)
   virtual const double* psi_to_pinned() = 0;
+  // Pipelined snapshots (two slots, k & 1): enqueue energy sums and the FP64 psi into
+  // pinned slot k; wait for slot k and read it; restore psi from slot k.
+  virtual void snapshot_enqueue(int k) = 0;
+  virtual const double* snapshot_wait(int k, sbec_energy_terms* terms, double* comp_sums) = 0;
+  virtual void restore_snapshot(int k) = 0;
   virtual double l2_change(int a, int b) = 0;                      // ||a-b||^2/||b||^2
   virtual void max_abs(int a, int b, double* max_a, double* max_diff) = 0;
   virtual double ddi_phi_max() = 0;                                // last periodic Φ (ITP check)

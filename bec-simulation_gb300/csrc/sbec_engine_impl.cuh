@@ -172,6 +172,11 @@ class Engine final : public EngineBase {
     for (void* p : allocs_) cudaFree(p);
     if (host_res_) cudaFreeHost(host_res_);
     if (host_psi_) cudaFreeHost(host_psi_);
+    for (int k = 0; k < 2; ++k) {
+      if (snap_res_[k]) cudaFreeHost(snap_res_[k]);
+      if (snap_psi_[k]) cudaFreeHost(snap_psi_[k]);
+      if (snap_ev_[k]) cudaEventDestroy(snap_ev_[k]);
+    }
     cudaStreamDestroy(stream_);
   }
 
@@ -297,9 +302,53 @@ class Engine final : public EngineBase {
     return host_psi_;
   }
 
+  // ---- pipelined snapshots: two pinned slots, each receiving the reduction sums and
+  // the FP64 psi of one save point in stream order, with an event marking completion.
+  // The host reads slot k while the stream already runs the next segment.
+  void snapshot_enqueue(int k) override {
+    k &= 1;
+    if (!snap_res_[k]) {
+      cuda_check(cudaMallocHost(&snap_res_[k], 32 * sizeof(double)), "cudaMallocHost");
+      cuda_check(cudaMallocHost(&snap_psi_[k], sizeof(double) * 2 * nc_), "cudaMallocHost");
+      cuda_check(cudaEventCreateWithFlags(&snap_ev_[k], cudaEventDisableTiming), "cudaEventCreate");
+    }
+    energy_enqueue();
+    cuda_check(cudaMemcpyAsync(snap_res_[k], results_, 32 * sizeof(double), cudaMemcpyDeviceToHost, stream_),
+               "snapshot sums");
+    const void* src = psi_[kPsi];
+    if (sizeof(R) != 8) {
+      pb();
+      k_to_f64<R><<<grid_for(nc_), 256, 0, stream_>>>(psi_[kPsi], stage_, nc_);
+      done("convert", (16.0 + (double)sizeof(cplx<R>)) * nc_);
+      src = stage_;
+    }
+    cuda_check(cudaMemcpyAsync(snap_psi_[k], src, sizeof(double) * 2 * nc_, cudaMemcpyDeviceToHost, stream_),
+               "snapshot psi");
+    cuda_check(cudaEventRecord(snap_ev_[k], stream_), "cudaEventRecord");
+  }
+
+  const double* snapshot_wait(int k, sbec_energy_terms* terms, double* comp_sums) override {
+    k &= 1;
+    if (!snap_ev_[k]) fail(SBEC_ERR_INVALID, "no snapshot in flight");
+    cuda_check(cudaEventSynchronize(snap_ev_[k]), "cudaEventSynchronize");
+    *terms = energy_from(snap_res_[k], comp_sums);
+    return snap_psi_[k];
+  }
+
+  void restore_snapshot(int k) override {
+    sync();
+    set_psi(snap_psi_[k & 1]);
+  }
+
   sbec_energy_terms energy_terms_and_norms(double* comp_sums) override {
-    sbec_energy_terms e{};
-    const double dV = s_.dV;
+    energy_enqueue();
+    fetch(32);
+    return energy_from(host_res_, comp_sums);
+  }
+
+  // Launch every reduction of the energy and the component norms; the sums land
+  // in results_[0..31] (no host synchronisation).
+  void energy_enqueue() {
     // kinetic: forward FFT of a copy, sum k^2 |psi_hat|^2 dV / N (src/energy.jl:56-65)
     cplx<R>* scr = slot_scratch();
     cuda_check(cudaMemcpyAsync(scr, psi_[kPsi], sizeof(cplx<R>) * nc_, cudaMemcpyDeviceToDevice, stream_), "copy");
@@ -332,26 +381,31 @@ class Engine final : public EngineBase {
       done("reduce", 6.0 * (double)sizeof(R) * N_);
       finish<1>(nb, false, 31);
     }
-    fetch(32);
+  }
+
+  // Energy terms and component sums from a host copy of results_[0..31].
+  sbec_energy_terms energy_from(const double* res, double* comp_sums) const {
+    sbec_energy_terms e{};
+    const double dV = s_.dV;
     const double N = (double)N_;
-    e.kinetic = 0.5 * (host_res_[0] * dV / N);
-    e.trap = host_res_[20] * dV;
+    e.kinetic = 0.5 * (res[0] * dV / N);
+    e.trap = res[20] * dV;
     double ez = 0.0;
     for (int c = 0; c < s_.D; ++c) {
       const double mc = (double)(s_.F - c);
       const double Ec = -zeeman_p * mc + zeeman_q * mc * mc;
-      ez += Ec * host_res_[1 + c] * dV;
+      ez += Ec * res[1 + c] * dV;
     }
     e.zeeman = ez;
     if (!s_.tensor) {
-      e.c0 = 0.5 * s_.c0 * host_res_[21] * dV;
-      e.c1 = 0.5 * s_.c1 * host_res_[22] * dV;
+      e.c0 = 0.5 * s_.c0 * res[21] * dV;
+      e.c1 = 0.5 * s_.c1 * res[22] * dV;
     }
-    if (s_.ddi) e.ddi = 0.5 * host_res_[31] * dV;
-    if (s_.c_lhy != 0.0) e.lhy = (2.0 / 5.0) * s_.c_lhy * host_res_[23] * dV;
-    if (s_.tensor) e.tensor = host_res_[30] * dV;
+    if (s_.ddi) e.ddi = 0.5 * res[31] * dV;
+    if (s_.c_lhy != 0.0) e.lhy = (2.0 / 5.0) * s_.c_lhy * res[23] * dV;
+    if (s_.tensor) e.tensor = res[30] * dV;
     if (comp_sums)
-      for (int c = 0; c < s_.D; ++c) comp_sums[c] = host_res_[1 + c];
+      for (int c = 0; c < s_.D; ++c) comp_sums[c] = res[1 + c];
     return e;
   }
 
@@ -1538,6 +1592,9 @@ class Engine final : public EngineBase {
   bool use_pdl_ = false;  // SBEC_PDL=1 enables; measured slower for these short kernels
   // line-kernel variants in use (see sbec_lines.h); chosen by the autotuner
   int v_row_ = 0, v_str_ = 0, v_x_ = 0;
+  double* snap_res_[2] = {nullptr, nullptr};  // pinned snapshot slots
+  double* snap_psi_[2] = {nullptr, nullptr};
+  cudaEvent_t snap_ev_[2] = {nullptr, nullptr};
   bool tune_on_ = true;       // SBEC_TUNE=0: variant 0 everywhere
   int tune_force_ = -1;       // SBEC_TUNE_FORCE=v: variant v wherever it is compiled
   bool row_tuned_ = false;

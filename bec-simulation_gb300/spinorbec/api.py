@@ -314,9 +314,14 @@ class _Recorder:
 
 
 def run_simulation(ws: Workspace, callback: Optional[Callable] = None, keep_psi: bool = True) -> SimulationResult:
-    """``run_simulation!`` (src/simulation.jl:1-94): leapfrog real time or the standard ITP loop."""
+    """``run_simulation!`` (src/simulation.jl:1-94): leapfrog real time or the standard ITP loop.
+
+    Without a user callback the save points are recorded from pinned snapshots while the
+    device runs the next segment (sbec_set_snapshot_mode); a user callback, which may read or
+    change the workspace, gets synchronous save points as in the reference."""
     sp = ws.sim_params
     rec = _Recorder(ws, callback, keep_psi, use_count_arg=False)
+    check(ws._lib.sbec_set_snapshot_mode(ws.handle, 1 if callback is None else 0))
     st = ws._lib.sbec_run_simulation(ws.handle, sp.n_steps, sp.save_every, rec.cfunc, None)
     rec.raise_pending()
     check(st)

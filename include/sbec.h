@@ -219,6 +219,12 @@ sbec_status sbec_profile_read(sbec_ws* ws, sbec_kernel_stat* out, int32_t max, i
 sbec_status sbec_launch_count(sbec_ws* ws, int64_t* n);
 /* The workspace's CUDA stream (cudaStream_t), for callers that order or time work on it. */
 sbec_status sbec_ws_stream(sbec_ws* ws, void** stream);
+/* Save-point delivery of sbec_run_simulation: 0 (default) synchronous; 1 pipelined — each
+ * snapshot is copied to a pinned slot in stream order and handed to the callback while the
+ * device already runs the next segment (leapfrog path).  Only for callbacks that read the
+ * snapshot and do not call back into this workspace; a stop request still leaves psi, t and
+ * step at the save point.  No counterpart in the reference. */
+sbec_status sbec_set_snapshot_mode(sbec_ws* ws, int32_t pipelined);
 /* Autotuner decisions of a workspace / batch (FFT line-kernel variant per call shape, with
  * the measured time of every variant), as text; *len receives the full length.  No
  * counterpart in the reference (FFTW plans are chosen inside FFTW). */
