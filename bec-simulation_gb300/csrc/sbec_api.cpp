@@ -223,8 +223,7 @@ void run_leapfrog_pipelined(sbec_ws* ws, int64_t n_steps, int64_t save_every, sb
       fail(SBEC_ERR_CALLBACK, "callback requested stop");
     }
   };
-  check_cb(snapshot(ws, cb, user));
-  e.lf_open(dt);
+  e.lf_open(dt);  // the caller has delivered the step-0 snapshot
   int64_t step = 0;
   int pending = -1, k = 0;
   while (step < n_steps) {
@@ -716,8 +715,9 @@ sbec_status sbec_ground_state(sbec_ws* ws, int64_t n_steps, double tol, int64_t 
   int64_t steps = 0;
   for (int64_t step = 1; step <= n_steps; ++step) {
     if (!use_c && step > 10 && step % check_every != 0) {
-      // run up to the next convergence check in one fused block
-      const int64_t nxt = std::min(n_steps, (step / check_every + 1) * check_every) - 1;
+      // run steps step..nxt in one fused block: up to the step before the next
+      // convergence check, or to n_steps when no check remains
+      const int64_t nxt = std::min(n_steps, (step / check_every + 1) * check_every - 1);
       split_steps(ws, nxt - step + 1);
       step = nxt;
       steps = step;

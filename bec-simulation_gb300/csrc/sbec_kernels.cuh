@@ -787,7 +787,9 @@ enum RowFlags {
   RP_FWD_X = 8,
   RP_KIN_X = 16,
   RP_POT2 = 32,
-  RP_NORM = 64
+  RP_NORM = 64,
+  RP_CORR = 128,  // multiply by corr[solve] on load (batched ITP: actual / predicted scale)
+  RP_MID = 256    // after POT1: norm partial, multiply by pred[solve], POT2 (p2) — before FWD_X
 };
 
 template <typename R>
@@ -807,6 +809,8 @@ struct RowArgs {
   const R* c0s;             // per-solve couplings (null: p1/p2 values)
   const R* c1s;
   int n_slots;              // launch size: active slots (host side)
+  const R* corr;            // RP_CORR
+  const R* pred;            // RP_MID
 };
 
 template <typename R, int D>
@@ -849,26 +853,39 @@ k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
   const int nr = (int)min((int64_t)RPB, a.n_rows - row0);
   R scale = (R)1;
   if (a.flags & RP_SCALE) scale = (R)(1.0 / sqrt(a.norm_total[b] * a.dV));
+  if (a.flags & RP_CORR) scale = a.corr[b];
+  const bool scaled = (a.flags & (RP_SCALE | RP_CORR)) != 0;
   for (int f = tid; f < NL * N; f += blockDim.x) {
     const int line = f / N, x = f % N;
     const int c = line / RPB, r = line % RPB;
     cplx<R> v = mk<R>(0, 0);
     if (r < nr) v = psi[c * a.N + (row0 + r) * N + x];
-    if (a.flags & RP_SCALE) v = v * scale;
+    if (scaled) v = v * scale;
     s[f] = v;
   }
   __syncthreads();
   const int t = tid % TPL, l = tid / TPL;
   const bool fa = l < NL;  // this thread works on an FFT line
   if (a.flags & RP_INV_X) fft_tile<R, N, +1, P>(s, 1, N, l, t, tw, fa);
+  double acc = 0.0;
   if (a.flags & RP_POT1) {
+    const R pred = (a.flags & RP_MID) ? a.pred[b] : (R)1;
     for (int p = tid; p < RPB * N; p += blockDim.x) {
       const int r = p / N, x = p % N;
       if (r >= nr) continue;
       cplx<R> v[D];
 #pragma unroll
       for (int c = 0; c < D; ++c) v[c] = s[(c * RPB + r) * N + x];
-      pot_stage<R, D>(v, a.p1.V[(row0 + r) * N + x], a.p1, st, c0, c1);
+      const R Vp = a.p1.V[(row0 + r) * N + x];
+      pot_stage<R, D>(v, Vp, a.p1, st, c0, c1);
+      if (a.flags & RP_MID) {
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+          acc += (double)v[c].x * v[c].x + (double)v[c].y * v[c].y;
+          v[c] = v[c] * pred;
+        }
+        pot_stage<R, D>(v, Vp, a.p2, st, c0, c1);
+      }
 #pragma unroll
       for (int c = 0; c < D; ++c) s[(c * RPB + r) * N + x] = v[c];
     }
@@ -880,7 +897,6 @@ k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
     __syncthreads();
     fft_tile<R, N, +1, P>(s, 1, N, l, t, tw, fa);
   }
-  double acc = 0.0;
   if (a.flags & (RP_POT2 | RP_NORM)) {
     for (int p = tid; p < RPB * N; p += blockDim.x) {
       const int r = p / N, x = p % N;
@@ -903,7 +919,7 @@ k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
     const int c = line / RPB, r = line % RPB;
     if (r < nr) psi[c * a.N + (row0 + r) * N + x] = s[f];
   }
-  if (a.flags & RP_NORM) {
+  if (a.flags & (RP_NORM | RP_MID)) {
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
     if ((tid & 31) == 0) red[tid >> 5] = acc;
     __syncthreads();
@@ -1307,6 +1323,23 @@ __global__ void k_seg_finish_rows(const double* __restrict__ partials, int bps, 
   double x = 0.0;
   for (int i = 0; i < bps; ++i) x += partials[(size_t)slot * bps + i];
   out[active ? active[slot] : slot] = x;
+}
+
+// Batched ITP with a predicted renormalisation (RP_MID): from the norm partials of
+// each active solve, the actual scale s = 1/sqrt(norm dV), the correction
+// corr = s / pred for the next pass's load, and the next prediction pred = s.
+template <typename R>
+__global__ void k_seg_pred(const double* __restrict__ partials, int bps, int n_slots, const int* __restrict__ active,
+                           double dV, R* __restrict__ corr, R* __restrict__ pred) {
+  pdl_begin();
+  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= n_slots) return;
+  double x = 0.0;
+  for (int i = 0; i < bps; ++i) x += partials[(size_t)slot * bps + i];
+  const int b = active[slot];
+  const double sc = 1.0 / sqrt(x * dV);
+  corr[b] = (R)(sc / (double)pred[b]);
+  pred[b] = (R)sc;
 }
 
 // Per-solve [sum n^2... ] energy terms and component sums: K = D + 4 values

@@ -11,7 +11,8 @@ namespace sbec {
 
 template <typename K>
 inline void line_set_smem(K kernel, size_t bytes) {
-  if (bytes > 48 * 1024)
+  // opt in above 40 KB: dynamic plus the kernels' static shared arrays must fit the limit
+  if (bytes > 40 * 1024)
     cuda_check(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes),
                "cudaFuncSetAttribute");
 }

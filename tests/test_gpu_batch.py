@@ -54,3 +54,31 @@ def test_batch_fp32_energy(gpu):
         ro = O.find_ground_state(grid=og, atom=O.Rb87, interactions=O.InteractionParams(c0, c1),
                                  V=O.harmonic_potential(og, (1.0, 1.0)), psi_init=p0, **kw)
         assert abs(r["energy"] - ro["energy"]) / abs(ro["energy"]) < 1e-6
+
+
+def test_batch_fp32_merged_step_energy(gpu):
+    """SBEC_BATCH_MERGED=1: two passes per ITP step with a predicted renormalisation; the
+    same ground state as the reference order (energy within 1e-6)."""
+    import os
+
+    n, L = (64, 64), (20.0, 20.0)
+    og = O.make_grid(O.GridConfig(n, L))
+    hg = S.make_grid(S.GridConfig(n, L))
+    psis = [O.init_psi(og, 1, st, seed=5) for st in ("polar", "ferromagnetic")]
+    c1s = [-0.5, 0.5]
+    kw = dict(dt=0.005, n_steps=1000, tol=1e-8)
+    old = os.environ.get("SBEC_BATCH_MERGED")
+    os.environ["SBEC_BATCH_MERGED"] = "1"
+    try:
+        res = S.find_ground_states_batched(grid=hg, atom=S.Rb87, interactions=[S.InteractionParams(10.0, c)
+                                                                               for c in c1s],
+                                           psi_inits=psis, potential=S.HarmonicTrap(1.0, 1.0), precision="fp32", **kw)
+    finally:
+        if old is None:
+            os.environ.pop("SBEC_BATCH_MERGED")
+        else:
+            os.environ["SBEC_BATCH_MERGED"] = old
+    for c1, p0, r in zip(c1s, psis, res):
+        ro = O.find_ground_state(grid=og, atom=O.Rb87, interactions=O.InteractionParams(10.0, c1),
+                                 V=O.harmonic_potential(og, (1.0, 1.0)), psi_init=p0, **kw)
+        assert abs(r["energy"] - ro["energy"]) / abs(ro["energy"]) < 1e-6

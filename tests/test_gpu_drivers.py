@@ -166,3 +166,30 @@ def test_multistart_picks_lowest(gpu):
     assert abs(rg["energy"] - ro["energy"]) <= ENERGY_TOL_FP64 * abs(ro["energy"])
     for a, b in zip(rg["all_results"], ro["all_results"]):
         assert abs(a["energy"] - b["energy"]) <= ENERGY_TOL_FP64 * abs(b["energy"])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_ground_state_steps_not_multiple_of_check(gpu, precision):
+    """n_steps = 53 with checks every 5 steps: the last block ends at n_steps (no check)."""
+    og = O.make_grid(O.GridConfig((64,), (20.0,)))
+    hg = S.make_grid(S.GridConfig((64,), (20.0,)))
+    kw = dict(dt=0.005, n_steps=53, tol=1e-14)
+    ro = O.find_ground_state(grid=og, atom=O.Rb87, interactions=O.InteractionParams(10.0, -0.5),
+                             V=O.harmonic_potential(og, (1.0,)), **kw)
+    rg = S.find_ground_state(grid=hg, atom=S.Rb87, interactions=S.InteractionParams(10.0, -0.5),
+                             potential=S.HarmonicTrap(1.0), precision=precision, **kw)
+    assert rg["steps"] == ro["steps"] == 53
+    tol = ENERGY_TOL_FP64 if precision == "fp64" else 1e-6
+    assert abs(rg["energy"] - ro["energy"]) <= tol * abs(ro["energy"])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_long_lines_1d_2048(gpu, precision):
+    """1-D lines of 2048 points: the fused row pass needs more than the default 48 KB of shared memory."""
+    ws_o, ws_g = make_pair((2048,), (40.0,), 1, c0=10.0, c1=0.5, omega=(1.0,), zeeman=(0.0, 0.1), dt=1e-3,
+                           precision=precision, state="polar")
+    for _ in range(20):
+        O.split_step(ws_o)
+    S.split_step(ws_g, 20)
+    tol = PSI_TOL_FP64 if precision == "fp64" else 5e-5
+    assert rel_psi_err(ws_g.psi, ws_o.psi) < tol
