@@ -303,6 +303,38 @@ def log(msg: str) -> None:
     print(f"[bench {time.perf_counter() - _T0:8.1f}s] {msg}", file=sys.stderr, flush=True)
 
 
+# ----------------------------------------------------------------------------- 1-D quickstart
+def bench_quickstart(S, reps: int = 3) -> dict:
+    """The reference's own CPU-runnable case: 1-D spin-1 Rb87 ground state, 64 points, box 20,
+    c0=10, c1=-0.5, trap 1, dt=0.005, up to 5000 steps, tol 1e-10, polar start; solves/s of the
+    plain FP64 and FP32-bulk forms on the GPU and of the CPU restatement (one solve)."""
+    import oracle as O
+
+    out = {"workload": "1D spin-1 64-pt ITP ground state (quickstart), tol 1e-10, up to 5000 steps"}
+    g = S.make_grid(S.GridConfig((64,), (20.0,)))
+    for prec in ("fp64", "fp32"):
+        kw = dict(grid=g, atom=S.Rb87, interactions=S.InteractionParams(10.0, -0.5), potential=S.HarmonicTrap(1.0),
+                  dt=0.005, n_steps=5000, tol=1e-10, initial_state="polar", precision=prec)
+        S.find_ground_state(**kw)["workspace"].close()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            r = S.find_ground_state(**kw)
+            r["workspace"].close()
+        secs = (time.perf_counter() - t0) / reps
+        out[prec] = {"solves_per_s": 1.0 / secs, "seconds": secs, "steps": r["steps"], "energy": r["energy"],
+                     "converged": r["converged"]}
+    og = O.make_grid(O.GridConfig((64,), (20.0,)))
+    t0 = time.perf_counter()
+    ro = O.find_ground_state(grid=og, atom=O.Rb87, interactions=O.InteractionParams(10.0, -0.5),
+                             V=O.harmonic_potential(og, (1.0,)), dt=0.005, n_steps=5000, tol=1e-10)
+    secs = time.perf_counter() - t0
+    out["cpu_port"] = {"solves_per_s": 1.0 / secs, "seconds": secs, "steps": ro["steps"], "energy": ro["energy"],
+                       "kind": "port"}
+    out["fp64_energy_rel_err_vs_oracle"] = abs(out["fp64"]["energy"] - ro["energy"]) / abs(ro["energy"])
+    out["fp32_energy_rel_err_vs_oracle"] = abs(out["fp32"]["energy"] - ro["energy"]) / abs(ro["energy"])
+    return out
+
+
 # ----------------------------------------------------------------------------- serving
 def bench_serving(S, n_requests: int, fp64_probe_steps: int = 20) -> dict:
     """Poisson request stream (seeded, mean 200 req/s) served with continuous batching in the
@@ -553,6 +585,10 @@ def main_gpu(args) -> None:
         plain = {"value": v64, "unit": UNIT, "steps_per_run": p_steps}
 
     log("main workload done")
+    quick = None
+    if not args.no_quickstart:
+        quick = bench_quickstart(S)
+        log("quickstart done")
     batched = None
     if not args.no_batched:
         batched = bench_batched(S)
@@ -581,6 +617,7 @@ def main_gpu(args) -> None:
             "e2e": e2e,
             "autotune": autotune,
             "plain_fp64": plain,
+            "quickstart_1d": quick,
             "batched_ground_states": batched,
             "serving": serving,
             "dipolar_3d_f6": dipolar,
@@ -644,6 +681,8 @@ def only_section(args) -> None:
 
     if args.only == "batched":
         out = bench_batched(S)
+    elif args.only == "quickstart":
+        out = bench_quickstart(S)
     elif args.only == "serving":
         out = bench_serving(S, args.serve_requests)
     else:
@@ -664,9 +703,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-quickstart", action="store_true")
     ap.add_argument("--no-3d", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=24)
-    ap.add_argument("--only", default=None, choices=["batched", "serving", "3d"],
+    ap.add_argument("--only", default=None, choices=["batched", "serving", "3d", "quickstart"],
                     help="run one optional section alone and print its JSON")
     ap.add_argument("--grid-3d", type=int, default=128)
     ap.add_argument("--ncu-case", default=None, help="short run for profiling: 2d256_fp32|2d256_fp64|batch256_fp32|3d_f6_fp32|3d_f6_fp64")
