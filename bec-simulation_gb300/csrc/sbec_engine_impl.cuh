@@ -109,6 +109,7 @@ class Engine final : public EngineBase {
     if (const char* t = std::getenv("SBEC_TUNE")) tune_on_ = std::atoi(t) != 0;
     if (const char* f = std::getenv("SBEC_TUNE_FORCE")) tune_force_ = std::atoi(f);
     if (const char* m = std::getenv("SBEC_BATCH_MERGED")) merged_itp_ = std::atoi(m) != 0;
+    if (const char* t = std::getenv("SBEC_TENSOR_LANES")) tensor_lanes_ = std::atoi(t) != 0;
     const int D = s_.D;
     N_ = s_.N;
     nc_ = N_ * D;
@@ -1560,6 +1561,19 @@ class Engine final : public EngineBase {
 
   template <int D>
   void launch_tensor_d(const TensorArgs<R>& a) {
+    if constexpr (sizeof(R) == 4) {
+      if (tensor_lanes_) {
+        using TL = TensorLanes<D>;
+        const size_t smem = TL::smem_bytes();
+        auto kern = k_tensor_lanes<D>;
+        static const bool once = (set_smem(kern, smem), true);
+        (void)once;
+        pb();
+        kern<<<(unsigned)((N_ + TL::PPB - 1) / TL::PPB), 256, smem, stream_>>>(a);
+        done("tensor", (2.0 * (double)sizeof(cplx<R>) * D + (double)sizeof(R)) * (double)N_);
+        return;
+      }
+    }
     constexpr int T = 64;
     const size_t smem = sizeof(cplx<R>) * T * (D * (D + 1) / 2);
     auto kern = k_tensor<R, D>;
@@ -1657,6 +1671,7 @@ class Engine final : public EngineBase {
   // line-kernel variants in use (see sbec_lines.h); chosen by the autotuner
   int v_row_ = 0, v_str_ = 0, v_x_ = 0;
   bool merged_itp_ = false;  // SBEC_BATCH_MERGED=1: two-pass FP32 batched ITP step (predicted scale)
+  bool tensor_lanes_ = true;  // FP32 tensor step with one lane group per point (SBEC_TENSOR_LANES=0: one thread)
   R* bcorr_ = nullptr;  // merged FP32 batched ITP: per-solve correction, prediction, ones
   R* bpred_ = nullptr;
   R* bones_ = nullptr;

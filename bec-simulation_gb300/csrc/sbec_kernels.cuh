@@ -1054,6 +1054,132 @@ __global__ void __launch_bounds__(64) k_tensor(TensorArgs<R> a) {
   for (int c = 0; c < D; ++c) a.psi[c * a.N + p] = v[c];
 }
 
+// ---------------------------------------------------------------------------
+// FP32 tensor step with one group of L lanes per point (lane c holds component c):
+// the same operator as tensor_point, laid out for occupancy.  One thread per point
+// needs the whole 13-component spinor, h and the series terms in registers (255 and
+// spills for F = 6) and keeps 8 warps per SM resident; here each lane holds one row of
+// h, the upper triangle of h is built cooperatively (entries round-robin over the
+// lanes, lower entries taken as conjugates so h stays exactly Hermitian) and each
+// Horner product broadcasts the vector through a double-buffered shared slot.  After
+// the block-wide staging of G, groups synchronise only among their own lanes.
+// ---------------------------------------------------------------------------
+template <int D>
+struct TensorLanes {
+  static constexpr int L = D <= 8 ? 8 : 16;  // lanes per point
+  static constexpr int PPB = 256 / L;        // points per 256-thread block
+  static constexpr int NJ = 2 * D - 1;
+  static constexpr int G_FLOATS = (NJ * D * D + 3) / 4 * 4;
+  static constexpr size_t smem_bytes() {
+    return sizeof(float) * G_FLOATS + sizeof(float2) * (size_t)PPB * (D * D + 2 * L);
+  }
+};
+
+template <int L>
+__device__ __forceinline__ float group_sum(float x, unsigned mask) {
+#pragma unroll
+  for (int o = L / 2; o > 0; o >>= 1) x += __shfl_xor_sync(mask, x, o);
+  return x;
+}
+
+template <int D, int L>
+__device__ __forceinline__ void diag_lane(float2& v, float Vp, const TensorArgs<float>& a, bool own, int c,
+                                          unsigned mask) {
+  const float n = group_sum<L>(own ? abs2(v) : 0.0f, mask);
+  float Vint = a.c0 * n;
+  if (a.c_lhy != 0.0f) Vint += a.c_lhy * n * sqrtf(n);
+  const float veff = Vp + Vint;
+  if (!own) return;
+  if (a.itp) {
+    v = v * (expf(-veff * a.tau_d) * a.zee[c].x);
+  } else {
+    float sn, cm1;
+    sin_cosm1(veff * a.tau_d, sn, cm1);
+    const float2 z = cmul_comp(v, a.zee[c], a.zee_lo[c]);
+    v = z + z * mk<float>(cm1, -sn);
+  }
+}
+
+template <int D, int L>
+__device__ __forceinline__ void tensor_lane(float2& v, const TensorArgs<float>& a, const float* Gs, float2* Hs,
+                                            float2* Ys, bool own, int c, unsigned mask) {
+  const float nl = group_sum<L>(own ? abs2(v) : 0.0f, mask);
+  if (nl < 1e-20f) return;
+  if (own) Ys[c] = v;
+  __syncwarp(mask);
+  // upper triangle h[i][j] (j >= i) = sum_J G[J][i][j] conj(v[J-i]) v[J-j], entries round-robin
+  for (int e0 = c; e0 < D * (D + 1) / 2; e0 += L) {
+    int i = 0, e = e0;
+    while (e >= D - i) {
+      e -= D - i;
+      ++i;
+    }
+    const int j = i + e;
+    float2 acc = mk<float>(0.0f, 0.0f);
+    for (int J = j; J <= i + D - 1; ++J) acc += Gs[(J * D + i) * D + j] * cmulc(Ys[J - i], Ys[J - j]);
+    Hs[i * D + j] = acc;
+  }
+  __syncwarp(mask);
+  float2 hrow[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) hrow[j] = !own ? mk<float>(0.0f, 0.0f) : (j >= c ? Hs[c * D + j] : conj(Hs[j * D + c]));
+  const double x = a.bound_coef * (double)nl * fabs((double)a.tau);
+  int nsub = 1;
+  if (x > 0.5) nsub = (int)ceil(x / 0.5);
+  const double xs = x / nsub;
+  int K = 0;
+  {
+    double term = 1.0;
+    while (K < 40) {
+      term *= xs / (double)(K + 1);
+      if (term < a.eps) break;
+      ++K;
+    }
+    K = K + 1;
+  }
+  const float dtau = a.tau / (float)nsub;
+  for (int sub = 0; sub < nsub; ++sub) {
+    float2 y = v;
+    for (int k = K; k >= 1; --k) {
+      float2* yb = Ys + (k & 1) * L;
+      if (own) yb[c] = y;
+      __syncwarp(mask);
+      float2 t = mk<float>(0.0f, 0.0f);
+#pragma unroll
+      for (int j = 0; j < D; ++j) t += hrow[j] * yb[j];
+      const float f = dtau / (float)k;
+      y = v + (a.itp ? (-f) * t : mul_mi(f * t));
+    }
+    v = y;
+  }
+  __syncwarp(mask);
+}
+
+template <int D>
+__global__ void __launch_bounds__(256) k_tensor_lanes(TensorArgs<float> a) {
+  using TL = TensorLanes<D>;
+  constexpr int L = TL::L;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* Gs = reinterpret_cast<float*>(smem_raw);
+  float2* Hs = reinterpret_cast<float2*>(Gs + TL::G_FLOATS);
+  float2* Ysb = Hs + TL::PPB * D * D;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < TL::NJ * D * D; i += blockDim.x) Gs[i] = (float)a.G[i];
+  __syncthreads();
+  const int g = tid / L, c = tid % L;
+  const int64_t p = (int64_t)blockIdx.x * TL::PPB + g;
+  if (p >= a.N) return;  // the whole group leaves; only group-local synchronisation follows
+  const unsigned mask = ((L == 32) ? 0xffffffffu : ((1u << L) - 1u)) << ((tid & 31) / L * L);
+  const bool own = c < D;
+  float2 v = own ? a.psi[c * a.N + p] : mk<float>(0.0f, 0.0f);
+  const float Vp = a.V[p];
+  if (a.pre_diag) diag_lane<D, L>(v, Vp, a, own, c, mask);
+  for (int r = 0; r < a.n_apply; ++r)
+    tensor_lane<D, L>(v, a, Gs, Hs + g * D * D, Ysb + g * 2 * L, own, c, mask);
+  if (a.post_diag) diag_lane<D, L>(v, Vp, a, own, c, mask);
+  if (own) a.psi[c * a.N + p] = v;
+}
+
 // Spin density only (src/observables.jl:61-86).
 template <typename R, int D>
 __global__ void __launch_bounds__(256) k_spin_density(const cplx<R>* __restrict__ psi, int64_t N, SpinTabs<R> st,

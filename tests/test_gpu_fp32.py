@@ -46,3 +46,30 @@ def test_fp32_real_time_error_bounded(gpu, case):
     assert rel_psi_err(ws_g.psi, ws_o.psi) < 5e-5
     assert abs(S.total_norm(ws_g) - N0) / N0 < 2e-6
     assert abs(S.total_energy(ws_g) - O.total_energy(ws_o)) / abs(E0) < 1e-5
+
+
+@pytest.mark.parametrize("F,lanes", [(2, "1"), (6, "1"), (6, "0")])
+def test_fp32_tensor_step_kernels(gpu, F, lanes):
+    """The FP32 general-F tensor step: the lane-group kernel (default) and the
+    one-thread-per-point kernel (SBEC_TENSOR_LANES=0) against the FP64 oracle."""
+    import os
+
+    ip = O.interaction_params_from_constraint(c_total=600.0, c1_ratio=1 / 36, F=F,
+                                              c_extra=(0.0, 0.0, 50.0) if F == 6 else (30.0,))
+    old = os.environ.get("SBEC_TENSOR_LANES")
+    os.environ["SBEC_TENSOR_LANES"] = lanes
+    try:
+        ws_o, ws_g = make_pair((16, 16, 16), (12.0, 12.0, 12.0), F, c0=ip.c0, c1=ip.c1, c_extra=ip.c_extra,
+                               omega=(1.0, 1.0, 1.2), dt=1e-3, precision="fp32", state="random", seed=9)
+    finally:
+        if old is None:
+            os.environ.pop("SBEC_TENSOR_LANES")
+        else:
+            os.environ["SBEC_TENSOR_LANES"] = old
+    assert ws_g.tensor_channels()[0]
+    for _ in range(10):
+        O.split_step(ws_o)
+    S.split_step(ws_g, 10)
+    assert rel_psi_err(ws_g.psi, ws_o.psi) < 5e-5
+    assert abs(S.total_energy(ws_g) - O.total_energy(ws_o)) / abs(O.total_energy(ws_o)) < 1e-5
+    ws_g.close()
