@@ -557,9 +557,59 @@ __device__ __forceinline__ void nF_apply(const cplx<R> (&v)[D], R nx, R ny, R nz
   }
 }
 
+// FP32 spin-1 rotation in Cartesian components.  With X = (v_-1 - v_+1, -i(v_+1 + v_-1),
+// sqrt2 v_0) (sqrt2 times the Cartesian spinor), <F> = (Im(X_y* X_z), Im(X_z* X_x),
+// Im(X_x* X_y)) and exp(-i th n·F) rotates Re X and Im X about n:
+// X + sin th (n x X) + (cos th - 1)(X - n (n·X)); in imaginary time
+// exp(-th n·F) X = X - i sinh th (n x X) + (cosh th - 1)(X - n (n·X)).  The m = 0
+// component is kept unscaled (w = v_0, X_z = sqrt2 w) so the rounded sqrt2 only enters
+// the correction terms; a scale in and out would change |v_0| by the same factor every
+// call.  Same operator as the m-basis form below, with about half the arithmetic.
+__device__ __forceinline__ void rodrigues_cart(float2 (&v)[3], float c1, float tau, int itp) {
+  constexpr float s2 = 1.41421356237f, r2 = 0.70710678118f;
+  const float2 Ux = v[2] - v[0];
+  const float2 Uy = mul_mi(v[0] + v[2]);
+  const float2 w = v[1];
+  const float fx = s2 * (Uy.x * w.y - Uy.y * w.x);
+  const float fy = s2 * (w.x * Ux.y - w.y * Ux.x);
+  const float fz = Ux.x * Uy.y - Ux.y * Uy.x;
+  const float f2 = fx * fx + fy * fy + fz * fz;
+  if (!(f2 > 1e-37f)) return;  // |<F>| below ~1e-19 rotates by less than an ulp
+  const float inv = rsqrtf(f2);
+  const float nx = fx * inv, ny = fy * inv, nz = fz * inv;
+  const float th = c1 * (f2 * inv) * tau;
+  const float2 nX = nx * Ux + ny * Uy + (s2 * nz) * w;  // n·X
+  const float2 cx = (s2 * ny) * w - nz * Uy;            // (n x X)_x
+  const float2 cy = nz * Ux - (s2 * nx) * w;            // (n x X)_y
+  const float2 czs = r2 * (nx * Uy - ny * Ux);          // (n x X)_z / sqrt2
+  const float2 px = Ux - nx * nX, py = Uy - ny * nX, pw = w - (r2 * nz) * nX;  // X - n (n·X)
+  float2 X, Y, W;
+  if (itp) {
+    float sh, chm1;
+    sinh_coshm1(th, sh, chm1);
+    X = Ux + mul_mi(sh * cx) + chm1 * px;
+    Y = Uy + mul_mi(sh * cy) + chm1 * py;
+    W = w + mul_mi(sh * czs) + chm1 * pw;
+  } else {
+    float sn, cm1;
+    sin_cosm1(th, sn, cm1);
+    X = Ux + sn * cx + cm1 * px;
+    Y = Uy + sn * cy + cm1 * py;
+    W = w + sn * czs + cm1 * pw;
+  }
+  const float2 iY = mul_i(Y);
+  v[0] = 0.5f * (iY - X);
+  v[1] = W;
+  v[2] = 0.5f * (iY + X);
+}
+
 // Spin-1 Rodrigues rotation exp(-i theta n·F) (src/spin_mixing.jl:71-98).
 template <typename R, int D>
 __device__ __forceinline__ void rodrigues_point(cplx<R> (&v)[D], R c1, R tau, int itp, const SpinTabs<R>& st) {
+  if constexpr (sizeof(R) == 4 && D == 3) {
+    rodrigues_cart(v, c1, tau, itp);
+    return;
+  }
   R fx, fy, fz;
   spin_vector<R, D>(v, st, fx, fy, fz);
   R fm, inv;

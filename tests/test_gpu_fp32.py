@@ -55,7 +55,7 @@ def test_fp32_tensor_step_kernels(gpu, F, lanes):
     import os
 
     ip = O.interaction_params_from_constraint(c_total=600.0, c1_ratio=1 / 36, F=F,
-                                              c_extra=(0.0, 0.0, 50.0) if F == 6 else (30.0,))
+                                              c_extra=(0.0, 0.0, 50.0) if F == 6 else (0.0, 0.0, 20.0))
     old = os.environ.get("SBEC_TENSOR_LANES")
     os.environ["SBEC_TENSOR_LANES"] = lanes
     try:
