@@ -1119,9 +1119,11 @@ struct TensorLanes {
   static constexpr int L = D <= 8 ? 8 : 16;  // lanes per point
   static constexpr int PPB = 256 / L;        // points per 256-thread block
   static constexpr int NJ = 2 * D - 1;
+  static constexpr int NT = D * (D + 1) / 2;  // upper-triangle entries
   static constexpr int G_FLOATS = (NJ * D * D + 3) / 4 * 4;
+  static constexpr int E_INTS = (NT + 3) / 4 * 4;
   static constexpr size_t smem_bytes() {
-    return sizeof(float) * G_FLOATS + sizeof(float2) * (size_t)PPB * (D * D + 2 * L);
+    return sizeof(float) * G_FLOATS + sizeof(int) * E_INTS + sizeof(float2) * (size_t)PPB * (NT + D * D + 2 * L);
   }
 };
 
@@ -1151,22 +1153,36 @@ __device__ __forceinline__ void diag_lane(float2& v, float Vp, const TensorArgs<
 }
 
 template <int D, int L>
-__device__ __forceinline__ void tensor_lane(float2& v, const TensorArgs<float>& a, const float* Gs, float2* Hs,
-                                            float2* Ys, bool own, int c, unsigned mask) {
+__device__ __forceinline__ void tensor_lane(float2& v, const TensorArgs<float>& a, const float* Gs, const int* Ent,
+                                            float2* Ps, float2* Hs, float2* Ys, bool own, int c, unsigned mask) {
+  constexpr int NT = D * (D + 1) / 2;
   const float nl = group_sum<L>(own ? abs2(v) : 0.0f, mask);
   if (nl < 1e-20f) return;
   if (own) Ys[c] = v;
   __syncwarp(mask);
-  // upper triangle h[i][j] (j >= i) = sum_J G[J][i][j] conj(v[J-i]) v[J-j], entries round-robin
-  for (int e0 = c; e0 < D * (D + 1) / 2; e0 += L) {
-    int i = 0, e = e0;
-    while (e >= D - i) {
-      e -= D - i;
-      ++i;
-    }
-    const int j = i + e;
+  // products P[b][a] = conj(v_b) v_a (b <= a), upper-triangle storage, row b from b*D - b(b-1)/2
+  for (int e = c; e < NT; e += L) {
+    const int b = Ent[e] & 0xff, aa = Ent[e] >> 8;
+    Ps[b * D - b * (b - 1) / 2 + (aa - b)] = cmulc(Ys[b], Ys[aa]);
+  }
+  __syncwarp(mask);
+  // h[i][j] (j >= i) = sum_{J=j}^{i+D-1} G[J][i][j] conj(v[J-i]) v[J-j] = sum G conj(P[J-j][J-i]);
+  // entries ordered by diagonal (equal term counts in each round of the lanes)
+  for (int e = c; e < NT; e += L) {
+    const int i = Ent[e] & 0xff, j = Ent[e] >> 8;
     float2 acc = mk<float>(0.0f, 0.0f);
-    for (int J = j; J <= i + D - 1; ++J) acc += Gs[(J * D + i) * D + j] * cmulc(Ys[J - i], Ys[J - j]);
+    int bq = 0;                                   // b = J - j, a = J - i = b + (j - i)
+    int idx = (j - i);                            // index of P[0][j-i]
+    const float* g = Gs + (j * D + i) * D + j;    // G[J][i][j] at J = j
+    for (int J = j; J <= i + D - 1; ++J) {
+      const float2 p = Ps[idx];
+      const float gv = *g;
+      acc.x = fmaf(gv, p.x, acc.x);
+      acc.y = fmaf(-gv, p.y, acc.y);
+      idx += D - bq;
+      ++bq;
+      g += D * D;
+    }
     Hs[i * D + j] = acc;
   }
   __syncwarp(mask);
@@ -1211,10 +1227,21 @@ __global__ void __launch_bounds__(256) k_tensor_lanes(TensorArgs<float> a) {
   constexpr int L = TL::L;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float* Gs = reinterpret_cast<float*>(smem_raw);
-  float2* Hs = reinterpret_cast<float2*>(Gs + TL::G_FLOATS);
+  int* Ent = reinterpret_cast<int*>(Gs + TL::G_FLOATS);
+  float2* Psb = reinterpret_cast<float2*>(Ent + TL::E_INTS);
+  float2* Hs = Psb + TL::PPB * TL::NT;
   float2* Ysb = Hs + TL::PPB * D * D;
   const int tid = threadIdx.x;
   for (int i = tid; i < TL::NJ * D * D; i += blockDim.x) Gs[i] = (float)a.G[i];
+  if (tid < TL::NT) {
+    // entry tid in diagonal order: d = j - i, then i; packed as i | (j << 8)
+    int e = tid, d = 0;
+    while (e >= D - d) {
+      e -= D - d;
+      ++d;
+    }
+    Ent[tid] = e | ((e + d) << 8);
+  }
   __syncthreads();
   const int g = tid / L, c = tid % L;
   const int64_t p = (int64_t)blockIdx.x * TL::PPB + g;
@@ -1225,7 +1252,7 @@ __global__ void __launch_bounds__(256) k_tensor_lanes(TensorArgs<float> a) {
   const float Vp = a.V[p];
   if (a.pre_diag) diag_lane<D, L>(v, Vp, a, own, c, mask);
   for (int r = 0; r < a.n_apply; ++r)
-    tensor_lane<D, L>(v, a, Gs, Hs + g * D * D, Ysb + g * 2 * L, own, c, mask);
+    tensor_lane<D, L>(v, a, Gs, Ent, Psb + g * TL::NT, Hs + g * D * D, Ysb + g * 2 * L, own, c, mask);
   if (a.post_diag) diag_lane<D, L>(v, Vp, a, own, c, mask);
   if (own) a.psi[c * a.N + p] = v;
 }
