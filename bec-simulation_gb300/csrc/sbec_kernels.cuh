@@ -439,6 +439,11 @@ struct PotArgs {
   cplx<R> zee_lo[kMaxD];       // FP32 tails of the Zeeman factors
 };
 
+// Upper bound of the Taylor sub-steps of one exponential (rotation or tensor step):
+// legitimate states need a few; an overflowed state (|phi| or n infinite) gets this
+// many and finishes with a non-finite result instead of looping for 2^31 sub-steps.
+constexpr int kMaxSub = 4096;
+
 // sin x and cos x - 1 in FP32.  For |x| <= 1/2 (the usual case: the phase angles of
 // one split step are small) both come from their Taylor series, summed by Horner's
 // rule in x^2 through the x^9 and x^10 terms (the first omitted term is below 3e-11
@@ -747,7 +752,8 @@ __device__ __forceinline__ void rotate_taylor(cplx<R> (&v)[D], R px, R py, R pz,
   const R pm = sqrt(px * px + py * py + pz * pz);
   if (pm * fabs(tau) < (R)1e-14) return;
   const float bound = (float)(pm * fabs(tau)) * (float)F;
-  const int nsub = bound > 0.5f ? (int)ceilf(bound / 0.5f) : 1;
+  // at most kMaxSub sub-steps: a non-finite state must not turn into an endless loop
+  const int nsub = bound > 0.5f ? (bound < 0.5f * kMaxSub ? (int)ceilf(bound / 0.5f) : kMaxSub) : 1;
   const float xs = bound / (float)nsub;
   int K = 1;
   {
@@ -1043,7 +1049,7 @@ __device__ __forceinline__ void tensor_point(cplx<R> (&v)[D], const TensorArgs<R
   }
   const double x = a.bound_coef * (double)nl * fabs((double)a.tau);
   int nsub = 1;
-  if (x > 0.5) nsub = (int)ceil(x / 0.5);
+  if (x > 0.5) nsub = x < 0.5 * kMaxSub ? (int)ceil(x / 0.5) : kMaxSub;  // bounded for non-finite states
   const double xs = x / nsub;
   // number of terms: smallest K with xs^(K+1)/(K+1)! < eps
   int K = 0;
@@ -1191,7 +1197,7 @@ __device__ __forceinline__ void tensor_lane(float2& v, const TensorArgs<float>& 
   for (int j = 0; j < D; ++j) hrow[j] = !own ? mk<float>(0.0f, 0.0f) : (j >= c ? Hs[c * D + j] : conj(Hs[j * D + c]));
   const double x = a.bound_coef * (double)nl * fabs((double)a.tau);
   int nsub = 1;
-  if (x > 0.5) nsub = (int)ceil(x / 0.5);
+  if (x > 0.5) nsub = x < 0.5 * kMaxSub ? (int)ceil(x / 0.5) : kMaxSub;  // bounded for non-finite states
   const double xs = x / nsub;
   int K = 0;
   {
