@@ -170,6 +170,12 @@ class Engine final : public EngineBase {
 
   ~Engine() override {
     cudaStreamSynchronize(stream_);
+    if (side_) {
+      cudaStreamSynchronize(side_);
+      cudaStreamDestroy(side_);
+      for (auto& ev : copied_ev_)
+        if (ev) cudaEventDestroy(ev);
+    }
     for (auto& kv : graphs_)
       if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
     for (void* p : allocs_) cudaFree(p);
@@ -315,13 +321,76 @@ class Engine final : public EngineBase {
       cuda_check(cudaMallocHost(&snap_psi_[k], sizeof(double) * 2 * nc_), "cudaMallocHost");
       cuda_check(cudaEventCreateWithFlags(&snap_ev_[k], cudaEventDisableTiming), "cudaEventCreate");
     }
+    if (s_.ddi) {  // the dipolar energy shares the step's spin-density fields: stay on the step stream
+      energy_enqueue();
+      snapshot_copy_out(k, psi_[kPsi]);
+      return;
+    }
+    // The step stream only copies psi (device to device); the reductions, the FP64
+    // conversion and the host copies run on a second stream from that copy, so they
+    // overlap the next segment instead of delaying it.
+    if (!side_) {
+      cuda_check(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking), "cudaStreamCreate");
+      for (int i = 0; i < 2; ++i) {
+        cuda_check(cudaEventCreateWithFlags(&copied_ev_[i], cudaEventDisableTiming), "cudaEventCreate");
+        snap_copy_[i] = alloc<cplx<R>>(nc_);
+        if (sizeof(R) != 8) snap_stage_[i] = alloc<double2>(nc_);
+      }
+      side_partials_n_ = partials_n_;
+      side_partials_ = alloc<double>(side_partials_n_);
+      side_results_ = alloc<double>(64);
+      side_scratch_ = alloc<cplx<R>>(nc_);
+    }
+    cuda_check(cudaMemcpyAsync(snap_copy_[k], psi_[kPsi], sizeof(cplx<R>) * nc_, cudaMemcpyDeviceToDevice, stream_),
+               "snapshot copy");
+    cuda_check(cudaEventRecord(copied_ev_[k], stream_), "cudaEventRecord");
+    cuda_check(cudaStreamWaitEvent(side_, copied_ev_[k], 0), "cudaStreamWaitEvent");
+    struct Redirect {  // the energy launches address these members; point them at the side set
+      Engine* e;
+      cplx<R>* psi;
+      cudaStream_t st;
+      double *part, *res;
+      size_t part_n;
+      cplx<R>* scr;
+      double2* stage;
+      Redirect(Engine* en, int slot) : e(en) {
+        psi = e->psi_[kPsi];
+        st = e->stream_;
+        part = e->partials_;
+        part_n = e->partials_n_;
+        res = e->results_;
+        scr = e->scratch_;
+        stage = e->stage_;
+        e->psi_[kPsi] = e->snap_copy_[slot];
+        e->stream_ = e->side_;
+        e->partials_ = e->side_partials_;
+        e->partials_n_ = e->side_partials_n_;
+        e->results_ = e->side_results_;
+        e->scratch_ = e->side_scratch_;
+        if (e->snap_stage_[slot]) e->stage_ = e->snap_stage_[slot];
+      }
+      ~Redirect() {
+        e->psi_[kPsi] = psi;
+        e->stream_ = st;
+        e->partials_ = part;
+        e->partials_n_ = part_n;
+        e->results_ = res;
+        e->scratch_ = scr;
+        e->stage_ = stage;
+      }
+    } redirect(this, k);
     energy_enqueue();
+    snapshot_copy_out(k, psi_[kPsi]);
+  }
+
+  // results_[0..31] and psi (as FP64) of the current stream into pinned slot k, then its event.
+  void snapshot_copy_out(int k, const cplx<R>* src_psi) {
     cuda_check(cudaMemcpyAsync(snap_res_[k], results_, 32 * sizeof(double), cudaMemcpyDeviceToHost, stream_),
                "snapshot sums");
-    const void* src = psi_[kPsi];
+    const void* src = src_psi;
     if (sizeof(R) != 8) {
       pb();
-      k_to_f64<R><<<grid_for(nc_), 256, 0, stream_>>>(psi_[kPsi], stage_, nc_);
+      k_to_f64<R><<<grid_for(nc_), 256, 0, stream_>>>(src_psi, stage_, nc_);
       done("convert", (16.0 + (double)sizeof(cplx<R>)) * nc_);
       src = stage_;
     }
@@ -340,6 +409,7 @@ class Engine final : public EngineBase {
 
   void restore_snapshot(int k) override {
     sync();
+    if (side_) cuda_check(cudaStreamSynchronize(side_), "cudaStreamSynchronize");
     set_psi(snap_psi_[k & 1]);
   }
 
@@ -1675,6 +1745,14 @@ class Engine final : public EngineBase {
   R* bcorr_ = nullptr;  // merged FP32 batched ITP: per-solve correction, prediction, ones
   R* bpred_ = nullptr;
   R* bones_ = nullptr;
+  cudaStream_t side_ = nullptr;  // pipelined snapshots: reductions and copies of the save points
+  cudaEvent_t copied_ev_[2] = {nullptr, nullptr};
+  cplx<R>* snap_copy_[2] = {nullptr, nullptr};
+  double2* snap_stage_[2] = {nullptr, nullptr};
+  double* side_partials_ = nullptr;
+  size_t side_partials_n_ = 0;
+  double* side_results_ = nullptr;
+  cplx<R>* side_scratch_ = nullptr;
   double* snap_res_[2] = {nullptr, nullptr};  // pinned snapshot slots
   double* snap_psi_[2] = {nullptr, nullptr};
   cudaEvent_t snap_ev_[2] = {nullptr, nullptr};
