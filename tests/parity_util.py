@@ -8,7 +8,7 @@ import numpy as np
 import oracle as O
 import spinorbec as S
 
-PSI_TOL_FP64 = 1e-10      # max |Δψ| / max |ψ| (spec parity bar for the plain form)
+PSI_TOL_FP64 = 1e-10      # max |Δψ| / max |ψ| (parity bar of the plain FP64 form)
 ENERGY_TOL_FP64 = 1e-12   # relative energy
 
 
