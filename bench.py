@@ -584,6 +584,21 @@ def main_gpu(args) -> None:
         v64 = dist.world * units_per_run(p_steps) * max(1, args.steps // 2) / (ms64 / 1e3)
         plain = {"value": v64, "unit": UNIT, "steps_per_run": p_steps}
 
+    # ---- error of the FP32-bulk run against the plain FP64 form (itself within 1e-10 of
+    # the oracle in the parity tests) after the full 5000-step run
+    accuracy = None
+    if not args.no_plain:
+        finals = {}
+        for prec in ("fp32", "fp64"):
+            w = make(prec, steps, steps + 1)
+            S.run_simulation(w, keep_psi=False)
+            finals[prec] = (w.psi, S.total_energy(w), S.total_norm(w), S.magnetization(w))
+            w.close()
+        (p32, e32, n32, m32), (p64, e64, n64, m64) = finals["fp32"], finals["fp64"]
+        accuracy = {"steps": steps, "psi_max_rel": float(np.max(np.abs(p32 - p64)) / np.max(np.abs(p64))),
+                    "energy_rel": abs(e32 - e64) / abs(e64), "norm_rel": abs(n32 - n64) / abs(n64),
+                    "magnetization_abs": abs(m32 - m64)}
+
     log("main workload done")
     quick = None
     if not args.no_quickstart:
@@ -617,6 +632,7 @@ def main_gpu(args) -> None:
             "e2e": e2e,
             "autotune": autotune,
             "plain_fp64": plain,
+            "fp32_vs_fp64": accuracy,
             "quickstart_1d": quick,
             "batched_ground_states": batched,
             "serving": serving,
