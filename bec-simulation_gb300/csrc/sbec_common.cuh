@@ -121,13 +121,20 @@ __device__ __forceinline__ R ldg_r(const R* p) {
   return __ldg(p);
 }
 
-// Programmatic dependent launch: let the next kernel in the stream be scheduled
-// now, and wait until the previous grid has completed (and its writes are
-// visible) before touching its outputs.  No-ops when launched without the attribute.
-__device__ __forceinline__ void pdl_begin() {
+// Programmatic dependent launch (both are no-ops for a launch without the attribute).
+// pdl_wait: at kernel start, wait until the previous grid has completed and its
+// writes are visible.  pdl_trigger: late in a kernel, let the next grid start
+// launching (its blocks then wait in pdl_wait); placed before the final stores so the
+// next grid's launch overlaps this grid's tail instead of holding SM slots for the
+// whole of this grid.
+__device__ __forceinline__ void pdl_wait() {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
+  cudaGridDependencySynchronize();
+#endif
+}
+__device__ __forceinline__ void pdl_trigger() {
 #if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
   cudaTriggerProgrammaticLaunchCompletion();
-  cudaGridDependencySynchronize();
 #endif
 }
 

@@ -957,7 +957,7 @@ class Engine final : public EngineBase {
 
   void launch_check(const char* what) { cuda_check(cudaGetLastError(), what); }
 
-  // Launch with programmatic stream serialisation (the kernel calls pdl_begin()).
+  // Launch with programmatic stream serialisation (the kernel waits in pdl_wait()).
   template <typename... KArgs, typename... Args>
   void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, Args... args) {
     cudaLaunchConfig_t cfg = {};
@@ -1737,7 +1737,7 @@ class Engine final : public EngineBase {
   double* bres_ = nullptr;
   int oper_ = 1;
   bool use_graphs_ = true;
-  bool use_pdl_ = false;  // SBEC_PDL=1 enables; measured slower for these short kernels
+  bool use_pdl_ = true;  // programmatic dependent launch (SBEC_PDL=0 disables)
   // line-kernel variants in use (see sbec_lines.h); chosen by the autotuner
   int v_row_ = 0, v_str_ = 0, v_x_ = 0;
   bool merged_itp_ = false;  // SBEC_BATCH_MERGED=1: two-pass FP32 batched ITP step (predicted scale)

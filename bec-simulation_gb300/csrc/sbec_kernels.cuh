@@ -77,7 +77,7 @@ struct PhaseRef {
 template <typename R, int N, int LPB, int P = 0>
 __global__ void __launch_bounds__(LPB * (N / PlanOf<R, N, P>::E))
 k_fft_x(cplx<R>* __restrict__ data, int64_t n_lines, int mode, PhaseRef<R> ph, Tw<R> tw) {
-  pdl_begin();
+  pdl_wait();
   constexpr int TPL = N / PlanOf<R, N, P>::E;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);
@@ -98,6 +98,7 @@ k_fft_x(cplx<R>* __restrict__ data, int64_t n_lines, int mode, PhaseRef<R> ph, T
       fft_tile<R, N, +1, P>(s, 1, N, l, t, tw);
     }
   }
+  pdl_trigger();
   for (int f = tid; f < nl * N; f += blockDim.x) g[f] = s[f];
 }
 
@@ -112,7 +113,7 @@ template <typename R, int N, int W, int P = 0>
 __global__ void __launch_bounds__(W * (N / PlanOf<R, N, P>::E))
 k_fft_strided(cplx<R>* __restrict__ data, int64_t S, int64_t inner, int64_t outer_stride, int n_in,
               int n_out, int mode, PhaseRef<R> ph, Tw<R> tw, const int* __restrict__ omap, int oper) {
-  pdl_begin();
+  pdl_wait();
   constexpr int TPL = N / PlanOf<R, N, P>::E;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);
@@ -163,6 +164,7 @@ k_fft_strided(cplx<R>* __restrict__ data, int64_t S, int64_t inner, int64_t oute
       fft_tile<R, N, +1, P>(s, W, 1, w, t, tw);
     }
   }
+  pdl_trigger();
   for (int f = tid; f < W * N; f += blockDim.x) {
     const int i = f / W, ww = f % W;
     if (i < n_out && ww < nw) g[(int64_t)i * S + ww] = s[f];
@@ -892,7 +894,7 @@ constexpr int row_threads() {
 template <typename R, int N, int D, int RPB, int P = 0>
 __global__ void __launch_bounds__(row_threads<R, N, D, RPB, P>())
 k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
-  pdl_begin();
+  pdl_wait();
   constexpr int TPL = N / PlanOf<R, N, P>::E;
   constexpr int NL = D * RPB;  // line = c*RPB + r
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -970,6 +972,7 @@ k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
     }
     __syncthreads();
   }
+  pdl_trigger();
   for (int f = tid; f < NL * N; f += blockDim.x) {
     const int line = f / N, x = f % N;
     const int c = line / RPB, r = line % RPB;
@@ -1310,7 +1313,7 @@ __device__ __forceinline__ void block_reduce_store(double (&vals)[K], double* pa
 // Sum (or max) K values over nb partial blocks into out[k].
 template <int K>
 __global__ void k_reduce_finish(const double* __restrict__ partials, int nb, int is_max, double* __restrict__ out) {
-  pdl_begin();
+  pdl_wait();
   const int k = threadIdx.x;
   if (k >= K) return;
   double x = is_max ? 0.0 : 0.0;
@@ -1526,7 +1529,7 @@ __global__ void k_seg_finish(const double* __restrict__ partials, int nb, int n_
 template <typename R>
 __global__ void k_seg_finish_rows(const double* __restrict__ partials, int bps, int n_slots,
                                   const int* __restrict__ active, double* __restrict__ out) {
-  pdl_begin();
+  pdl_wait();
   const int slot = blockIdx.x * blockDim.x + threadIdx.x;
   if (slot >= n_slots) return;
   double x = 0.0;
@@ -1540,7 +1543,7 @@ __global__ void k_seg_finish_rows(const double* __restrict__ partials, int bps, 
 template <typename R>
 __global__ void k_seg_pred(const double* __restrict__ partials, int bps, int n_slots, const int* __restrict__ active,
                            double dV, R* __restrict__ corr, R* __restrict__ pred) {
-  pdl_begin();
+  pdl_wait();
   const int slot = blockIdx.x * blockDim.x + threadIdx.x;
   if (slot >= n_slots) return;
   double x = 0.0;
@@ -1651,7 +1654,7 @@ __global__ void k_scale(cplx<R>* a, int64_t n, double s) {
 // psi /= sqrt(sum_c sums[c]*dV) with the sums already on the device (src/split_step.jl:185-195).
 template <typename R>
 __global__ void k_normalize_apply(cplx<R>* a, int64_t N, int D, const double* __restrict__ sums, double dV) {
-  pdl_begin();
+  pdl_wait();
   double ns = 0.0;
   for (int c = 0; c < D; ++c) ns += sums[c] * dV;
   const R s = (R)(1.0 / sqrt(ns));
@@ -1663,7 +1666,7 @@ __global__ void k_normalize_apply(cplx<R>* a, int64_t N, int D, const double* __
 template <typename R>
 __global__ void k_batch_normalize(cplx<R>* a, int64_t per_solve, const int* __restrict__ active, int n_slots,
                                   const double* __restrict__ norm, double dV) {
-  pdl_begin();
+  pdl_wait();
   const int64_t total = per_solve * n_slots;
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
     const int b = active[q / per_solve];
