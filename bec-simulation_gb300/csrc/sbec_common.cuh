@@ -111,6 +111,50 @@ __device__ __forceinline__ cplx<R> tw_mul(cplx<R> x, const Tw<R>& t, int idx, bo
   }
 }
 
+// a + b rounded to FP32 without a systematic bias, for |a| >= |b| (a state value plus
+// a small correction).  The exact sum is s + e (Fast2Sum); s moves one ulp towards e
+// when |e| exceeds a threshold drawn uniformly from [0, ulp) by a hash of the operands'
+// bits (deterministic: equal inputs give equal results), so the expected result is
+// the exact sum.  Needed where an FP32 state is turned by small angles near a
+// coordinate axis: near the real axis the inward shift of the real part (x^2/2 |z|) is
+// below half an ulp and round-to-nearest keeps it outside every time while the
+// imaginary part, near zero, is resolved finely — a slowly turning near-real state (the
+// polar ground state in its trap, or its real spectrum under the kinetic phase) then
+// gains norm at x^2 per rotation.
+__device__ __forceinline__ float sr_add(float a, float b, unsigned salt) {
+  const float s = __fadd_rn(a, b);
+  const float e = __fsub_rn(b, __fsub_rn(s, a));
+  const float up = __int_as_float(__float_as_int(s) + (((e > 0.0f) == (s > 0.0f)) ? 1 : -1));
+  const unsigned h = (__float_as_uint(a) ^ (__float_as_uint(b) * 0x9E3779B9u) ^ salt) >> 8;
+  const float thr = (float)h * (1.0f / 16777216.0f) * fabsf(up - s);
+  return (e != 0.0f && s != 0.0f && fabsf(e) > thr) ? up : s;
+}
+
+// x * w for a kinetic phase table entry.  Real-time FP32 tables hold
+// scale * (cos, sin) as (head, tail) with scale an exact power of two (1/N on the x
+// axis, where the inverse-FFT normalisation is folded in, 1 elsewhere); the product is
+// formed as x scale + x (w - scale): x scale is exact, w - scale comes from the head and
+// tail without cancellation for the small angles of low k, and the final addition is
+// rounded without bias (sr_add) — a near-real spectrum turned by small angles would
+// otherwise gain norm at every step.  Imaginary-time (decay) tables, renormalised every
+// step, and FP64 use the compensated / plain product.
+template <typename R>
+__device__ __forceinline__ cplx<R> phase_mul(cplx<R> x, const Tw<R>& t, int idx, R scale, int unbiased) {
+  if constexpr (sizeof(R) == 4) {
+    const float4 w4 = __ldg(reinterpret_cast<const float4*>(t.hi) + idx);
+    if (!unbiased) return cmul_comp(x, mk<float>(w4.x, w4.y), mk<float>(w4.z, w4.w));
+    const float cm = __fadd_rn(__fsub_rn(w4.x, scale), w4.z);
+    const float sn = __fadd_rn(w4.y, w4.w);
+    const float bx = __fmaf_rn(x.x, cm, __fmul_rn(-x.y, sn));
+    const float by = __fmaf_rn(x.y, cm, __fmul_rn(x.x, sn));
+    return mk<float>(sr_add(__fmul_rn(x.x, scale), bx, 0x85ebca6bu), sr_add(__fmul_rn(x.y, scale), by, 0xc2b2ae35u));
+  } else {
+    (void)scale;
+    (void)unbiased;
+    return x * __ldg(t.hi + idx);
+  }
+}
+
 template <typename R>
 __device__ __forceinline__ cplx<R> ldg(const cplx<R>* p) {
   return __ldg(p);

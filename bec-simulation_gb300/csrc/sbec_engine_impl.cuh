@@ -1127,6 +1127,8 @@ class Engine final : public EngineBase {
       p.tab[a].lo = ptab_lo_[a];
       p.n[a] = s_.n[a];
     }
+    p.scale0 = (R)(1.0 / (double)N_);  // N_ is a power of two: exact
+    p.unbiased = (sizeof(R) == 4 && phase_itp_ == 0) ? 1 : 0;
     return p;
   }
 

@@ -68,7 +68,35 @@ struct PhaseRef {
   Tw<R> tab[3];
   int n[3];
   int ndim;
+  R scale0;      // exact power-of-two scale folded into tab[0] (1/N)
+  int unbiased;  // real-time FP32 tables: phase_mul's unbiased form
 };
+
+// The FP32 real-time kinetic factor of a 2-D / 3-D point: the per-axis factors
+// scale_a (1 + c_a + i s_a) (tables: head and tail; scale 1/N on x, 1 elsewhere, both
+// exact powers of two) are combined as (1 + C + iS) = prod_a (1 + c_a + i s_a) in the
+// small quantities c_a, s_a (full relative precision for low k), and x is turned once:
+// x/N + (x/N)(C + iS) with the addition rounded without bias (sr_add).
+__device__ __forceinline__ float2 kinetic_rot(float2 x, const PhaseRef<float>& ph, int i0, int i1, int ilast) {
+  float C = 0.0f, Sn = 0.0f;
+  auto fold = [&](const Tw<float>& t, int idx, float scale, float inv) {
+    const float4 w4 = __ldg(reinterpret_cast<const float4*>(t.hi) + idx);
+    const float c = __fmul_rn(__fadd_rn(__fsub_rn(w4.x, scale), w4.z), inv);
+    const float sn = __fmul_rn(__fadd_rn(w4.y, w4.w), inv);
+    const float nC = __fadd_rn(__fadd_rn(C, c), __fmaf_rn(C, c, __fmul_rn(-Sn, sn)));
+    const float nS = __fadd_rn(__fadd_rn(Sn, sn), __fmaf_rn(Sn, c, __fmul_rn(C, sn)));
+    C = nC;
+    Sn = nS;
+  };
+  const float inv0 = 1.0f / ph.scale0;  // N: exact
+  fold(ph.tab[0], i0, ph.scale0, inv0);
+  if (ph.ndim == 3) fold(ph.tab[1], i1, 1.0f, 1.0f);
+  fold(ph.tab[ph.ndim - 1], ilast, 1.0f, 1.0f);
+  const float2 xs = mk<float>(__fmul_rn(x.x, ph.scale0), __fmul_rn(x.y, ph.scale0));
+  const float bx = __fmaf_rn(xs.x, C, __fmul_rn(-xs.y, Sn));
+  const float by = __fmaf_rn(xs.y, C, __fmul_rn(xs.x, Sn));
+  return mk<float>(sr_add(xs.x, bx, 0x85ebca6bu), sr_add(xs.y, by, 0xc2b2ae35u));
+}
 
 // ---------------------------------------------------------------------------
 // FFT along x (contiguous lines).  mode 0: forward, 1: inverse,
@@ -93,7 +121,7 @@ k_fft_x(cplx<R>* __restrict__ data, int64_t n_lines, int mode, PhaseRef<R> ph, T
   } else {
     fft_tile<R, N, -1, P>(s, 1, N, l, t, tw);
     if (mode == 2) {
-      for (int f = tid; f < LPB * N; f += blockDim.x) s[f] = tw_mul<R>(s[f], ph.tab[0], f % N, false);
+      for (int f = tid; f < LPB * N; f += blockDim.x) s[f] = phase_mul<R>(s[f], ph.tab[0], f % N, ph.scale0, ph.unbiased);
       __syncthreads();
       fft_tile<R, N, +1, P>(s, 1, N, l, t, tw);
     }
@@ -153,11 +181,14 @@ k_fft_strided(cplx<R>* __restrict__ data, int64_t S, int64_t inner, int64_t oute
         const int i = f / W, ww = f % W;
         if constexpr (sizeof(R) == 8) {
           s[f] = s[f] * (inner_ph[ww] * __ldg(last.hi + i));
+        } else if (ph.unbiased) {
+          // FP32 real time: all axis factors as one rotation, applied with one unbiased rounding
+          s[f] = kinetic_rot(s[f], ph, inner_idx[ww][0], ph.ndim == 3 ? inner_idx[ww][1] : 0, i);
         } else {
-          // FP32: one compensated product per axis factor (unbiased rounding)
-          cplx<R> v = tw_mul<R>(s[f], ph.tab[0], inner_idx[ww][0], false);
-          if (ph.ndim == 3) v = tw_mul<R>(v, ph.tab[1], inner_idx[ww][1], false);
-          s[f] = tw_mul<R>(v, last, i, false);
+          // FP32 imaginary time: one compensated product per axis factor
+          cplx<R> v = phase_mul<R>(s[f], ph.tab[0], inner_idx[ww][0], ph.scale0, 0);
+          if (ph.ndim == 3) v = phase_mul<R>(v, ph.tab[1], inner_idx[ww][1], (R)1, 0);
+          s[f] = phase_mul<R>(v, last, i, (R)1, 0);
         }
       }
       __syncthreads();
@@ -469,6 +500,26 @@ __device__ __forceinline__ void sin_cosm1(float x, float& sn, float& cm1) {
   }
 }
 
+// z (1 + cm1 - i sn) = z + z (cm1 - i sn) for a small FP32 rotation: the whole
+// correction (radial cm1 z and tangential -i sn z) is formed first and added with one
+// rounding.  Left to FMA contraction the radial part is added last, in a rounding of
+// its own, and is dropped whenever it is below half an ulp (|x| below ~2.4e-4, the trap
+// centre) while the tangential part survives; the final addition is rounded without
+// bias (sr_add).  The _rn intrinsics are not contracted.
+__device__ __forceinline__ float2 rot_small(float2 z, float cm1, float sn) {
+  const float bx = __fmaf_rn(z.x, cm1, __fmul_rn(z.y, sn));
+  const float by = __fmaf_rn(z.y, cm1, __fmul_rn(-z.x, sn));
+  return make_float2(sr_add(z.x, bx, 0x9e3779b9u), sr_add(z.y, by, 0x7f4a7c15u));
+}
+
+// u + (a A + b B) with the correction formed in full before the single addition to u
+// (same reason as rot_small; a, b real coefficients, A, B complex).
+__device__ __forceinline__ float2 add_corr(float2 u, float a, float2 A, float b, float2 B) {
+  const float cx = __fmaf_rn(b, B.x, __fmul_rn(a, A.x));
+  const float cy = __fmaf_rn(b, B.y, __fmul_rn(a, A.y));
+  return make_float2(__fadd_rn(u.x, cx), __fadd_rn(u.y, cy));
+}
+
 // sinh x and cosh x - 1 in FP32 (the imaginary-time spin rotation): Taylor series
 // through the x^9 / x^10 terms for |x| <= 1/2, as in sin_cosm1 (cosh x - 1 then keeps
 // full relative precision, where coshf(x) - 1 cancels), otherwise from one expf.
@@ -512,12 +563,8 @@ __device__ __forceinline__ void diag_apply(cplx<R> (&v)[D], R veff, R tau, int i
   } else {
     float sn, cm1;
     sin_cosm1(veff * tau, sn, cm1);
-    const float2 w1 = mk<float>(cm1, -sn);
 #pragma unroll
-    for (int c = 0; c < D; ++c) {
-      const float2 z = cmul_comp(v[c], zee[c], zee_lo[c]);
-      v[c] = z + z * w1;
-    }
+    for (int c = 0; c < D; ++c) v[c] = rot_small(cmul_comp(v[c], zee[c], zee_lo[c]), cm1, sn);
   }
 }
 
@@ -600,9 +647,9 @@ __device__ __forceinline__ void rodrigues_cart(float2 (&v)[3], float c1, float t
   } else {
     float sn, cm1;
     sin_cosm1(th, sn, cm1);
-    X = Ux + sn * cx + cm1 * px;
-    Y = Uy + sn * cy + cm1 * py;
-    W = w + sn * czs + cm1 * pw;
+    X = add_corr(Ux, sn, cx, cm1, px);
+    Y = add_corr(Uy, sn, cy, cm1, py);
+    W = add_corr(w, sn, czs, cm1, pw);
   }
   const float2 iY = mul_i(Y);
   v[0] = 0.5f * (iY - X);
@@ -951,7 +998,7 @@ k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
   }
   if (a.flags & (RP_FWD_X | RP_KIN_X)) fft_tile<R, N, -1, P>(s, 1, N, l, t, tw, fa);
   if (a.flags & RP_KIN_X) {
-    for (int f = tid; f < NL * N; f += blockDim.x) s[f] = tw_mul<R>(s[f], ph.tab[0], f % N, false);
+    for (int f = tid; f < NL * N; f += blockDim.x) s[f] = phase_mul<R>(s[f], ph.tab[0], f % N, ph.scale0, ph.unbiased);
     __syncthreads();
     fft_tile<R, N, +1, P>(s, 1, N, l, t, tw, fa);
   }
@@ -1156,8 +1203,7 @@ __device__ __forceinline__ void diag_lane(float2& v, float Vp, const TensorArgs<
   } else {
     float sn, cm1;
     sin_cosm1(veff * a.tau_d, sn, cm1);
-    const float2 z = cmul_comp(v, a.zee[c], a.zee_lo[c]);
-    v = z + z * mk<float>(cm1, -sn);
+    v = rot_small(cmul_comp(v, a.zee[c], a.zee_lo[c]), cm1, sn);
   }
 }
 
