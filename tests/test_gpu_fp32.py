@@ -73,3 +73,26 @@ def test_fp32_tensor_step_kernels(gpu, F, lanes):
     assert rel_psi_err(ws_g.psi, ws_o.psi) < 5e-5
     assert abs(S.total_energy(ws_g) - O.total_energy(ws_o)) / abs(O.total_energy(ws_o)) < 1e-5
     ws_g.close()
+
+
+def test_fp32_long_leapfrog_norm_from_real_ground_state(gpu):
+    """2000 leapfrog steps from the (real) polar ground state in its trap: FP32 norm within
+    1e-6 of FP64.  Round-to-nearest of small rotations of a near-real state gains norm
+    at ~3.5e-9 per step; the unbiased rounding of the diagonal and kinetic phases
+    leaves a zero-mean error."""
+    n, L = (128, 128), (30.0, 30.0)
+    hg = S.make_grid(S.GridConfig(n, L))
+    gs = S.find_ground_state(grid=hg, atom=S.Na23, interactions=S.InteractionParams(10.0, 0.5),
+                             zeeman=S.ZeemanParams(0.0, 0.1), potential=S.HarmonicTrap(1.0, 1.0), dt=0.005,
+                             n_steps=400, tol=1e-9, initial_state="polar")
+    psi0 = gs["workspace"].psi
+    gs["workspace"].close()
+    norms = {}
+    for prec in ("fp32", "fp64"):
+        ws = S.make_workspace(grid=hg, atom=S.Na23, interactions=S.InteractionParams(10.0, 0.5),
+                              zeeman=S.ZeemanParams(0.0, 0.1), potential=S.HarmonicTrap(1.0, 1.0),
+                              sim_params=S.SimParams(1e-3, 2000, False, None, 2000), psi_init=psi0, precision=prec)
+        S.run_simulation(ws, keep_psi=False)
+        norms[prec] = S.total_norm(ws)
+        ws.close()
+    assert abs(norms["fp32"] - norms["fp64"]) / norms["fp64"] < 1e-6
