@@ -1147,6 +1147,10 @@ class Engine final : public EngineBase {
         case 1: f(std::integral_constant<int, 1>{}); break;
         case 2: f(std::integral_constant<int, 2>{}); break;
         case 3: f(std::integral_constant<int, 3>{}); break;
+        case 4: f(std::integral_constant<int, 4>{}); break;
+        case 5: f(std::integral_constant<int, 5>{}); break;
+        case 6: f(std::integral_constant<int, 6>{}); break;
+        case 7: f(std::integral_constant<int, 7>{}); break;
         default: f(std::integral_constant<int, 0>{}); break;
       }
     }

@@ -147,6 +147,38 @@ __device__ __forceinline__ void fft_stage(cplx<R>* s, int SI, int SL, int l, int
   __syncthreads();
 }
 
+// One Stockham stage from src into a separate buffer dst: the loads of this stage
+// cannot be overwritten by its own stores, so one barrier (after the stores) suffices.
+template <typename R, int N, int E, int RAD, int SIGN>
+__device__ __forceinline__ void fft_stage_pp(const cplx<R>* src, cplx<R>* dst, int SI, int SL, int l, int t, int Ns,
+                                             const Tw<R>& tw, bool act) {
+  constexpr int TPL = N / E;
+  constexpr int NBT = E / RAD;
+  constexpr int STRIDE = N / RAD;
+  if (act) {
+    cplx<R> v[E];
+#pragma unroll
+    for (int b = 0; b < NBT; ++b) {
+      const int j = t + b * TPL;
+#pragma unroll
+      for (int r = 0; r < RAD; ++r) v[b * RAD + r] = src[(j + r * STRIDE) * SI + l * SL];
+    }
+    fft_stage_store<R, N, E, RAD, SIGN>(dst, SI, SL, l, t, Ns, tw, v);
+  }
+  __syncthreads();
+}
+
+// The stages alternating between buffers a and b; returns the buffer holding the result.
+template <typename R, int N, int E, int SIGN, int RAD, int... REST>
+__device__ __forceinline__ cplx<R>* run_stages_pp(cplx<R>* a, cplx<R>* b, int SI, int SL, int l, int t, int Ns,
+                                                  const Tw<R>& tw, bool act) {
+  fft_stage_pp<R, N, E, RAD, SIGN>(a, b, SI, SL, l, t, Ns, tw, act);
+  if constexpr (sizeof...(REST) > 0)
+    return run_stages_pp<R, N, E, SIGN, REST...>(b, a, SI, SL, l, t, Ns * RAD, tw, act);
+  else
+    return b;
+}
+
 template <typename R, int N, int E, int SIGN, int RAD, int... REST>
 __device__ __forceinline__ void run_stages(cplx<R>* s, int SI, int SL, int l, int t, int Ns, const Tw<R>& tw,
                                            bool act) {
@@ -167,6 +199,11 @@ template <int N> struct FftPlan32;
     static __device__ __forceinline__ void run(cplx<R>* s, int SI, int SL, int l, int t,        \
                                                const Tw<R>& tw, bool act) {                      \
       run_stages<R, NN, EE, SIGN, __VA_ARGS__>(s, SI, SL, l, t, 1, tw, act);                     \
+    }                                                                                            \
+    template <typename R, int SIGN>                                                              \
+    static __device__ __forceinline__ cplx<R>* run_pp(cplx<R>* a, cplx<R>* b, int SI, int SL,   \
+                                                      int l, int t, const Tw<R>& tw, bool act) { \
+      return run_stages_pp<R, NN, EE, SIGN, __VA_ARGS__>(a, b, SI, SL, l, t, 1, tw, act);        \
     }                                                                                            \
   };
 SBEC_PLAN(FftPlan, 2, 2, 2)
@@ -235,6 +272,31 @@ template <typename R, int N, int SIGN, int P = 0>
 __device__ __forceinline__ void fft_tile(cplx<R>* s, int SI, int SL, int l, int t, const Tw<R>& tw,
                                          bool act = true) {
   PlanOf<R, N, P>::template run<R, SIGN>(s, SI, SL, l, t, tw, act);
+}
+
+// Ping-pong form: the tile in a, the same-sized buffer b; returns the buffer holding the
+// transform (a or b, by the parity of the stage count).  One barrier per stage.
+template <typename R, int N, int SIGN, int P = 0>
+__device__ __forceinline__ cplx<R>* fft_tile_pp(cplx<R>* a, cplx<R>* b, int SI, int SL, int l, int t, const Tw<R>& tw,
+                                                bool act = true) {
+  return PlanOf<R, N, P>::template run_pp<R, SIGN>(a, b, SI, SL, l, t, tw, act);
+}
+
+// The transform of the tile at cur: in place (PP false, two barriers per stage) or
+// ping-pong through oth (PP true, one barrier per stage).  On return cur points at
+// the result and oth at the other buffer.
+template <typename R, int N, int SIGN, int P, bool PP>
+__device__ __forceinline__ void fft_tile_sel(cplx<R>*& cur, cplx<R>*& oth, int SI, int SL, int l, int t,
+                                             const Tw<R>& tw, bool act = true) {
+  if constexpr (PP) {
+    cplx<R>* r = fft_tile_pp<R, N, SIGN, P>(cur, oth, SI, SL, l, t, tw, act);
+    if (r != cur) {
+      oth = cur;
+      cur = r;
+    }
+  } else {
+    fft_tile<R, N, SIGN, P>(cur, SI, SL, l, t, tw, act);
+  }
 }
 
 }  // namespace sbec

@@ -101,14 +101,16 @@ __device__ __forceinline__ float2 kinetic_rot(float2 x, const PhaseRef<float>& p
 // ---------------------------------------------------------------------------
 // FFT along x (contiguous lines).  mode 0: forward, 1: inverse,
 // 2: forward, x phase (1-D kinetic step), inverse.
+// PP: the stages ping-pong between two tiles of shared memory (one barrier each).
 // ---------------------------------------------------------------------------
-template <typename R, int N, int LPB, int P = 0>
+template <typename R, int N, int LPB, int P = 0, bool PP = false>
 __global__ void __launch_bounds__(LPB * (N / PlanOf<R, N, P>::E))
 k_fft_x(cplx<R>* __restrict__ data, int64_t n_lines, int mode, PhaseRef<R> ph, Tw<R> tw) {
   pdl_wait();
   constexpr int TPL = N / PlanOf<R, N, P>::E;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);
+  cplx<R>* s2 = s + LPB * N;
   const int tid = threadIdx.x;
   const int64_t line0 = (int64_t)blockIdx.x * LPB;
   const int nl = (int)min((int64_t)LPB, n_lines - line0);
@@ -117,13 +119,13 @@ k_fft_x(cplx<R>* __restrict__ data, int64_t n_lines, int mode, PhaseRef<R> ph, T
   __syncthreads();
   const int t = tid % TPL, l = tid / TPL;
   if (mode == 1) {
-    fft_tile<R, N, +1, P>(s, 1, N, l, t, tw);
+    fft_tile_sel<R, N, +1, P, PP>(s, s2, 1, N, l, t, tw);
   } else {
-    fft_tile<R, N, -1, P>(s, 1, N, l, t, tw);
+    fft_tile_sel<R, N, -1, P, PP>(s, s2, 1, N, l, t, tw);
     if (mode == 2) {
       for (int f = tid; f < LPB * N; f += blockDim.x) s[f] = phase_mul<R>(s[f], ph.tab[0], f % N, ph.scale0, ph.unbiased);
       __syncthreads();
-      fft_tile<R, N, +1, P>(s, 1, N, l, t, tw);
+      fft_tile_sel<R, N, +1, P, PP>(s, s2, 1, N, l, t, tw);
     }
   }
   pdl_trigger();
@@ -136,8 +138,9 @@ k_fft_x(cplx<R>* __restrict__ data, int64_t n_lines, int mode, PhaseRef<R> ph, T
 // i < n_out (pruned transforms of the zero-padded DDI grid).
 // mode 0 forward, 1 inverse, 2 forward, x phase, inverse (last axis of the
 // kinetic step; the line's lower-axis coordinates come from i0 + w).
+// PP: the stages ping-pong between two tiles of shared memory (one barrier each).
 // ---------------------------------------------------------------------------
-template <typename R, int N, int W, int P = 0>
+template <typename R, int N, int W, int P = 0, bool PP = false>
 __global__ void __launch_bounds__(W * (N / PlanOf<R, N, P>::E))
 k_fft_strided(cplx<R>* __restrict__ data, int64_t S, int64_t inner, int64_t outer_stride, int n_in,
               int n_out, int mode, PhaseRef<R> ph, Tw<R> tw, const int* __restrict__ omap, int oper) {
@@ -145,6 +148,7 @@ k_fft_strided(cplx<R>* __restrict__ data, int64_t S, int64_t inner, int64_t oute
   constexpr int TPL = N / PlanOf<R, N, P>::E;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);
+  cplx<R>* s2 = s + W * N;
   __shared__ cplx<R> inner_ph[W];
   __shared__ int inner_idx[W][2];
   const int tid = threadIdx.x;
@@ -172,9 +176,9 @@ k_fft_strided(cplx<R>* __restrict__ data, int64_t S, int64_t inner, int64_t oute
   __syncthreads();
   const int w = tid % W, t = tid / W;
   if (mode == 1) {
-    fft_tile<R, N, +1, P>(s, W, 1, w, t, tw);
+    fft_tile_sel<R, N, +1, P, PP>(s, s2, W, 1, w, t, tw);
   } else {
-    fft_tile<R, N, -1, P>(s, W, 1, w, t, tw);
+    fft_tile_sel<R, N, -1, P, PP>(s, s2, W, 1, w, t, tw);
     if (mode == 2) {
       const Tw<R> last = ph.tab[ph.ndim - 1];
       for (int f = tid; f < W * N; f += blockDim.x) {
@@ -192,7 +196,7 @@ k_fft_strided(cplx<R>* __restrict__ data, int64_t S, int64_t inner, int64_t oute
         }
       }
       __syncthreads();
-      fft_tile<R, N, +1, P>(s, W, 1, w, t, tw);
+      fft_tile_sel<R, N, +1, P, PP>(s, s2, W, 1, w, t, tw);
     }
   }
   pdl_trigger();
@@ -938,7 +942,7 @@ constexpr int row_threads() {
   return (t + 31) / 32 * 32;
 }
 
-template <typename R, int N, int D, int RPB, int P = 0>
+template <typename R, int N, int D, int RPB, int P = 0, bool PP = false>
 __global__ void __launch_bounds__(row_threads<R, N, D, RPB, P>())
 k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
   pdl_wait();
@@ -946,6 +950,7 @@ k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
   constexpr int NL = D * RPB;  // line = c*RPB + r
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);
+  cplx<R>* s2 = s + NL * N;  // second tile of the ping-pong stages (PP)
   __shared__ double red[32];
   const int tid = threadIdx.x;
   const int slot = a.active ? (int)(blockIdx.x / a.blocks_per_solve) : 0;
@@ -971,7 +976,7 @@ k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
   __syncthreads();
   const int t = tid % TPL, l = tid / TPL;
   const bool fa = l < NL;  // this thread works on an FFT line
-  if (a.flags & RP_INV_X) fft_tile<R, N, +1, P>(s, 1, N, l, t, tw, fa);
+  if (a.flags & RP_INV_X) fft_tile_sel<R, N, +1, P, PP>(s, s2, 1, N, l, t, tw, fa);
   double acc = 0.0;
   if (a.flags & RP_POT1) {
     const R pred = (a.flags & RP_MID) ? a.pred[b] : (R)1;
@@ -996,11 +1001,11 @@ k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
     }
     __syncthreads();
   }
-  if (a.flags & (RP_FWD_X | RP_KIN_X)) fft_tile<R, N, -1, P>(s, 1, N, l, t, tw, fa);
+  if (a.flags & (RP_FWD_X | RP_KIN_X)) fft_tile_sel<R, N, -1, P, PP>(s, s2, 1, N, l, t, tw, fa);
   if (a.flags & RP_KIN_X) {
     for (int f = tid; f < NL * N; f += blockDim.x) s[f] = phase_mul<R>(s[f], ph.tab[0], f % N, ph.scale0, ph.unbiased);
     __syncthreads();
-    fft_tile<R, N, +1, P>(s, 1, N, l, t, tw, fa);
+    fft_tile_sel<R, N, +1, P, PP>(s, s2, 1, N, l, t, tw, fa);
   }
   if (a.flags & (RP_POT2 | RP_NORM)) {
     for (int p = tid; p < RPB * N; p += blockDim.x) {

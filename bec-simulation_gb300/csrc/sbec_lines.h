@@ -2,11 +2,16 @@
 // variants the autotuner chooses between.  A variant V combines
 //   plan family  V & 1:  0 = the precision's default radix set (FP64 radix-16,
 //                            FP32 radix-4/8), 1 = the other one;
-//   tile scale   V >> 1: 0 = ~64-thread tiles (spread a single small solve over
-//                            all SMs), 1 = wider tiles (x lines / row pass 2x
-//                            the lines per block, strided 4x the columns, i.e.
-//                            64-128 contiguous bytes per row segment).
-// FP32 lines of kMinTunedLine points or more have all four variants, each compiled
+//   tile scale   (V >> 1) & 1: 0 = ~64-thread tiles (spread a single small solve
+//                            over all SMs), 1 = wider tiles (x lines / row pass
+//                            2x the lines per block, strided 4x the columns, i.e.
+//                            64-128 contiguous bytes per row segment);
+//   stages       V >> 2: 0 = in place (two block barriers per Stockham stage),
+//                            1 = ping-pong between two shared tiles (one barrier
+//                            per stage, twice the shared memory; x and strided
+//                            lines fall back to in place above 200 KB, a row pass
+//                            that does not fit is not a candidate).
+// FP32 lines of kMinTunedLine points or more have all eight variants, each compiled
 // in its own translation unit (sbec_lines_f32_v<V>.cu); FP64 and shorter lines
 // have variant 0 only.
 #pragma once
@@ -18,7 +23,7 @@
 
 namespace sbec {
 
-constexpr int kLineVariants = 4;
+constexpr int kLineVariants = 8;
 constexpr int kMinTunedLine = 32;
 
 template <typename R>
@@ -48,7 +53,7 @@ inline int row_rpb_host(bool fp32, int n, int D, int V) {
   V = line_variant(fp32, n, V);
   int r = 64 / (D * line_tpl(fp32, n, V));
   if (r < 1) r = 1;
-  return r << (V >> 1);
+  return r << ((V >> 1) & 1);
 }
 
 inline int row_threads_host(bool fp32, int n, int D, int V) {
@@ -60,7 +65,8 @@ inline int row_threads_host(bool fp32, int n, int D, int V) {
 }
 
 inline size_t row_smem_host(bool fp32, int n, int D, int V) {
-  return (size_t)(fp32 ? 8 : 16) * D * row_rpb_host(fp32, n, D, V) * n;
+  const int pp = (line_variant(fp32, n, V) >> 2) & 1;
+  return (size_t)(fp32 ? 8 : 16) * D * row_rpb_host(fp32, n, D, V) * n << pp;
 }
 
 // A row-pass variant can run: at most 1024 threads and 200 KB of shared memory.

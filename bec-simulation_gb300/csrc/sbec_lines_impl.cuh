@@ -38,8 +38,11 @@ template <typename R, int N, int V>
 constexpr int x_lpb_v() {
   constexpr int tpl = N / PlanOf<R, N, (V & 1)>::E;
   constexpr int lpb = 64 / tpl;
-  return (lpb < 1 ? 1 : lpb) << (V >> 1);
+  return (lpb < 1 ? 1 : lpb) << ((V >> 1) & 1);
 }
+
+// Ping-pong stages for variants with bit 2 set, where the two tiles fit in 200 KB.
+constexpr bool line_pp_v(int V, long tile_bytes) { return ((V >> 2) & 1) && 2 * tile_bytes <= 200 * 1024; }
 
 // Strided tiles: at least 16 contiguous bytes per row segment, ~64 threads at
 // scale 0, 4x the columns at scale 1; capped at 1024 threads and 96 KB.
@@ -49,7 +52,7 @@ constexpr int strided_w_v() {
   constexpr int seg = 16 / (int)sizeof(cplx<R>);
   int w = 64 / tpl;
   if (w < seg) w = seg;
-  w <<= 2 * (V >> 1);
+  w <<= 2 * ((V >> 1) & 1);
   while (w > 1 && (w * tpl > 1024 || (long)w * N * (int)sizeof(cplx<R>) > 96 * 1024)) w /= 2;
   return w;
 }
@@ -58,7 +61,7 @@ template <typename R, int N, int D, int V>
 constexpr int row_rpb_v() {
   constexpr int tpl = N / PlanOf<R, N, (V & 1)>::E;
   constexpr int r = 64 / (D * tpl);
-  return (r < 1 ? 1 : r) << (V >> 1);
+  return (r < 1 ? 1 : r) << ((V >> 1) & 1);
 }
 
 template <typename R, int V>
@@ -69,8 +72,10 @@ struct LineImpl {
   static void fft_x(const LineCtx<R>& c, const Tw<R>& tw, cplx<R>* data, int64_t n_lines, int mode) {
     constexpr int LPB = x_lpb_v<R, NN, V>();
     constexpr int TPL = NN / PlanOf<R, NN, P>::E;
-    const size_t smem = sizeof(cplx<R>) * LPB * NN;
-    auto kern = k_fft_x<R, NN, LPB, P>;
+    constexpr long TILE = (long)sizeof(cplx<R>) * LPB * NN;
+    constexpr bool PP = line_pp_v(V, TILE);
+    const size_t smem = PP ? 2 * TILE : TILE;
+    auto kern = k_fft_x<R, NN, LPB, P, PP>;
     static const bool once = (line_set_smem(kern, smem), true);
     (void)once;
     const int64_t blocks = (n_lines + LPB - 1) / LPB;
@@ -83,8 +88,10 @@ struct LineImpl {
                           int oper) {
     constexpr int W = strided_w_v<R, NN, V>();
     constexpr int TPL = NN / PlanOf<R, NN, P>::E;
-    const size_t smem = sizeof(cplx<R>) * W * NN;
-    auto kern = k_fft_strided<R, NN, W, P>;
+    constexpr long TILE = (long)sizeof(cplx<R>) * W * NN;
+    constexpr bool PP = line_pp_v(V, TILE);
+    const size_t smem = PP ? 2 * TILE : TILE;
+    auto kern = k_fft_strided<R, NN, W, P, PP>;
     static const bool once = (line_set_smem(kern, smem), true);
     (void)once;
     dim3 grid((unsigned)((inner + W - 1) / W), (unsigned)outer);
@@ -96,11 +103,13 @@ struct LineImpl {
   static void row(const LineCtx<R>& c, const Tw<R>& tw, const RowArgs<R>& a, int blocks) {
     constexpr int RPB = row_rpb_v<R, NN, D, V>();
     constexpr int NT = row_threads<R, NN, D, RPB, P>();
-    if constexpr (NT > 1024 || (long)sizeof(cplx<R>) * D * RPB * NN > 200 * 1024) {
+    constexpr long TILE = (long)sizeof(cplx<R>) * D * RPB * NN;
+    constexpr bool PP = ((V >> 2) & 1) != 0;
+    if constexpr (NT > 1024 || (PP ? 2 * TILE : TILE) > 200 * 1024) {
       fail(SBEC_ERR_UNSUPPORTED, "row pass tile too large for this line length");
     } else {
-      const size_t smem = sizeof(cplx<R>) * D * RPB * NN;
-      auto kern = k_row_pass<R, NN, D, RPB, P>;
+      const size_t smem = PP ? 2 * TILE : TILE;
+      auto kern = k_row_pass<R, NN, D, RPB, P, PP>;
       static const bool once = (line_set_smem(kern, smem), true);
       (void)once;
       line_launch(c, kern, dim3((unsigned)blocks), dim3(NT), smem, a, c.st, c.ph, tw);

@@ -1,11 +1,12 @@
 """FFT line-kernel variants and their autotuner.
 
-Every compiled variant (plan family x tile scale) must give the FP32-form result
+Every compiled variant (plan family x tile scale x stage form) must give the FP32-form result
 on its own: each is forced in turn (SBEC_TUNE_FORCE, read when a workspace is
 created) and checked against the FP64 oracle on the fused row/column path, the
 batched ground state and the unfused x-line path (3-D with DDI).  With tuning on,
 the decisions are reported and two workspaces of one shape give identical
-results."""
+results.  The ping-pong stage form (variants 4-7) does the arithmetic of the in-place
+form (variants 0-3) in the same order, so the two give bit-identical states."""
 
 import os
 
@@ -18,7 +19,7 @@ from parity_util import make_pair, rel_psi_err
 
 pytestmark = pytest.mark.gpu
 
-VARIANTS = [0, 1, 2, 3]
+VARIANTS = list(range(8))
 
 
 class _env:
@@ -79,6 +80,19 @@ def test_forced_variant_unfused_3d_ddi(gpu, v):
     assert rel_psi_err(ws_g.psi, ws_o.psi) < 5e-5
     assert abs(S.total_energy(ws_g) - O.total_energy(ws_o)) / abs(O.total_energy(ws_o)) < 1e-5
     ws_g.close()
+
+
+@pytest.mark.parametrize("v", [0, 1, 2, 3])
+def test_ping_pong_stages_bit_identical(gpu, v):
+    psis = []
+    for form in (v, v + 4):
+        with _env(SBEC_TUNE_FORCE=form):
+            ws_g = make_pair((128, 64), (20.0, 20.0), 1, c0=10.0, c1=0.5, omega=(1.0, 1.0), zeeman=(0.0, 0.1),
+                             dt=1e-3, precision="fp32", state="random", seed=5)[1]
+        S.split_step(ws_g, 30)
+        psis.append(ws_g.psi.copy())
+        ws_g.close()
+    assert np.array_equal(psis[0], psis[1])
 
 
 def test_tuning_reports_and_is_shared(gpu):
