@@ -51,22 +51,33 @@ def test_forced_variant_fused_2d(gpu, v):
     ws_g.close()
 
 
-@pytest.mark.parametrize("v", VARIANTS)
-def test_forced_variant_batched_ground_state(gpu, v):
-    n, L = (128, 128), (20.0, 20.0)
-    og = O.make_grid(O.GridConfig(n, L))
-    hg = S.make_grid(S.GridConfig(n, L))
+_GS_N, _GS_L = (128, 128), (20.0, 20.0)
+_GS_C1 = [-0.5, 0.5, 0.2]
+_GS_KW = dict(dt=0.005, n_steps=400, tol=1e-12)
+
+
+@pytest.fixture(scope="module")
+def gs_oracle():
+    """Initial states and oracle ground-state energies, shared by every forced variant."""
+    og = O.make_grid(O.GridConfig(_GS_N, _GS_L))
     psis = [O.init_psi(og, 1, st, seed=3) for st in ("polar", "ferromagnetic", "random")]
-    c1s = [-0.5, 0.5, 0.2]
-    kw = dict(dt=0.005, n_steps=400, tol=1e-12)
+    energies = [O.find_ground_state(grid=og, atom=O.Rb87, interactions=O.InteractionParams(10.0, c1),
+                                    V=O.harmonic_potential(og, (1.0, 1.0)), psi_init=p0, **_GS_KW)["energy"]
+                for c1, p0 in zip(_GS_C1, psis)]
+    return psis, energies
+
+
+@pytest.mark.parametrize("v", VARIANTS)
+def test_forced_variant_batched_ground_state(gpu, gs_oracle, v):
+    psis, energies = gs_oracle
+    hg = S.make_grid(S.GridConfig(_GS_N, _GS_L))
     with _env(SBEC_TUNE_FORCE=v):
         res = S.find_ground_states_batched(grid=hg, atom=S.Rb87, interactions=[S.InteractionParams(10.0, c)
-                                                                               for c in c1s],
-                                           psi_inits=psis, potential=S.HarmonicTrap(1.0, 1.0), precision="fp32", **kw)
-    for c1, p0, r in zip(c1s, psis, res):
-        ro = O.find_ground_state(grid=og, atom=O.Rb87, interactions=O.InteractionParams(10.0, c1),
-                                 V=O.harmonic_potential(og, (1.0, 1.0)), psi_init=p0, **kw)
-        assert abs(r["energy"] - ro["energy"]) / abs(ro["energy"]) < 1e-6
+                                                                               for c in _GS_C1],
+                                           psi_inits=psis, potential=S.HarmonicTrap(1.0, 1.0), precision="fp32",
+                                           **_GS_KW)
+    for e_o, r in zip(energies, res):
+        assert abs(r["energy"] - e_o) / abs(e_o) < 1e-6
 
 
 @pytest.mark.parametrize("v", VARIANTS)
