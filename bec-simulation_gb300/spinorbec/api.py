@@ -275,6 +275,32 @@ def ddi_potential(ws: Workspace, padded: bool = False):
 
 # ---- drivers -------------------------------------------------------------------
 
+class _SnapshotStore:
+    """Host storage for psi snapshots: each snapshot is a view into a 64 MiB block (or one
+    snapshot, if larger).  A block that size is backed by huge pages where the kernel offers
+    them, so filling it faults far fewer pages than one fresh array per save point, and the
+    copy keeps pace with the device's next segment."""
+
+    BLOCK_BYTES = 64 << 20
+
+    def __init__(self, n_points, D: int):
+        self.n_points = tuple(n_points)
+        self.D = D
+        self.n = int(np.prod(self.n_points)) * D          # complex values per snapshot
+        self.per_block = max(1, self.BLOCK_BYTES // (16 * self.n))
+        self.block = None
+        self.used = 0
+
+    def take(self, src_ptr) -> np.ndarray:
+        if self.block is None or self.used == self.per_block:
+            self.block = np.empty(2 * self.n * self.per_block, dtype=np.float64)
+            self.used = 0
+        dst = self.block[2 * self.n * self.used:2 * self.n * (self.used + 1)]
+        self.used += 1
+        dst[:] = np.ctypeslib.as_array(src_ptr, shape=(2 * self.n,))
+        return from_interleaved(dst, self.n_points, self.D)
+
+
 class _Recorder:
     def __init__(self, ws: Workspace, callback, keep_psi: bool, use_count_arg: bool):
         self.ws = ws
@@ -284,6 +310,7 @@ class _Recorder:
         self.first = True
         self.count = 0
         self.err = None
+        store = _SnapshotStore(ws.grid.config.n_points, ws.D) if keep_psi else None
 
         def _cb(user, snap_p):
             try:
@@ -293,9 +320,7 @@ class _Recorder:
                 self.res.norms.append(s.norm)
                 self.res.magnetizations.append(s.magnetization)
                 if self.keep_psi:
-                    n = int(np.prod(ws.grid.config.n_points)) * ws.D
-                    arr = np.ctypeslib.as_array(s.psi, shape=(2 * n,)).copy()
-                    self.res.psi_snapshots.append(from_interleaved(arr, ws.grid.config.n_points, ws.D))
+                    self.res.psi_snapshots.append(store.take(s.psi))
                 if self.first:
                     self.first = False
                 elif self.callback is not None:

@@ -70,3 +70,25 @@ def test_host_layout_roundtrip():
     assert buf[0] == psi[0, 0, 0].real and buf[1] == psi[0, 0, 0].imag
     assert buf[2] == psi[1, 0, 0].real  # x fastest (column-major, src/types.jl:239-244)
     assert np.array_equal(S.from_interleaved(buf, (4, 6), 3), psi)
+
+
+def test_snapshot_store_blocks():
+    """Save-point copies land in disjoint views of shared host blocks, same values and
+    layout as a plain copy, a new block started when one is full."""
+    from spinorbec.api import _SnapshotStore
+    import spinorbec as S
+
+    rng = np.random.default_rng(1)
+    store = _SnapshotStore((4, 6), 3)
+    store.per_block = 2
+    outs, refs = [], []
+    for _ in range(5):
+        src = rng.standard_normal(2 * 4 * 6 * 3)
+        outs.append(store.take(src.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        refs.append(S.from_interleaved(src.copy(), (4, 6), 3))
+        src[:] = 0.0  # the source slot is reused by the next save point
+    for o, r in zip(outs, refs):
+        assert np.array_equal(o, r) and o.flags["F_CONTIGUOUS"]
+    outs[0][...] = 0.0
+    assert np.array_equal(outs[1], refs[1])
+    assert outs[0].base is outs[1].base and outs[2].base is not outs[0].base
