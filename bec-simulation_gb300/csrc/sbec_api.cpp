@@ -248,6 +248,7 @@ void run_leapfrog_pipelined(sbec_ws* ws, int64_t n_steps, int64_t save_every, sb
     if (step < n_steps) e.lf_open(dt);
   }
   if (pending >= 0) deliver(pending);
+  e.check_segments();
 }
 
 // _normalize_psi_constrained! (src/ground_state.jl:279-320)
@@ -506,6 +507,7 @@ sbec_status sbec_run_simulation(sbec_ws* ws, int64_t n_steps, int64_t save_every
       if (step % save_every == 0) check_cb(snapshot(ws, cb, user));
       if (step < n_steps) e.lf_open(dt);
     }
+    e.check_segments();
   } else {
     const double dt = e.dt;
     e.half_potential(dt / 2, false);

@@ -152,6 +152,7 @@ class EngineBase {
   virtual void lf_open(double dt) = 0;               // V(dt/2), forward x
   virtual void lf_steps(long long n, double dt) = 0;  // n x [K(dt) with merged V(dt)]
   virtual void lf_close(double dt) = 0;              // K(dt), V(dt/2)
+  virtual void check_segments() {}                   // report a failed persistent segment
   virtual void fused_split_steps(long long n, double dt, double kin_dt, bool kin_itp, bool itp,
                                  bool normalize) = 0;
 

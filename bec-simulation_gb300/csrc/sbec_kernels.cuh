@@ -98,6 +98,14 @@ __device__ __forceinline__ float2 kinetic_rot(float2 x, const PhaseRef<float>& p
   return mk<float>(sr_add(xs.x, bx, 0x85ebca6bu), sr_add(xs.y, by, 0xc2b2ae35u));
 }
 
+// A load of line data: plain (may be served by L1), or CG: through L2 only, for data
+// that other blocks of the same launch wrote (the persistent segment kernel).
+template <bool CG, typename T>
+__device__ __forceinline__ T ld_line(const T* p) {
+  if constexpr (CG) return __ldcg(p);
+  else return *p;
+}
+
 // ---------------------------------------------------------------------------
 // FFT along x (contiguous lines).  mode 0: forward, 1: inverse,
 // 2: forward, x phase (1-D kinetic step), inverse.
@@ -140,25 +148,25 @@ k_fft_x(cplx<R>* __restrict__ data, int64_t n_lines, int mode, PhaseRef<R> ph, T
 // kinetic step; the line's lower-axis coordinates come from i0 + w).
 // PP: the stages ping-pong between two tiles of shared memory (one barrier each).
 // ---------------------------------------------------------------------------
-template <typename R, int N, int W, int P = 0, bool PP = false>
-__global__ void __launch_bounds__(W * (N / PlanOf<R, N, P>::E))
-k_fft_strided(cplx<R>* __restrict__ data, int64_t S, int64_t inner, int64_t outer_stride, int n_in,
-              int n_out, int mode, PhaseRef<R> ph, Tw<R> tw, const int* __restrict__ omap, int oper) {
-  pdl_wait();
+// The work of one block: W lines starting at inner index i0 of outer line o.  CG: load
+// the lines through L2 only (the persistent segment kernel reads data other blocks wrote
+// during the same launch).  trig: signal dependent launches before the final stores.
+template <typename R, int N, int W, int P, bool PP, bool CG>
+__device__ __forceinline__ void fft_strided_block(cplx<R>* __restrict__ data, int64_t S, int64_t inner,
+                                                  int64_t outer_stride, int n_in, int n_out, int mode,
+                                                  const PhaseRef<R>& ph, const Tw<R>& tw, int64_t i0, int64_t o,
+                                                  unsigned char* smem_raw, bool trig) {
   constexpr int TPL = N / PlanOf<R, N, P>::E;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);
   cplx<R>* s2 = s + W * N;
   __shared__ cplx<R> inner_ph[W];
   __shared__ int inner_idx[W][2];
   const int tid = threadIdx.x;
-  const int64_t i0 = (int64_t)blockIdx.x * W;
   const int nw = (int)min((int64_t)W, inner - i0);
-  const int64_t o = omap ? (int64_t)omap[blockIdx.y / oper] * oper + blockIdx.y % oper : (int64_t)blockIdx.y;
   cplx<R>* g = data + o * outer_stride + i0;
   for (int f = tid; f < W * N; f += blockDim.x) {
     const int i = f / W, w = f % W;
-    s[f] = (i < n_in && w < nw) ? g[(int64_t)i * S + w] : mk<R>(0, 0);
+    s[f] = (i < n_in && w < nw) ? ld_line<CG>(g + (int64_t)i * S + w) : mk<R>(0, 0);
   }
   if (mode == 2 && tid < W) {
     // lower-axis factors of the kinetic phase for this line
@@ -199,11 +207,22 @@ k_fft_strided(cplx<R>* __restrict__ data, int64_t S, int64_t inner, int64_t oute
       fft_tile_sel<R, N, +1, P, PP>(s, s2, W, 1, w, t, tw);
     }
   }
-  pdl_trigger();
+  if (trig) pdl_trigger();
   for (int f = tid; f < W * N; f += blockDim.x) {
     const int i = f / W, ww = f % W;
     if (i < n_out && ww < nw) g[(int64_t)i * S + ww] = s[f];
   }
+}
+
+template <typename R, int N, int W, int P = 0, bool PP = false>
+__global__ void __launch_bounds__(W * (N / PlanOf<R, N, P>::E))
+k_fft_strided(cplx<R>* __restrict__ data, int64_t S, int64_t inner, int64_t outer_stride, int n_in,
+              int n_out, int mode, PhaseRef<R> ph, Tw<R> tw, const int* __restrict__ omap, int oper) {
+  pdl_wait();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int64_t o = omap ? (int64_t)omap[blockIdx.y / oper] * oper + blockIdx.y % oper : (int64_t)blockIdx.y;
+  fft_strided_block<R, N, W, P, PP, false>(data, S, inner, outer_stride, n_in, n_out, mode, ph, tw,
+                                           (int64_t)blockIdx.x * W, o, smem_raw, true);
 }
 
 // ---------------------------------------------------------------------------
@@ -942,19 +961,18 @@ constexpr int row_threads() {
   return (t + 31) / 32 * 32;
 }
 
-template <typename R, int N, int D, int RPB, int P = 0, bool PP = false>
-__global__ void __launch_bounds__(row_threads<R, N, D, RPB, P>())
-k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
-  pdl_wait();
+// The work of row-pass block blk (CG and trig as in fft_strided_block).
+template <typename R, int N, int D, int RPB, int P, bool PP, bool CG>
+__device__ __forceinline__ void row_pass_block(const RowArgs<R>& a, const SpinTabs<R>& st, const PhaseRef<R>& ph,
+                                               const Tw<R>& tw, int blk, unsigned char* smem_raw, bool trig) {
   constexpr int TPL = N / PlanOf<R, N, P>::E;
   constexpr int NL = D * RPB;  // line = c*RPB + r
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* s = reinterpret_cast<cplx<R>*>(smem_raw);
   cplx<R>* s2 = s + NL * N;  // second tile of the ping-pong stages (PP)
   __shared__ double red[32];
   const int tid = threadIdx.x;
-  const int slot = a.active ? (int)(blockIdx.x / a.blocks_per_solve) : 0;
-  const int lblk = a.active ? (int)(blockIdx.x % a.blocks_per_solve) : (int)blockIdx.x;
+  const int slot = a.active ? (int)(blk / a.blocks_per_solve) : 0;
+  const int lblk = a.active ? (int)(blk % a.blocks_per_solve) : blk;
   const int b = a.active ? a.active[slot] : 0;
   cplx<R>* psi = a.psi + (int64_t)b * a.solve_stride;
   const R c0 = a.c0s ? a.c0s[b] : a.p1.c0;
@@ -969,7 +987,7 @@ k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
     const int line = f / N, x = f % N;
     const int c = line / RPB, r = line % RPB;
     cplx<R> v = mk<R>(0, 0);
-    if (r < nr) v = psi[c * a.N + (row0 + r) * N + x];
+    if (r < nr) v = ld_line<CG>(psi + c * a.N + (row0 + r) * N + x);
     if (scaled) v = v * scale;
     s[f] = v;
   }
@@ -1024,7 +1042,7 @@ k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
     }
     __syncthreads();
   }
-  pdl_trigger();
+  if (trig) pdl_trigger();
   for (int f = tid; f < NL * N; f += blockDim.x) {
     const int line = f / N, x = f % N;
     const int c = line / RPB, r = line % RPB;
@@ -1037,8 +1055,112 @@ k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
     if (tid == 0) {
       double x = 0.0;
       for (int w = 0; w < (int)((blockDim.x + 31) >> 5); ++w) x += red[w];
-      a.partials[blockIdx.x] = x;
+      a.partials[blk] = x;
     }
+  }
+}
+
+template <typename R, int N, int D, int RPB, int P = 0, bool PP = false>
+__global__ void __launch_bounds__(row_threads<R, N, D, RPB, P>())
+k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
+  pdl_wait();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  row_pass_block<R, N, D, RPB, P, PP, false>(a, st, ph, tw, (int)blockIdx.x, smem_raw, true);
+}
+
+// ---------------------------------------------------------------------------
+// Persistent leapfrog segment (src/simulation.jl:49-94, the merged steps between save
+// points) for 2-D grids: one cooperative launch runs n steps, each the kinetic column
+// pass (y FFT, kinetic phase, inverse y FFT) and the row pass (inverse x FFT, full
+// potential step, forward x FFT), separated by grid-wide barriers instead of kernel
+// boundaries.  Every block does the same per-line work as the separate kernels with
+// the same plan, so the state is bit-identical to theirs.
+// ---------------------------------------------------------------------------
+struct GridBarrier {
+  unsigned int count;  // blocks arrived at the current barrier
+  unsigned int gen;    // barriers completed
+  int err;             // 1: a wait ran out (the launch then returns early)
+  int pad;
+};
+
+constexpr unsigned int kBarrierSpinLimit = 1u << 22;  // >= ~0.4 s of polling
+
+// Grid-wide barrier of a cooperative launch (all blocks resident).  Thread 0 of each
+// block arrives with a release fence and waits, polling with a bounded count, for the
+// last arriver to advance the generation; on a timeout (or another block's) it records
+// the error and the block returns false.
+__device__ __forceinline__ bool grid_barrier(GridBarrier* b) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int* gen = &b->gen;
+    volatile int* err = &b->err;
+    int good = *err == 0;
+    if (good) {
+      const unsigned int g = *gen;
+      __threadfence();
+      if (atomicAdd(&b->count, 1u) == gridDim.x - 1) {
+        atomicExch(&b->count, 0u);
+        __threadfence();
+        atomicAdd(&b->gen, 1u);
+      } else {
+        unsigned int spins = 0;
+        while (*gen == g) {
+          if (*err != 0) {
+            good = 0;
+            break;
+          }
+          if (++spins > kBarrierSpinLimit) {
+            atomicExch(&b->err, 1);
+            good = 0;
+            break;
+          }
+          __nanosleep(100);
+        }
+      }
+      __threadfence();
+    }
+    ok = good;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// Tile shapes of the segment kernel: the row pass of the default plan, and as many
+// y columns per block as fill the same thread count.
+template <typename R, int NX, int NY, int D, int P>
+struct SegShape {
+  static constexpr int TPLX = NX / PlanOf<R, NX, P>::E;
+  static constexpr int TPLY = NY / PlanOf<R, NY, P>::E;
+  static constexpr int RPB = (64 / (D * TPLX)) < 1 ? 1 : 64 / (D * TPLX);
+  static constexpr int T = row_threads<R, NX, D, RPB, P>();
+  static constexpr int W = T / TPLY;
+  static_assert(W * TPLY == T, "segment tiles need T divisible by the y line's threads");
+  static constexpr int TILE = (D * RPB * NX > W * NY) ? D * RPB * NX : W * NY;
+  static constexpr size_t smem_bytes = 2 * (size_t)TILE * sizeof(cplx<R>);  // ping-pong stages
+};
+
+template <typename R, int NX, int NY, int D, int P>
+__global__ void __launch_bounds__(SegShape<R, NX, NY, D, P>::T)
+k_lf_segment(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> twx, Tw<R> twy, long long n_steps,
+             GridBarrier* bar) {
+  using Sh = SegShape<R, NX, NY, D, P>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int row_units = (int)((a.n_rows + Sh::RPB - 1) / Sh::RPB);
+  constexpr int col_per = (NX + Sh::W - 1) / Sh::W;  // column tiles per component
+  const int col_units = col_per * D;
+  for (long long step = 0; step < n_steps; ++step) {
+    for (int u = blockIdx.x; u < col_units; u += gridDim.x) {
+      fft_strided_block<R, NY, Sh::W, P, true, true>(a.psi, NX, NX, a.N, NY, NY, 2, ph, twy,
+                                                     (int64_t)(u % col_per) * Sh::W, u / col_per, smem_raw, false);
+      __syncthreads();
+    }
+    if (!grid_barrier(bar)) return;
+    for (int u = blockIdx.x; u < row_units; u += gridDim.x) {
+      row_pass_block<R, NX, D, Sh::RPB, P, true, true>(a, st, ph, twx, u, smem_raw, false);
+      __syncthreads();
+    }
+    if (step + 1 < n_steps && !grid_barrier(bar)) return;
   }
 }
 

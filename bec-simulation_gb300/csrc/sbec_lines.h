@@ -43,6 +43,13 @@ struct LineKernels {
   static void row(const LineCtx<R>& c, const Tw<R>& tw, int n, int D, const RowArgs<R>& a, int blocks);
 };
 
+// Persistent 2-D leapfrog segments (sbec_segment_f32.cu, kernel k_lf_segment): FP32,
+// square grids of 64-512 points per side, D in {1, 3}.  One cooperative launch runs
+// n_steps merged leapfrog steps of the default plan.
+bool lf_segment_supported(bool fp32, int nx, int ny, int D);
+void lf_segment_launch(const LineCtx<float>& c, const Tw<float>& twx, const Tw<float>& twy, const RowArgs<float>& a,
+                       int n, int D, long long n_steps, GridBarrier* bar);
+
 // The variant actually compiled for a line of n points.
 inline int line_variant(bool fp32, int n, int V) { return (fp32 && n >= kMinTunedLine) ? V : 0; }
 
