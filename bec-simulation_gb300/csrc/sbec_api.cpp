@@ -88,7 +88,8 @@ void kinetic(sbec_ws* ws, double dt, bool itp) {
 }
 
 // split_step! x n through the fused row passes when the workspace allows it
-// (no DDI / tensor, renormalisation every step or never); else operator by operator.
+// (no DDI / tensor, renormalisation every step or never); else operator by operator,
+// replayed from graph chunks when renormalisation is every step or never.
 void split_steps(sbec_ws* ws, long long n);
 
 // split_step! (src/split_step.jl:10-35)
@@ -111,6 +112,14 @@ void split_steps(sbec_ws* ws, long long n) {
   const bool no_norm = !it || e.normalize_every <= 0;
   if (n > 0 && e.fused_path() && (norm_each || no_norm)) {
     e.fused_split_steps(n, e.dt, ws->kin_dt, ws->kin_itp, it, norm_each);
+    for (long long i = 0; i < n; ++i) {
+      e.t += it ? 0.0 : e.dt;
+      e.step += 1;
+    }
+    return;
+  }
+  if (n > 1 && (norm_each || no_norm)) {
+    e.unfused_split_steps(n, e.dt, ws->kin_dt, ws->kin_itp, it, norm_each);
     for (long long i = 0; i < n; ++i) {
       e.t += it ? 0.0 : e.dt;
       e.step += 1;
@@ -509,18 +518,24 @@ sbec_status sbec_run_simulation(sbec_ws* ws, int64_t n_steps, int64_t save_every
     }
     e.check_segments();
   } else {
+    // the same leapfrog on the general path: V(dt/2), then per save segment
+    // (n-1) x [K, V(dt)] from graph chunks, K, V(dt/2), the save point, V(dt/2)
     const double dt = e.dt;
     e.half_potential(dt / 2, false);
-    for (int64_t step = 1; step <= n_steps; ++step) {
+    int64_t step = 0;
+    while (step < n_steps) {
+      const int64_t seg_end = std::min(n_steps, (step / save_every + 1) * save_every);
+      const int64_t nseg = seg_end - step;
+      e.unfused_lf_steps(nseg - 1, dt, ws->kin_dt, ws->kin_itp);
       e.kinetic(ws->kin_dt, ws->kin_itp);
-      const bool is_save = step % save_every == 0;
-      const bool is_last = step == n_steps;
-      const bool need_split = is_save || is_last;
-      e.half_potential(need_split ? dt / 2 : dt, false);
-      e.t += dt;
-      e.step += 1;
-      if (is_save) check_cb(snapshot(ws, cb, user));
-      if (need_split && !is_last) e.half_potential(dt / 2, false);
+      e.half_potential(dt / 2, false);
+      for (int64_t i = 0; i < nseg; ++i) {
+        e.t += dt;
+        e.step += 1;
+      }
+      step = seg_end;
+      if (step % save_every == 0) check_cb(snapshot(ws, cb, user));
+      if (step < n_steps) e.half_potential(dt / 2, false);
     }
   }
   e.sync();
@@ -969,6 +984,13 @@ sbec_status sbec_set_snapshot_mode(sbec_ws* ws, int32_t pipelined) {
   SBEC_API_BEGIN
   need(ws, "workspace");
   ws->pipelined_snapshots = pipelined != 0;
+  SBEC_API_END
+}
+
+sbec_status sbec_set_graph_mode(sbec_ws* ws, int32_t graphs) {
+  SBEC_API_BEGIN
+  need(ws, "workspace");
+  ws->eng->set_graphs(graphs != 0);
   SBEC_API_END
 }
 

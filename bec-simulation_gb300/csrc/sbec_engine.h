@@ -153,8 +153,14 @@ class EngineBase {
   virtual void lf_steps(long long n, double dt) = 0;  // n x [K(dt) with merged V(dt)]
   virtual void lf_close(double dt) = 0;              // K(dt), V(dt/2)
   virtual void check_segments() {}                   // report a failed persistent segment
+  virtual void set_graphs(bool on) = 0;               // sbec_set_graph_mode
   virtual void fused_split_steps(long long n, double dt, double kin_dt, bool kin_itp, bool itp,
                                  bool normalize) = 0;
+  // The same operator sequences on the general path (DDI, tensor, any D), replayed from
+  // CUDA graphs of a few steps: n x split_step! and n x [K(kin_dt), V(dt)].
+  virtual void unfused_split_steps(long long n, double dt, double kin_dt, bool kin_itp, bool itp,
+                                   bool normalize) = 0;
+  virtual void unfused_lf_steps(long long n, double dt, double kin_dt, bool kin_itp) = 0;
 
   // Batches of independent solves sharing grid, F, V, dt and Zeeman (per-solve c0, c1, psi).
   virtual int n_solves() const = 0;

@@ -677,6 +677,43 @@ class Engine final : public EngineBase {
     graph_end(key);
   }
 
+  // ---- the general path in graph chunks of kGraphChunk steps (the last chunk shorter);
+  // the kinetic tables are made current before a replay, since a replay does not
+  // rebuild them.
+  static constexpr long long kGraphChunk = 16;
+
+  template <typename Body>
+  void graph_chunks(int kind, long long n, double dtv, double kin_dt, bool kin_itp, int flags, Body&& body) {
+    update_phase(kin_dt, kin_itp);
+    for (long long done_steps = 0; done_steps < n;) {
+      const long long m = std::min(kGraphChunk, n - done_steps);
+      const GraphKey key{kind, m, dtv, kin_dt, zeeman_p, zeeman_q, flags};
+      if (!graph_replay(key)) {
+        graph_begin(key);
+        for (long long i = 0; i < m; ++i) body();
+        graph_end(key);
+      }
+      done_steps += m;
+    }
+  }
+
+  void unfused_split_steps(long long n, double dtv, double kin_dt, bool kin_itp, bool it, bool normalize) override {
+    const int flags = (kin_itp ? 1 : 0) | (it ? 2 : 0) | (normalize ? 4 : 0);
+    graph_chunks(5, n, dtv, kin_dt, kin_itp, flags, [&] {
+      half_potential(dtv / 2, it);
+      kinetic(kin_dt, kin_itp);
+      half_potential(dtv / 2, it);
+      if (normalize) this->normalize();
+    });
+  }
+
+  void unfused_lf_steps(long long n, double dtv, double kin_dt, bool kin_itp) override {
+    graph_chunks(6, n, dtv, kin_dt, kin_itp, kin_itp ? 1 : 0, [&] {
+      kinetic(kin_dt, kin_itp);
+      half_potential(dtv, false);
+    });
+  }
+
   // ---- CUDA graphs of repeated step blocks.  A block runs eagerly the first
   // time a key is seen (creating lazily built tables), is captured on the
   // second and replayed from then on; profiling runs stay eager so every
@@ -695,6 +732,8 @@ class Engine final : public EngineBase {
     cudaGraphExec_t exec = nullptr;
     long long launches = 0;
   };
+
+  void set_graphs(bool on) override { use_graphs_ = on; }
 
   bool graph_replay(const GraphKey& k) {
     if (prof.enabled() || !use_graphs_) return false;

@@ -151,6 +151,7 @@ _PROTOS = {
     "sbec_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "sbec_ws_stream": (C.c_int, [_P, C.POINTER(C.c_void_p)]),
     "sbec_set_snapshot_mode": (C.c_int, [_P, C.c_int32]),
+    "sbec_set_graph_mode": (C.c_int, [_P, C.c_int32]),
     "sbec_tuning_report": (C.c_int, [_P, C.c_char_p, C.c_int64, C.POINTER(C.c_int64)]),
     "sbec_batch_tuning_report": (C.c_int, [_P, C.c_char_p, C.c_int64, C.POINTER(C.c_int64)]),
     "sbec_batch_create": (C.c_int, [C.POINTER(sbec_config), C.c_int32, _D, _D, _D, _D, C.POINTER(_P)]),

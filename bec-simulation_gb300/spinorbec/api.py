@@ -124,6 +124,11 @@ class Workspace:
         """Autotuner decisions (line-kernel variant per call shape, with every variant's time)."""
         return _report(self._lib.sbec_tuning_report, self.handle)
 
+    def set_graph_mode(self, graphs: bool) -> None:
+        """Replay repeated step blocks from CUDA graphs (default) or launch every kernel
+        eagerly (sbec_set_graph_mode); same kernels, same results."""
+        check(self._lib.sbec_set_graph_mode(self.handle, 1 if graphs else 0))
+
     @property
     def stream_ptr(self) -> int:
         p = C.c_void_p()
@@ -142,8 +147,9 @@ class Workspace:
 def make_workspace(*, grid: Grid, atom: AtomSpecies, interactions: InteractionParams, zeeman=None, potential=None,
                    sim_params: SimParams, psi_init: Optional[np.ndarray] = None, enable_ddi: bool = False,
                    c_dd: float = float("nan"), secular_ddi: bool = False, ddi_padding: bool = False,
-                   gS: Optional[dict] = None, precision: str = "fp64") -> Workspace:
-    """``make_workspace`` (src/initialization.jl:86-191) with a device-resident state."""
+                   gS: Optional[dict] = None, precision: str = "fp64", graphs: bool = True) -> Workspace:
+    """``make_workspace`` (src/initialization.jl:86-191) with a device-resident state.
+    graphs=False: the workspace launches every kernel eagerly (see Workspace.set_graph_mode)."""
     lib = load()
     zeeman = ZeemanParams() if zeeman is None else zeeman
     if callable(zeeman):
@@ -190,7 +196,10 @@ def make_workspace(*, grid: Grid, atom: AtomSpecies, interactions: InteractionPa
     V = np.ascontiguousarray(evaluate_potential(potential, grid).ravel(order="F"))
     h = C.c_void_p()
     check(lib.sbec_ws_create(C.byref(cfg), dptr(pbuf), dptr(V), C.byref(h)))
-    return Workspace(h, grid, F, sim_params, precision, zeeman)
+    ws = Workspace(h, grid, F, sim_params, precision, zeeman)
+    if not graphs:
+        ws.set_graph_mode(False)
+    return ws
 
 
 # ---- operators ---------------------------------------------------------------
@@ -426,8 +435,8 @@ def find_ground_state(*, grid: Grid, atom: AtomSpecies, interactions: Interactio
                       initial_state: str = "polar", psi_init=None, enable_ddi: bool = False,
                       c_dd: float = float("nan"), secular_ddi: bool = False, adaptive_dt: bool = False,
                       dt_max: Optional[float] = None, target_magnetization: Optional[float] = None,
-                      precision: str = "fp64") -> dict:
-    """``find_ground_state`` (src/ground_state.jl:80-237)."""
+                      precision: str = "fp64", graphs: bool = True) -> dict:
+    """``find_ground_state`` (src/ground_state.jl:80-237).  graphs as in make_workspace."""
     zeeman = ZeemanParams() if zeeman is None else zeeman
     psi0 = init_psi(grid, atom.F, initial_state) if psi_init is None else np.array(psi_init, order="F", copy=True)
     eff_cdd = c_dd if (enable_ddi and not math.isnan(c_dd)) else 0.0
@@ -435,12 +444,12 @@ def find_ground_state(*, grid: Grid, atom: AtomSpecies, interactions: Interactio
     if adaptive_dt:
         return _find_ground_state_adaptive(grid, atom, interactions, zeeman, potential, dt, n_steps, tol, psi0,
                                            enable_ddi, c_dd, secular_ddi, 10.0 * dt if dt_max is None else dt_max,
-                                           precision)
+                                           precision, graphs)
     use_c = target_magnetization is not None
     sp = SimParams(dt, n_steps, True, 0 if use_c else 1, max(1, n_steps // 10))
     ws = make_workspace(grid=grid, atom=atom, interactions=interactions, zeeman=zeeman, potential=potential,
                         sim_params=sp, psi_init=psi0, enable_ddi=enable_ddi, c_dd=c_dd, secular_ddi=secular_ddi,
-                        precision=precision)
+                        precision=precision, graphs=graphs)
     r = _lib.sbec_gs_result()
     check(ws._lib.sbec_ground_state(ws.handle, n_steps, float(tol), sp.save_every,
                                     float(target_magnetization) if use_c else float("nan"), C.byref(r)))
@@ -448,14 +457,14 @@ def find_ground_state(*, grid: Grid, atom: AtomSpecies, interactions: Interactio
 
 
 def _find_ground_state_adaptive(grid, atom, interactions, zeeman, potential, dt, n_steps, tol, psi0, enable_ddi,
-                                c_dd, secular_ddi, dt_max, precision):
+                                c_dd, secular_ddi, dt_max, precision, graphs=True):
     """``_find_ground_state_adaptive`` (src/ground_state.jl:172-237): host loop over device blocks."""
     current_dt = dt
     check_every = max(1, n_steps // 100)
     sp = SimParams(current_dt, check_every, True, 1, check_every)
     ws = make_workspace(grid=grid, atom=atom, interactions=interactions, zeeman=zeeman, potential=potential,
                         sim_params=sp, psi_init=psi0, enable_ddi=enable_ddi, c_dd=c_dd, secular_ddi=secular_ddi,
-                        precision=precision)
+                        precision=precision, graphs=graphs)
     E_prev = total_energy(ws)
     converged = False
     total = 0

@@ -11,6 +11,11 @@ is in flight.
 
 Per request the server records queueing, service and end-to-end latency; run()
 returns them with throughput and p50/p99.
+
+Request workspaces launch their kernels eagerly (graphs off): each lives for one short
+solve, and capturing and instantiating CUDA graphs in two dozen concurrent workspaces
+cost more than the replays saved (24-request stream: 8.9 solves/s eager against
+4.9-6.6 with graphs).
 """
 
 from __future__ import annotations
@@ -102,7 +107,7 @@ def run_request(req: SolveRequest) -> dict:
         r = api.find_ground_state(grid=grid, atom=atom, interactions=inter, potential=trap, dt=req.dt,
                                   n_steps=req.steps, tol=req.tol, initial_state="polar",
                                   enable_ddi=req.enable_ddi, c_dd=req.c_dd if req.enable_ddi else float("nan"),
-                                  precision=req.precision)
+                                  precision=req.precision, graphs=False)
         ws = r["workspace"]
         out = dict(energy=r["energy"], norm=api.total_norm(ws), converged=r["converged"], steps=r["steps"])
         ws.close()
@@ -111,7 +116,7 @@ def run_request(req: SolveRequest) -> dict:
     ws = api.make_workspace(grid=grid, atom=atom, interactions=inter, potential=trap,
                             zeeman=ZeemanParams(0.0, 0.1),
                             sim_params=SimParams(req.dt, req.steps, False, None, req.steps), psi_init=psi,
-                            enable_ddi=req.enable_ddi, c_dd=req.c_dd, precision=req.precision)
+                            enable_ddi=req.enable_ddi, c_dd=req.c_dd, precision=req.precision, graphs=False)
     res = api.run_simulation(ws, keep_psi=False)
     out = dict(energy=res.energies[-1], norm=res.norms[-1], converged=None, steps=req.steps)
     ws.close()

@@ -225,6 +225,11 @@ sbec_status sbec_ws_stream(sbec_ws* ws, void** stream);
  * snapshot and do not call back into this workspace; a stop request still leaves psi, t and
  * step at the save point.  No counterpart in the reference. */
 sbec_status sbec_set_snapshot_mode(sbec_ws* ws, int32_t pipelined);
+/* graphs = 1 (default): repeated step blocks are captured once as CUDA graphs and replayed;
+ * 0: every kernel is launched eagerly.  Same kernels, same results.  Eager suits workspaces
+ * that live for one short solve among many running concurrently (each would capture and
+ * instantiate its own graphs).  No counterpart in the reference. */
+sbec_status sbec_set_graph_mode(sbec_ws* ws, int32_t graphs);
 /* Autotuner decisions of a workspace / batch (FFT line-kernel variant per call shape, with
  * the measured time of every variant), as text; *len receives the full length.  No
  * counterpart in the reference (FFTW plans are chosen inside FFTW). */
