@@ -638,14 +638,37 @@ class Engine final : public EngineBase {
   // split_step! x n (src/split_step.jl:10-35) as row passes; with `normalize` the
   // renormalisation of step k is applied at the start of step k+1 (and flushed at
   // the end), using the |psi|^2 sums the closing pass of step k accumulated.
+  // The steps run as graph chunks of up to kGraphChunk steps (small graphs, captured once
+  // and shared by blocks of any length); a chunk that follows another starts with the
+  // previous step's renormalisation pending (key bit 8), and the last one is flushed
+  // after the chunks, so the operator sequence is that of one uninterrupted loop.
   void fused_split_steps(long long n, double dtv, double kin_dt, bool kin_itp, bool it, bool normalize) override {
     update_phase(kin_dt, kin_itp);
     ensure_row_tuned(dtv, it, false);
     if (n <= 0) return;
-    const GraphKey key{2, n, dtv, kin_dt, zeeman_p, zeeman_q, (kin_itp ? 1 : 0) | (it ? 2 : 0) | (normalize ? 4 : 0)};
-    if (graph_replay(key)) return;
-    graph_begin(key);
+    const int flags = (kin_itp ? 1 : 0) | (it ? 2 : 0) | (normalize ? 4 : 0);
     bool pending = false;
+    for (long long done_steps = 0; done_steps < n;) {
+      const long long m = std::min(kGraphChunk, n - done_steps);
+      const GraphKey key{2, m, dtv, kin_dt, zeeman_p, zeeman_q, flags | (pending ? 8 : 0)};
+      if (!graph_replay(key)) {
+        graph_begin(key);
+        fused_steps_body(m, dtv, it, normalize, pending);
+        graph_end(key);
+      }
+      pending = normalize;
+      done_steps += m;
+    }
+    if (pending) {
+      pb();
+      launch_pdl(k_normalize_apply<R>, dim3(grid_for(nc_)), dim3(256), 0, psi_[kPsi], (int64_t)(N_ * s_.D), 1,
+                 (const double*)(results_ + 40), s_.dV);
+      done("normalize", 2.0 * (double)sizeof(cplx<R>) * nc_);
+    }
+  }
+
+  // n fused split steps; `pending`: the renormalisation of the step before is still to apply.
+  void fused_steps_body(long long n, double dtv, bool it, bool normalize, bool pending) {
     for (long long i = 0; i < n; ++i) {
       if (s_.ndim == 1) {
         RowArgs<R> a = row_args(pending);
@@ -668,13 +691,6 @@ class Engine final : public EngineBase {
       }
       pending = normalize;
     }
-    if (pending) {
-      pb();
-      launch_pdl(k_normalize_apply<R>, dim3(grid_for(nc_)), dim3(256), 0, psi_[kPsi], (int64_t)(N_ * s_.D), 1,
-                 (const double*)(results_ + 40), s_.dV);
-      done("normalize", 2.0 * (double)sizeof(cplx<R>) * nc_);
-    }
-    graph_end(key);
   }
 
   // ---- the general path in graph chunks of kGraphChunk steps (the last chunk shorter);
@@ -728,7 +744,6 @@ class Engine final : public EngineBase {
     }
   };
   struct GraphEntry {
-    int seen = 0;
     cudaGraphExec_t exec = nullptr;
     long long launches = 0;
   };
@@ -744,12 +759,21 @@ class Engine final : public EngineBase {
     return true;
   }
 
+  // At most kMaxGraphs instantiated graphs and kMaxGraphKeys remembered keys per engine:
+  // keys that change every call (a Zeeman field set before each step) run eagerly and stop
+  // being recorded once the table is full.
+  static constexpr size_t kMaxGraphs = 64;
+  static constexpr size_t kMaxGraphKeys = 1024;
+
   void graph_begin(const GraphKey& k) {
     capturing_ = false;
     if (prof.enabled() || !use_graphs_) return;
-    GraphEntry& g = graphs_[k];
-    if (g.seen++ == 0) return;  // first use: eager
-    if (graphs_.size() > 64) return;
+    auto it = graphs_.find(k);
+    if (it == graphs_.end()) {  // first use: eager
+      if (graphs_.size() < kMaxGraphKeys) graphs_.emplace(k, GraphEntry{});
+      return;
+    }
+    if (it->second.exec || n_graphs_ >= kMaxGraphs) return;
     cuda_check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
     capturing_ = true;
     cap_launch0_ = prof.total_launches();
@@ -763,6 +787,7 @@ class Engine final : public EngineBase {
     GraphEntry& g = graphs_[k];
     cuda_check(cudaGraphInstantiate(&g.exec, graph, 0), "cudaGraphInstantiate");
     cudaGraphDestroy(graph);
+    ++n_graphs_;
     g.launches = prof.total_launches() - cap_launch0_;
     prof.add_launches(-g.launches);  // counted again on each replay
     cuda_check(cudaGraphLaunch(g.exec, stream_), "cudaGraphLaunch");
@@ -1820,6 +1845,7 @@ class Engine final : public EngineBase {
   R* phi_per_ = nullptr;
   cplx<R>* spec_[2] = {nullptr, nullptr};
   std::map<GraphKey, GraphEntry> graphs_;
+  size_t n_graphs_ = 0;  // instantiated graphs in graphs_
   const int* omap_ = nullptr;  // outer-index map for batched strided passes (null: identity)
   int nsolve_ = 1, n_active_ = 0, active_version_ = 0;
   cplx<R>* bpsi_ = nullptr;

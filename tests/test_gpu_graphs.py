@@ -1,7 +1,9 @@
-"""The general path (DDI, tensor) in CUDA-graph chunks: split_step! x n and the leapfrog
-segments replay graphs of up to 16 steps.  A replay runs the same kernels with the same
-arguments as the eager launches (SBEC_GRAPHS=0), so the states are bit-identical; the
-leapfrog with save points on the general path is also checked against the oracle."""
+"""Step blocks in CUDA-graph chunks: split_step! x n on the fused path (renormalisation
+carried across chunks) and on the general path (DDI, tensor), and the general path's
+leapfrog segments, replay graphs of up to 16 steps.  A replay runs the same kernels with
+the same arguments as the eager launches (SBEC_GRAPHS=0), so the states are
+bit-identical; the leapfrog with save points on the general path is also checked against
+the oracle."""
 
 import os
 
@@ -32,6 +34,8 @@ class _env:
 
 
 CASES = {
+    "fused_2d_f1": dict(n=(32, 32), L=(16.0, 16.0), F=1, c0=10.0, c1=0.5, omega=(1.0, 1.0)),
+    "fused_1d_f2": dict(n=(64,), L=(16.0,), F=2, c0=20.0, c1=1.0, omega=(1.0,)),
     "ddi_2d_f1": dict(n=(32, 32), L=(16.0, 16.0), F=1, c0=10.0, c1=0.5, omega=(1.0, 1.0), ddi=True, c_dd=3.0),
     "tensor_1d_f2": dict(n=(64,), L=(16.0,), F=2, c0=20.0, c1=1.0, omega=(1.0,), c_extra=(0.0, 0.0, 2.0)),
     "tensor_ddi_2d_f2": dict(n=(16, 16), L=(12.0, 12.0), F=2, c0=20.0, c1=1.0, omega=(1.0, 1.0),
