@@ -258,6 +258,32 @@ def run_batched(S, jobs, precision: str, n_steps: int, tol: float) -> tuple:
     return total, res
 
 
+def batched_row_roofline(tune: dict) -> dict:
+    """HBM roofline of the batched ITP row pass of the largest grid group, from the autotuner's
+    own CUDA-event timing of the variant it chose (median of three launches on the live batch).
+    Algorithmic bytes: read + write of every active solve's psi (3 x n^2 complex FP32) plus V
+    once (all solves share it)."""
+    import re
+    n = max(tune)
+    for line in tune[n]:
+        m = re.match(r"fp32 row flags=\S+ batched D=(\d+) grid=\S+ solves=(\d+) -> (.*) chosen v(\d+)", line)
+        if not m:
+            continue
+        D, solves, times, chosen = int(m.group(1)), int(m.group(2)), m.group(3), m.group(4)
+        us = float(re.search(rf"v{chosen}=([0-9.]+)us", times).group(1))
+        N = n * n
+        nbytes = solves * 2.0 * D * N * 8 + N * 4
+        peaks = measured_peaks()
+        hbm = float(peaks.get("hbm_gbs", 6800.0))
+        achieved = nbytes / (us * 1e-6) / 1e9
+        return {"kernel": f"row_pass (batched ITP, {solves} x {n}^2 spin-1, variant {chosen})", "bound": "hbm",
+                "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm, "us_per_launch": us,
+                "bytes_per_launch": nbytes,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback",
+                "timing": "autotuner CUDA events, median of three launches of the chosen variant"}
+    return None
+
+
 def bench_batched(S, sample: int = 6, n_steps: int = 10000, tol: float = 1e-8) -> dict:
     jobs = batched_workload(S)
     secs32, r32 = run_batched(S, jobs, "fp32", n_steps, tol)
@@ -292,7 +318,8 @@ def bench_batched(S, sample: int = 6, n_steps: int = 10000, tol: float = 1e-8) -
             "fp64_one_at_a_time_solves_per_s": len(jobs) / est64,
             "fp64_sample": f"{sample} solves timed one at a time ({secs64:.2f} s), extrapolated per grid size",
             "speedup_vs_fp64_one_at_a_time": est64 / secs32,
-            "energy_rel_err_fp32_vs_fp64_max": max(errs), "converged": conv, "autotune": tune}
+            "energy_rel_err_fp32_vs_fp64_max": max(errs), "converged": conv,
+            "row_pass_roofline": batched_row_roofline(tune), "autotune": tune}
 
 
 _T0 = time.perf_counter()
