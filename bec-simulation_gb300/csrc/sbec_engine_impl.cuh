@@ -111,6 +111,9 @@ class Engine final : public EngineBase {
     if (const char* m = std::getenv("SBEC_BATCH_MERGED")) merged_itp_ = std::atoi(m) != 0;
     if (const char* t = std::getenv("SBEC_TENSOR_LANES")) tensor_lanes_ = std::atoi(t) != 0;
     if (const char* g = std::getenv("SBEC_SEGMENT")) segment_on_ = std::atoi(g) != 0;
+    // host-side fault injection for the tests: the segment barrier's arrival counter starts
+    // beyond the block count, so no block is ever the last arriver and every wait runs out
+    if (const char* f = std::getenv("SBEC_FAULT_SEGMENT_STALL")) segment_stall_ = std::atoi(f) != 0;
     const int D = s_.D;
     N_ = s_.N;
     nc_ = N_ * D;
@@ -595,6 +598,15 @@ class Engine final : public EngineBase {
         bar_ = alloc<GridBarrier>(1);
         cuda_check(cudaMemsetAsync(bar_, 0, sizeof(GridBarrier), stream_), "memset barrier");
         cuda_check(cudaMallocHost(&bar_host_, sizeof(GridBarrier)), "cudaMallocHost");
+      }
+      if (segment_stall_) {
+        bar_host_->count = 1u << 30;
+        bar_host_->gen = 0;
+        bar_host_->err = 0;
+        cuda_check(cudaMemcpyAsync(bar_, bar_host_, sizeof(GridBarrier), cudaMemcpyHostToDevice, stream_),
+                   "barrier");
+        sync();
+        segment_stall_ = false;  // one injected stall per workspace
       }
       RowArgs<R> a = row_args(false);
       a.p1 = pot_full(dtv, false);
@@ -1861,6 +1873,7 @@ class Engine final : public EngineBase {
   bool use_pdl_ = true;  // programmatic dependent launch (SBEC_PDL=0 disables)
   bool segment_on_ = false;     // persistent leapfrog segments (SBEC_SEGMENT=1 enables)
   bool segment_used_ = false;   // a segment ran since the last check_segments()
+  bool segment_stall_ = false;  // SBEC_FAULT_SEGMENT_STALL: one injected barrier stall (tests)
   GridBarrier* bar_ = nullptr;  // grid barrier of the segment kernel
   GridBarrier* bar_host_ = nullptr;
   // line-kernel variants in use (see sbec_lines.h); chosen by the autotuner

@@ -1083,7 +1083,7 @@ struct GridBarrier {
   int pad;
 };
 
-constexpr unsigned int kBarrierSpinLimit = 1u << 22;  // >= ~0.4 s of polling
+constexpr unsigned int kBarrierSpinLimit = 1u << 20;  // 0.1-1 s of polling (100 ns sleeps)
 
 // Grid-wide barrier of a cooperative launch (all blocks resident).  Thread 0 of each
 // block arrives with a release fence and waits, polling with a bounded count, for the

@@ -83,3 +83,36 @@ def test_segment_against_oracle(gpu):
     ws_g.close()
     assert seen == [10, 20, 30, 40]
     assert err < 5e-5 and dE < 1e-5
+
+
+def test_segment_barrier_timeout_reports_error_and_recovers(gpu):
+    """Fault injected on the host (SBEC_FAULT_SEGMENT_STALL): the barrier's arrival counter
+    starts beyond the block count, so every wait of the first segment runs out (bounded
+    polling), the remaining segments of the run leave at once, and the run reports
+    SBEC_ERR_DEVICE.  The context and the workspace stay usable: the next run, from the
+    same initial state, matches a clean run bit for bit."""
+    n, F = 64, 1
+    L = (24.0, 24.0)
+    g = S.make_grid(S.GridConfig((n, n), L))
+    og = O.make_grid(O.GridConfig((n, n), L))
+    psi0 = O.init_psi(og, F, "random", seed=3)
+
+    def make(**env):
+        with _env(SBEC_SEGMENT=1, SBEC_TUNE_FORCE=0, **env):
+            return S.make_workspace(grid=g, atom=S.AtomSpecies("x", F), interactions=S.InteractionParams(10.0, 0.5),
+                                    zeeman=S.ZeemanParams(0.0, 0.1), potential=S.HarmonicTrap(1.0, 1.0),
+                                    sim_params=S.SimParams(1e-3, 30, False, None, 10), psi_init=psi0,
+                                    precision="fp32")
+
+    ws = make(SBEC_FAULT_SEGMENT_STALL=1)
+    with pytest.raises(Exception, match="grid barrier"):
+        S.run_simulation(ws, keep_psi=False)
+    ws.psi = psi0
+    ws.set_time(0.0, 0)
+    S.run_simulation(ws, keep_psi=False)
+    recovered = ws.psi
+    ws.close()
+    clean = make()
+    S.run_simulation(clean, keep_psi=False)
+    assert np.array_equal(recovered, clean.psi)
+    clean.close()
