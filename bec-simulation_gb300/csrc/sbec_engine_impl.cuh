@@ -254,6 +254,7 @@ class Engine final : public EngineBase {
     if (!s_.ddi) {
       a.pre_diag = 1;
       a.rot_a = sm;
+      a.nem_a = a.nem_b = nematic();
       a.rot_b = sm;
       a.post_diag = 1;
       launch_potential(a);
@@ -262,12 +263,14 @@ class Engine final : public EngineBase {
     PotArgs<R> first = a;
     first.pre_diag = 1;
     first.rot_a = sm;
+    first.nem_a = nematic();
     first.spin_out = spin3_;
     launch_potential(first);
     ddi_conv(s_.padded ? 1 : 0, spin3_, phi3_);
     PotArgs<R> second = a;
     second.ddi_rot = 1;
     second.phi = phi3_;
+    second.nem_b = nematic();
     second.rot_b = sm;
     second.post_diag = 1;
     launch_potential(second);
@@ -450,6 +453,11 @@ class Engine final : public EngineBase {
       SBEC_SWITCH_D(s_.D, launch_tensor_energy_d, nb);
       finish<1>(nb, false, 30);
     }
+    if (nematic()) {
+      const int nb = red_blocks(N_);
+      SBEC_SWITCH_D(s_.D, launch_pair_energy_d, nb);
+      finish<1>(nb, false, 29);
+    }
     if (s_.ddi) {
       SBEC_SWITCH_D(s_.D, launch_spin_density_d, spin3_);
       ddi_conv(0, spin3_, phi_per_);
@@ -482,6 +490,7 @@ class Engine final : public EngineBase {
     if (s_.ddi) e.ddi = 0.5 * res[31] * dV;
     if (s_.c_lhy != 0.0) e.lhy = (2.0 / 5.0) * s_.c_lhy * res[23] * dV;
     if (s_.tensor) e.tensor = res[30] * dV;
+    if (nematic()) e.tensor = 0.5 * s_.c2 * res[29] * dV;  // _nematic_energy (src/energy.jl:106-109)
     if (comp_sums)
       for (int c = 0; c < s_.D; ++c) comp_sums[c] = res[1 + c];
     return e;
@@ -811,6 +820,7 @@ class Engine final : public EngineBase {
 
   void batch_init(int n, const double* c0, const double* c1, const double* psi_all) override {
     if (!fused_path()) fail(SBEC_ERR_UNSUPPORTED, "batched solves need the fused path (no DDI / tensor, D in {1,3,5})");
+    if (nematic()) fail(SBEC_ERR_UNSUPPORTED, "batched solves do not take the nematic (c2) step");
     if (n < 1) fail(SBEC_ERR_INVALID, "n_solves must be >= 1");
     nsolve_ = n;
     const size_t tot = (size_t)n * nc_;
@@ -1551,6 +1561,7 @@ class Engine final : public EngineBase {
     const bool sm = std::fabs(s_.c1) >= 1e-30 && s_.D > 1;
     a.pre_diag = 1;
     a.rot_a = sm;
+    a.nem_a = a.nem_b = nematic();
     a.rot_b = sm;
     a.post_diag = 1;
     a.tau_s = (R)(tau_half / 2);
@@ -1697,6 +1708,10 @@ class Engine final : public EngineBase {
   }
 
   // ---- pointwise launchers
+  // The singlet-pair (nematic) step runs when c2 is set and the tensor path is off
+  // (src/split_step.jl:60-75, src/nematic.jl:44).
+  int nematic() const { return (!s_.tensor && std::fabs(s_.c2) >= 1e-30) ? 1 : 0; }
+
   PotArgs<R> pot_args(double tau_d, bool it) const {
     PotArgs<R> a{};
     a.psi = psi_[kPsi];
@@ -1707,6 +1722,7 @@ class Engine final : public EngineBase {
     a.c0 = (R)s_.c0;
     a.c1 = (R)s_.c1;
     a.c_lhy = (R)s_.c_lhy;
+    a.c2 = (R)s_.c2;
     zeeman_factors(tau_d, it, a.zee, a.zee_lo);
     return a;
   }
@@ -1799,6 +1815,13 @@ class Engine final : public EngineBase {
     pb();
     k_energy_local<R, D><<<nb, kRedThreads, 0, stream_>>>(psi_[kPsi], N_, V_, st_, partials_);
     done("reduce", ((double)sizeof(cplx<R>) * D + (double)sizeof(R)) * (double)N_);
+  }
+
+  template <int D>
+  void launch_pair_energy_d(int nb) {
+    pb();
+    k_pair_energy<R, D><<<nb, kRedThreads, 0, stream_>>>(psi_[kPsi], N_, partials_);
+    done("reduce", (double)sizeof(cplx<R>) * D * (double)N_);
   }
 
   template <int D>

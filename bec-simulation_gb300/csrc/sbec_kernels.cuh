@@ -488,9 +488,10 @@ struct PotArgs {
   const R* phi;                // DDI potential fields (3*N) or null
   R* spin_out;                 // spin density output (3*N) or null
   int pre_diag, rot_a, ddi_rot, rot_b, post_diag;
+  int nem_a, nem_b;            // singlet-pair (nematic) steps after rot_a / before rot_b
   int itp;
   R tau_d, tau_s, tau_ddi;
-  R c0, c1, c_lhy;
+  R c0, c1, c_lhy, c2;
   cplx<R> zee[kMaxD];          // per-component Zeeman factor for diag(tau_d)
   cplx<R> zee_lo[kMaxD];       // FP32 tails of the Zeeman factors
 };
@@ -873,6 +874,60 @@ __device__ __forceinline__ void spin_mixing_point(cplx<R> (&v)[D], R c1, R tau, 
   }
 }
 
+// Singlet-pair (nematic) step (src/nematic.jl:53-119): A00 = sum_c (-1)^c psi_c psi_(D-1-c)
+// / sqrt(D) from the state before the step (component c has m = F - c, so (-1)^(F-m) =
+// (-1)^c); each (m, -m) pair, and m = 0 with itself, is turned by the exact solution of
+// i d psi_m/dt = V psi*_(-m) with V = c2 A00 (-1)^c / sqrt(D):
+//   real time  psi_m <- cos(|V| tau) psi_m - i (V/|V|) sin(|V| tau) psi*_(-m)
+//   imaginary  psi_m <- cosh(|V| tau) psi_m - (V/|V|) sinh(|V| tau) psi*_(-m)
+// pairs with |V| < 1e-30 (and every pair when |c2| < 1e-30) are left as they are.  FP32
+// forms the rotation as psi + ((cos - 1) psi + ...) with cos - 1 kept to full precision.
+template <typename R, int D>
+__device__ __forceinline__ void nematic_point(cplx<R> (&v)[D], R c2, R tau, int itp) {
+  if (!(fabs(c2) >= (R)1e-30)) return;
+  const R isd = (R)(1.0 / sqrt((double)D));
+  cplx<R> A = mk<R>(0, 0);
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    const cplx<R> pr = v[c] * v[D - 1 - c];
+    A = (c & 1) ? A - pr : A + pr;
+  }
+  const cplx<R> Vb = (c2 * isd * isd) * A;
+#pragma unroll
+  for (int c = 0; c <= (D - 1) / 2; ++c) {
+    const int cp = D - 1 - c;
+    const cplx<R> V = (c & 1) ? mk<R>(-Vb.x, -Vb.y) : Vb;
+    const R absV = sqrt(V.x * V.x + V.y * V.y);
+    if (!(absV >= (R)1e-30)) continue;
+    const cplx<R> ph = mk<R>(V.x / absV, V.y / absV);
+    const R x = absV * tau;
+    R cm1, sn;  // cos - 1 and -i sin (real time) or cosh - 1 and -sinh (imaginary time)
+    cplx<R> b;  // coefficient of conj(psi_pair)
+    if constexpr (sizeof(R) == 4) {
+      if (itp) sinh_coshm1(x, sn, cm1);
+      else sin_cosm1(x, sn, cm1);
+    } else {
+      if (itp) {
+        sn = sinh(x);
+        cm1 = cosh(x) - 1.0;
+      } else {
+        sincos(x, &sn, &cm1);
+        cm1 -= 1.0;
+      }
+    }
+    b = itp ? mk<R>(-ph.x * sn, -ph.y * sn) : mk<R>(ph.y * sn, -ph.x * sn);  // -ph sn | -i ph sn
+    const cplx<R> vm = v[c], vn = v[cp];
+    if constexpr (sizeof(R) == 8) {
+      const R ca = cm1 + (R)1;
+      v[c] = ca * vm + b * conj(vn);
+      if (cp != c) v[cp] = ca * vn + b * conj(vm);
+    } else {
+      v[c] = vm + (cm1 * vm + b * conj(vn));
+      if (cp != c) v[cp] = vn + (cm1 * vn + b * conj(vm));
+    }
+  }
+}
+
 template <typename R, int D>
 __global__ void __launch_bounds__(256) k_potential(PotArgs<R> a, SpinTabs<R> st) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -883,9 +938,11 @@ __global__ void __launch_bounds__(256) k_potential(PotArgs<R> a, SpinTabs<R> st)
   const R Vp = a.V[p];
   if (a.pre_diag) diag_point<R, D>(v, Vp, a, a.c0);
   if (a.rot_a) spin_mixing_point<R, D>(v, a.c1, a.tau_s, a.itp, st);
+  if (a.nem_a) nematic_point<R, D>(v, a.c2, a.tau_s, a.itp);
   if (a.ddi_rot) {
     spin_rotate<R, D>(v, a.phi[p], a.phi[a.N + p], a.phi[2 * a.N + p], a.tau_ddi, a.itp, st);
   }
+  if (a.nem_b) nematic_point<R, D>(v, a.c2, a.tau_s, a.itp);
   if (a.rot_b) spin_mixing_point<R, D>(v, a.c1, a.tau_s, a.itp, st);
   if (a.post_diag) diag_point<R, D>(v, Vp, a, a.c0);
 #pragma unroll
@@ -947,6 +1004,8 @@ __device__ __forceinline__ void pot_stage(cplx<R> (&v)[D], R Vp, const PotArgs<R
   const bool sm = a.rot_a && fabs(c1) >= (R)1e-30;
   if (a.pre_diag) diag_point<R, D>(v, Vp, a, c0);
   if (sm) spin_mixing_point<R, D>(v, c1, a.tau_s, a.itp, st);
+  if (a.nem_a) nematic_point<R, D>(v, a.c2, a.tau_s, a.itp);
+  if (a.nem_b) nematic_point<R, D>(v, a.c2, a.tau_s, a.itp);
   if (sm) spin_mixing_point<R, D>(v, c1, a.tau_s, a.itp, st);
   if (a.post_diag) diag_point<R, D>(v, Vp, a, c0);
 }
@@ -1544,6 +1603,27 @@ __global__ void __launch_bounds__(kRedThreads) k_energy_local(const cplx<R>* __r
     acc[3] += n * n * sqrt(n);
   }
   block_reduce_store<4>(acc, partials, false);
+}
+
+// Sum over points of |A00|^2 = |sum_c (-1)^c psi_c psi_(D-1-c)|^2 / D, in FP64, for the
+// nematic energy (c2/2) sum |A00|^2 dV (src/energy.jl:106-109, src/observables.jl:94-111).
+template <typename R, int D>
+__global__ void __launch_bounds__(kRedThreads) k_pair_energy(const cplx<R>* __restrict__ psi, int64_t N,
+                                                             double* partials) {
+  double acc[1] = {0.0};
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (int64_t)gridDim.x * blockDim.x) {
+    double ar = 0.0, ai = 0.0;
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      const cplx<R> x = psi[c * N + p], y = psi[(D - 1 - c) * N + p];
+      const double pr = (double)x.x * y.x - (double)x.y * y.y;
+      const double pi = (double)x.x * y.y + (double)x.y * y.x;
+      ar += (c & 1) ? -pr : pr;
+      ai += (c & 1) ? -pi : pi;
+    }
+    acc[0] += (ar * ar + ai * ai) / (double)D;
+  }
+  block_reduce_store<1>(acc, partials, false);
 }
 
 // Tensor energy sum_S g_S sum_M |A_SM|^2 (src/tensor_interaction.jl:247-276).

@@ -248,9 +248,7 @@ Setup build_setup(const sbec_config& cfg) {
     tensor = !s.chS.empty();
   }
   s.tensor = tensor;
-  if (!tensor) s.c2 = get_cn(2);
-  if (!tensor && std::fabs(s.c2) >= 1e-30)
-    fail(SBEC_ERR_UNSUPPORTED, "nematic (c2) step without the tensor path is not on the GPU path");
+  if (!tensor) s.c2 = get_cn(2);  // the singlet-pair (nematic) step (src/nematic.jl:34-51)
 
   if (tensor) {
     auto tab = cg_table(F);

@@ -628,7 +628,11 @@ def _report(fn, handle) -> str:
 def find_ground_states_batched(*, grid: Grid, atom: AtomSpecies, interactions: list, psi_inits: list, zeeman=None,
                                potential=None, dt: float = 0.005, n_steps: int = 10000, tol: float = 1e-10,
                                precision: str = "fp32") -> list:
-    """``find_ground_state`` for many (interactions, psi0) pairs at once; one result per pair."""
+    """``find_ground_state`` for many (interactions, psi0) pairs at once; one result per pair.
+    The batch takes per-solve c0 and c1 and a shared c_lhy; couplings in c_extra (the
+    nematic c2 or the tensor path) are not on the batched path."""
+    if any(abs(float(v)) > 1e-30 for ip in interactions for v in ip.c_extra):
+        raise _lib.UnsupportedError("batched solves take c0, c1 and c_lhy only; c_extra needs find_ground_state")
     b = GroundStateBatch(grid=grid, atom=atom, c0s=[ip.c0 for ip in interactions], c1s=[ip.c1 for ip in interactions],
                          psi_inits=psi_inits, zeeman=zeeman, potential=potential, dt=dt,
                          c_lhy=interactions[0].c_lhy if interactions else 0.0, precision=precision)

@@ -950,6 +950,67 @@ def apply_spin_mixing_step(ws: Workspace, dt_frac: float, imaginary_time: bool) 
 
 
 # ----------------------------------------------------------------------------
+# Singlet-pair (nematic) step  (src/nematic.jl:1-119, src/observables.jl:94-111)
+# ----------------------------------------------------------------------------
+
+def _pair_signs(D: int) -> np.ndarray:
+    """(-1)^(F-m) for component c (m = F - c): +1 for even c, -1 for odd c."""
+    return np.array([1.0 if c % 2 == 0 else -1.0 for c in range(D)])
+
+
+def singlet_pair_amplitude(psi: np.ndarray, F: int) -> np.ndarray:
+    """``singlet_pair_amplitude`` (src/observables.jl:94-111):
+    A00 = sum_c (-1)^(F-m) psi_c psi_(D-1-c) / sqrt(D)."""
+    D = 2 * F + 1
+    sg = _pair_signs(D)
+    s = np.zeros(psi.shape[:-1], dtype=np.complex128)
+    for c in range(D):
+        s = s + sg[c] * psi[..., c] * psi[..., D - 1 - c]
+    return s * (1.0 / math.sqrt(float(D)))
+
+
+def apply_nematic_step(ws: Workspace, dt: float, imaginary_time: bool) -> None:
+    """``apply_nematic_step!`` (src/nematic.jl:34-51) on a workspace."""
+    nematic_step_psi(ws.psi, get_cn(ws.interactions, 2), dt, imaginary_time)
+
+
+def nematic_step_psi(psi: np.ndarray, c2: float, dt: float, imaginary_time: bool) -> None:
+    """``_nematic_loop!`` (src/nematic.jl:53-119) on psi[..., D] in place: each (m, -m) pair
+    turned by the exact solution of i d psi_m/dt = V psi*_(-m), V = c2 A00 (-1)^(F-m) / sqrt(D),
+    with A00 from the state before the step; skipped where |V| < 1e-30 (and entirely for
+    |c2| < 1e-30)."""
+    if abs(c2) < 1e-30:
+        return
+    D = psi.shape[-1]
+    flat = _flat_spinors(psi)
+    inv_sqrt_D = 1.0 / math.sqrt(float(D))
+    sg = _pair_signs(D)
+    A00 = np.zeros(flat.shape[0], dtype=np.complex128)
+    for c in range(D):
+        A00 = A00 + sg[c] * flat[:, c] * flat[:, D - 1 - c]
+    A00 = A00 * inv_sqrt_D
+    V_base = c2 * A00 * inv_sqrt_D
+    new = flat.copy()
+    for c in range((D + 1) // 2):
+        cp = D - 1 - c
+        V = V_base * sg[c]
+        absV = np.abs(V)
+        act = absV >= 1e-30
+        phase = np.where(act, V / np.where(act, absV, 1.0), 0.0)
+        if imaginary_time:
+            a = np.cosh(absV * dt)
+            b = -phase * np.sinh(absV * dt)
+        else:
+            a = np.cos(absV * dt)
+            b = -1j * phase * np.sin(absV * dt)
+        vm, vn = flat[:, c], flat[:, cp]
+        new[:, c] = np.where(act, a * vm + b * np.conj(vn), vm)
+        if cp != c:
+            new[:, cp] = np.where(act, a * vn + b * np.conj(vm), vn)
+    _set_flat_spinors(psi, new)
+
+
+# ----------------------------------------------------------------------------
 # General-F tensor interaction  (src/tensor_interaction.jl:130-276)
 # ----------------------------------------------------------------------------
 
@@ -1067,14 +1128,9 @@ YOSHIDA_W1 = 1.0 / (2.0 - 2.0 ** (1 / 3))
 YOSHIDA_W0 = 1.0 - 2.0 * YOSHIDA_W1
 
 
-def _unsupported_check(ws: Workspace) -> None:
-    if ws.tensor_cache is None and abs(get_cn(ws.interactions, 2)) >= 1e-30:
-        raise NotImplementedError("nematic (c2) step without the tensor path is not restated")
-
-
 def half_potential_step(ws: Workspace, dt_half: float, imaginary_time: bool) -> None:
-    """``_half_potential_step!`` (src/split_step.jl:48-133): symmetric inner splitting."""
-    _unsupported_check(ws)
+    """``_half_potential_step!`` (src/split_step.jl:48-133): symmetric inner splitting
+    diag, spin mixing, nematic | tensor, [DDI], nematic | tensor, spin mixing, diag."""
     zee = zeeman_at(ws.zeeman, ws.t)
     zd = zeeman_diagonal(zee, ws.F)
     diagonal_step(ws, dt_half / 2, zd, imaginary_time)
@@ -1082,11 +1138,13 @@ def half_potential_step(ws: Workspace, dt_half: float, imaginary_time: bool) -> 
         apply_tensor_interaction_step(ws, dt_half / 2, imaginary_time)
     else:
         apply_spin_mixing_step(ws, dt_half / 2, imaginary_time)
+        apply_nematic_step(ws, dt_half / 2, imaginary_time)
     if ws.ddi is not None:
         apply_ddi_step(ws, dt_half, imaginary_time)
     if ws.tensor_cache is not None:
         apply_tensor_interaction_step(ws, dt_half / 2, imaginary_time)
     else:
+        apply_nematic_step(ws, dt_half / 2, imaginary_time)
         apply_spin_mixing_step(ws, dt_half / 2, imaginary_time)
     diagonal_step(ws, dt_half / 2, zd, imaginary_time)
 
@@ -1193,6 +1251,10 @@ def energy_terms(ws: Workspace) -> dict:
     E_tensor = 0.0
     if ws.tensor_cache is not None:
         E_tensor = tensor_interaction_energy(psi, ws.tensor_cache, dV)
+    else:
+        c2 = get_cn(ws.interactions, 2)
+        if c2 != 0.0:  # _nematic_energy (src/energy.jl:106-109)
+            E_tensor = 0.5 * c2 * float(np.sum(np.abs(singlet_pair_amplitude(psi, ws.F)) ** 2)) * dV
     return dict(kinetic=E_kin, trap=E_trap, zeeman=E_zee, c0=E_c0, c1=E_c1, ddi=E_ddi,
                 lhy=E_lhy, tensor=E_tensor)
 

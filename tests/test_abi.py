@@ -56,8 +56,8 @@ def test_invalid_config_rejected_before_device(libsbec):
         S.make_workspace(grid=g, atom=S.Rb87, interactions=S.InteractionParams(1.0, 0.0),
                          sim_params=S.SimParams(1e-3, 1))
     g2 = S.make_grid(S.GridConfig((16,), (8.0,)))
-    with pytest.raises(S.UnsupportedError):  # nematic c2 without the tensor path
-        S.make_workspace(grid=g2, atom=S.AtomSpecies("x", 2), interactions=S.InteractionParams(1.0, 0.0, 0.0, (1.0,)),
+    with pytest.raises(S.UnsupportedError):  # spin F > 6
+        S.make_workspace(grid=g2, atom=S.AtomSpecies("x", 7), interactions=S.InteractionParams(1.0, 0.0),
                          sim_params=S.SimParams(1e-3, 1))
 
 

@@ -47,6 +47,10 @@ CASES = {
     "f6_ddi_pad_sec": dict(F=6, c0=50.0, c1=0.5, ddi=True, c_dd=60.0, padded=True, secular=True),
     "f6_tensor_ddi_pad": dict(F=6, c0=200.0, c1=200.0 / 36, c_extra=(0.0, 0.0, 50.0), ddi=True, c_dd=100.0,
                               padded=True),
+    # singlet-pair (nematic) step: c2 without a higher even c_k (src/nematic.jl)
+    "f1_nematic": dict(F=1, c0=10.0, c1=-0.5, c_extra=(50.0,), zeeman=(0.1, 0.05)),
+    "f2_nematic": dict(F=2, c0=30.0, c1=2.0, c_extra=(30.0,), zeeman=(0.2, -0.05)),
+    "f1_nematic_ddi": dict(F=1, c0=10.0, c1=0.3, c_extra=(20.0,), ddi=True, c_dd=40.0),
 }
 
 CASE_GRIDS = [((64,), (20.0,)), ((16, 32), (8.0, 12.0)), ((8, 16, 8), (6.0, 8.0, 6.0))]
@@ -100,7 +104,7 @@ def test_ddi_potential_fields(gpu, padded, secular, n, L):
 
 
 @pytest.mark.parametrize("n,L", CASE_GRIDS)
-@pytest.mark.parametrize("case", ["f1_sm_zeeman_lhy", "f2_tensor", "f1_ddi_pad"])
+@pytest.mark.parametrize("case", ["f1_sm_zeeman_lhy", "f2_tensor", "f1_ddi_pad", "f1_nematic", "f2_nematic"])
 def test_split_step_rt(gpu, n, L, case):
     kw = dict(CASES[case])
     F = kw.pop("F")
@@ -154,8 +158,8 @@ def test_unsupported_and_invalid(gpu):
         S.make_workspace(grid=og, atom=S.AtomSpecies("x", 1), interactions=S.InteractionParams(1.0, 0.0),
                          sim_params=S.SimParams(1e-3, 1))
     g2 = S.make_grid(S.GridConfig((16,), (10.0,)))
-    with pytest.raises(S.UnsupportedError):  # nematic-only c2 (next row)
-        S.make_workspace(grid=g2, atom=S.AtomSpecies("x", 2), interactions=S.InteractionParams(1.0, 0.0, 0.0, (1.0,)),
+    with pytest.raises(S.UnsupportedError):  # spin F > 6
+        S.make_workspace(grid=g2, atom=S.AtomSpecies("x", 7), interactions=S.InteractionParams(1.0, 0.0),
                          sim_params=S.SimParams(1e-3, 1))
     with pytest.raises(S.ArgumentError):
         S.make_workspace(grid=g2, atom=S.AtomSpecies("x", 1), interactions=S.InteractionParams(1.0, 0.0),
