@@ -882,8 +882,10 @@ __device__ __forceinline__ void spin_mixing_point(cplx<R> (&v)[D], R c1, R tau, 
 //   imaginary  psi_m <- cosh(|V| tau) psi_m - (V/|V|) sinh(|V| tau) psi*_(-m)
 // pairs with |V| < 1e-30 (and every pair when |c2| < 1e-30) are left as they are.  FP32
 // forms the rotation as psi + ((cos - 1) psi + ...) with cos - 1 kept to full precision.
+// Kept out of line: the potential stages call it only when c2 is set, and inlining it
+// would enlarge every row pass.
 template <typename R, int D>
-__device__ __forceinline__ void nematic_point(cplx<R> (&v)[D], R c2, R tau, int itp) {
+__device__ __noinline__ void nematic_point(cplx<R> (&v)[D], R c2, R tau, int itp) {
   if (!(fabs(c2) >= (R)1e-30)) return;
   const R isd = (R)(1.0 / sqrt((double)D));
   cplx<R> A = mk<R>(0, 0);
