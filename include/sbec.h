@@ -34,7 +34,7 @@ extern "C" {
 typedef enum sbec_status {
   SBEC_OK = 0,
   SBEC_ERR_INVALID = 1,      /* invalid argument / configuration (ArgumentError in the reference) */
-  SBEC_ERR_UNSUPPORTED = 2,  /* option outside the GPU path (Raman, loss, nematic-only c2, non power-of-two n) */
+  SBEC_ERR_UNSUPPORTED = 2,  /* option outside the GPU path (Raman, loss, non power-of-two n, F > 6) */
   SBEC_ERR_OOM = 3,          /* device allocation failed */
   SBEC_ERR_NUMERIC = 4,      /* NaN / ITP overflow detected (src/ground_state.jl:4-29) */
   SBEC_ERR_DEVICE = 5,       /* CUDA error or no device */
