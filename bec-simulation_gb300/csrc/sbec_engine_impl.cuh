@@ -1295,7 +1295,7 @@ class Engine final : public EngineBase {
   // ---- autotuner.  The first time a line-kernel call shape is met (outside a graph
   // capture) every compiled variant is timed on a copy of the data it would touch:
   // one warm-up launch, then the median of three CUDA-event timings, each on a
-  // fresh copy.  The fastest is kept in a table shared by all workspaces of the
+  // fresh copy (of 8 back-to-back launches for data up to 32 MB).  The fastest is kept in a table shared by all workspaces of the
   // process, so every solve of one shape runs the same kernels (the variants agree
   // to FP32 rounding, not bit for bit).
   static std::mutex& tune_mutex() {
@@ -1352,6 +1352,10 @@ class Engine final : public EngineBase {
     cuda_check(cudaEventCreate(&e0), "cudaEventCreate");
     cuda_check(cudaEventCreate(&e1), "cudaEventCreate");
     const size_t bytes = sizeof(cplx<R>) * extent;
+    // Small (latency-bound) shapes are timed as a burst of back-to-back launches, the way
+    // they run inside a step graph; one launch there is mostly launch latency, which is
+    // the same for every variant.
+    const int reps = bytes <= ((size_t)32 << 20) ? 8 : 1;
     std::string line = key + " ->";
     float best = 0.0f;
     int bv = cands[0];
@@ -1362,10 +1366,11 @@ class Engine final : public EngineBase {
       for (float& ti : t) {
         cuda_check(cudaMemcpyAsync(tune_buf_, src, bytes, cudaMemcpyDeviceToDevice, stream_), "cudaMemcpyAsync");
         cuda_check(cudaEventRecord(e0, stream_), "cudaEventRecord");
-        launch(v, tune_buf_);
+        for (int r = 0; r < reps; ++r) launch(v, tune_buf_);
         cuda_check(cudaEventRecord(e1, stream_), "cudaEventRecord");
         cuda_check(cudaEventSynchronize(e1), "cudaEventSynchronize");
         cuda_check(cudaEventElapsedTime(&ti, e0, e1), "cudaEventElapsedTime");
+        ti /= (float)reps;
       }
       std::sort(t, t + 3);
       line += " v" + std::to_string(v) + "=" + std::to_string(t[1] * 1000.0f).substr(0, 7) + "us";
