@@ -22,8 +22,8 @@ test/test_clebsch_gordan.jl, the g_S identities of
 test/test_interactions_constraint.jl, the conservation and order tests of
 test/test_split_step.jl, test/test_physics_level1.jl, test/test_ddi.jl,
 test/test_tensor_interaction.jl, test/test_analytical_validation.jl, the
-singlet-pair (nematic) tests of test/test_nematic.jl and the ground-state tests of
-test/test_simulation.jl).
+singlet-pair (nematic) tests of test/test_nematic.jl, the loss tests of
+test/test_losses.jl and the ground-state tests of test/test_simulation.jl).
 """
 
 from .spinorbec_oracle import *  # noqa: F401,F403

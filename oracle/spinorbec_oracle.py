@@ -590,6 +590,7 @@ class Workspace:
     tensor_cache: Optional[TensorCache] = None
     # last unpadded Φ, for the ITP overflow check (src/ground_state.jl:12-17)
     last_phi: Optional[tuple] = None
+    loss: Optional["LossParams"] = None  # real-time losses (src/losses.jl)
 
     @property
     def F(self) -> int:
@@ -619,7 +620,7 @@ def make_workspace(*, grid: Grid, atom: AtomSpecies, interactions: InteractionPa
                    zeeman=None, V: Optional[np.ndarray] = None, sim_params: SimParams,
                    psi_init: Optional[np.ndarray] = None, enable_ddi: bool = False,
                    c_dd: float = float("nan"), secular_ddi: bool = False,
-                   ddi_padding: bool = False) -> Workspace:
+                   ddi_padding: bool = False, loss: Optional["LossParams"] = None) -> Workspace:
     """``make_workspace`` (src/initialization.jl:86-191), including tensor-path activation (:164-185)."""
     F = atom.F
     sm = spin_matrices(F)
@@ -658,7 +659,7 @@ def make_workspace(*, grid: Grid, atom: AtomSpecies, interactions: InteractionPa
         ws_int = interactions
     return Workspace(psi=psi, t=0.0, step=0, grid=grid, sm=sm, interactions=ws_int, zeeman=zeeman,
                      V=V, sim_params=sim_params, kinetic_phase=kin, ddi=ddi, ddi_padded=ddi_pad,
-                     tensor_cache=tc)
+                     tensor_cache=tc, loss=loss)
 
 
 # ----------------------------------------------------------------------------
@@ -950,6 +951,54 @@ def apply_spin_mixing_step(ws: Workspace, dt_frac: float, imaginary_time: bool) 
 
 
 # ----------------------------------------------------------------------------
+# Density-dependent losses  (src/losses.jl:1-97)
+# ----------------------------------------------------------------------------
+
+@dataclass
+class LossParams:
+    """``LossParams(gamma_dr, L3)`` (src/types.jl): dipolar-relaxation rate and 3-body rate."""
+
+    gamma_dr: float
+    L3: float = 0.0
+
+
+def dipolar_relaxation_rates(F: int, gamma_dr: float) -> np.ndarray:
+    """``_dipolar_relaxation_rates`` (src/losses.jl:68-97): gamma_m = gamma_dr raw_m / Z with
+    raw_m = sum over q in (-1, -2), |m + q| <= F, of CG(F,m; 2,q | F,m+q)^2 and Z = sum raw / D."""
+    D = 2 * F + 1
+    raw = np.zeros(D)
+    for c in range(D):
+        m = F - c
+        s = 0.0
+        for q in (-1, -2):
+            mp = m + q
+            if abs(mp) > F:
+                continue
+            cg = clebsch_gordan(F, m, 2, q, F, mp)
+            s += cg * cg
+        raw[c] = s
+    if raw.sum() < 1e-30:
+        return np.zeros(D)
+    Z = raw.sum() / D
+    return np.array([gamma_dr * raw[c] / Z for c in range(D)])
+
+
+def apply_loss_step_psi(psi: np.ndarray, loss: Optional["LossParams"], F: int, dt: float) -> None:
+    """``apply_loss_step!`` (src/losses.jl:25-45) on psi[..., D] in place:
+    psi_m *= exp(-(gamma_m + L3) n dt / 2), n the total density before the step; components
+    with a rate below 1e-30 (and everything when both rates are below 1e-30) are untouched."""
+    if loss is None or (loss.gamma_dr < 1e-30 and loss.L3 < 1e-30):
+        return
+    n = total_density(psi)
+    rates = dipolar_relaxation_rates(F, loss.gamma_dr)
+    for c in range(psi.shape[-1]):
+        rate = rates[c] + loss.L3
+        if rate < 1e-30:
+            continue
+        psi[..., c] *= np.exp(-rate * n * dt / 2)
+
+
+# ----------------------------------------------------------------------------
 # Singlet-pair (nematic) step  (src/nematic.jl:1-119, src/observables.jl:94-111)
 # ----------------------------------------------------------------------------
 
@@ -1165,6 +1214,8 @@ def split_step(ws: Workspace) -> None:
     half_potential_step(ws, dt / 2, it)
     apply_kinetic_step_batched(ws)
     half_potential_step(ws, dt / 2, it)
+    if not it and ws.loss is not None:  # src/split_step.jl:21-23
+        apply_loss_step_psi(ws.psi, ws.loss, ws.F, dt)
     ws.t += 0.0 if it else dt
     ws.step += 1
     ne = ws.sim_params.normalize_every
@@ -1320,6 +1371,7 @@ def _run_leapfrog(ws, sp, res, callback, keep_psi) -> None:
             half_potential_step(ws, dt / 2, False)
         else:
             half_potential_step(ws, dt, False)
+        apply_loss_step_psi(ws.psi, ws.loss, ws.F, dt)  # src/simulation.jl:75-77
         ws.t += dt
         ws.step += 1
         if is_save:
@@ -1428,6 +1480,7 @@ def _adaptive_step_change(ws, adaptive, t_end, save_interval, callback, keep_psi
                 continue
         fsal_deferred = True
         fsal_dt = dt_step
+        apply_loss_step_psi(ws.psi, ws.loss, ws.F, dt_step)  # src/adaptive.jl:151-153
         ws.t += dt_step
         ws.step += 1
         n_acc += 1
@@ -1487,6 +1540,7 @@ def _adaptive_richardson(ws, adaptive, t_end, save_interval, callback, keep_psi)
             dt = max(dt_step * factor, adaptive.dt_min)
             n_rej += 1
             continue
+        apply_loss_step_psi(ws.psi, ws.loss, ws.F, dt_step)  # src/adaptive.jl:262-264
         ws.t += dt_step
         ws.step += 1
         n_acc += 1
@@ -1537,6 +1591,7 @@ def run_simulation_yoshida(ws: Workspace, adaptive: AdaptiveDtParams, t_end: flo
             dt = max(dt_step * factor, adaptive.dt_min)
             n_rej += 1
             continue
+        apply_loss_step_psi(ws.psi, ws.loss, ws.F, dt_step)  # src/yoshida.jl:64-66
         ws.t += dt_step
         ws.step += 1
         n_acc += 1
