@@ -23,7 +23,8 @@ test/test_interactions_constraint.jl, the conservation and order tests of
 test/test_split_step.jl, test/test_physics_level1.jl, test/test_ddi.jl,
 test/test_tensor_interaction.jl, test/test_analytical_validation.jl, the
 singlet-pair (nematic) tests of test/test_nematic.jl, the loss tests of
-test/test_losses.jl and the ground-state tests of test/test_simulation.jl).
+test/test_losses.jl, the Raman tests of test/test_raman.jl and the ground-state tests of
+test/test_simulation.jl).
 """
 
 from .spinorbec_oracle import *  # noqa: F401,F403

@@ -591,6 +591,7 @@ class Workspace:
     # last unpadded Φ, for the ITP overflow check (src/ground_state.jl:12-17)
     last_phi: Optional[tuple] = None
     loss: Optional["LossParams"] = None  # real-time losses (src/losses.jl)
+    raman: Optional["RamanCoupling"] = None  # Raman coupling (src/raman.jl)
 
     @property
     def F(self) -> int:
@@ -620,7 +621,8 @@ def make_workspace(*, grid: Grid, atom: AtomSpecies, interactions: InteractionPa
                    zeeman=None, V: Optional[np.ndarray] = None, sim_params: SimParams,
                    psi_init: Optional[np.ndarray] = None, enable_ddi: bool = False,
                    c_dd: float = float("nan"), secular_ddi: bool = False,
-                   ddi_padding: bool = False, loss: Optional["LossParams"] = None) -> Workspace:
+                   ddi_padding: bool = False, loss: Optional["LossParams"] = None,
+                   raman: Optional["RamanCoupling"] = None) -> Workspace:
     """``make_workspace`` (src/initialization.jl:86-191), including tensor-path activation (:164-185)."""
     F = atom.F
     sm = spin_matrices(F)
@@ -659,7 +661,7 @@ def make_workspace(*, grid: Grid, atom: AtomSpecies, interactions: InteractionPa
         ws_int = interactions
     return Workspace(psi=psi, t=0.0, step=0, grid=grid, sm=sm, interactions=ws_int, zeeman=zeeman,
                      V=V, sim_params=sim_params, kinetic_phase=kin, ddi=ddi, ddi_padded=ddi_pad,
-                     tensor_cache=tc, loss=loss)
+                     tensor_cache=tc, loss=loss, raman=raman)
 
 
 # ----------------------------------------------------------------------------
@@ -951,6 +953,54 @@ def apply_spin_mixing_step(ws: Workspace, dt_frac: float, imaginary_time: bool) 
 
 
 # ----------------------------------------------------------------------------
+# Raman coupling  (src/raman.jl:1-31, src/spinor_utils.jl:27-38, src/energy.jl:123-135)
+# ----------------------------------------------------------------------------
+
+@dataclass
+class RamanCoupling:
+    """``RamanCoupling{N}(Omega_R, delta, k_eff)`` (src/types.jl:179-183)."""
+
+    Omega_R: float
+    delta: float
+    k_eff: tuple
+
+
+def _raman_hamiltonians(sm: SpinMatrices, raman: RamanCoupling, grid: Grid) -> np.ndarray:
+    """H_R(r) = delta Fz + (Omega_R/2)(e^{i k.r} F+ + e^{-i k.r} F-) at every point, as an array
+    (points in column-major order, D, D)."""
+    shape = grid.config.n_points
+    kr = np.zeros(shape, order="F")
+    for d in range(len(shape)):
+        sl = [None] * len(shape)
+        sl[d] = slice(None)
+        kr = kr + raman.k_eff[d] * np.asarray(grid.x[d])[tuple(sl)]
+    ph = np.exp(1j * kr).ravel(order="F")
+    return (raman.delta * sm.Fz[None, :, :]
+            + (raman.Omega_R / 2) * (ph[:, None, None] * sm.Fp[None, :, :] + np.conj(ph)[:, None, None] * sm.Fm[None, :, :]))
+
+
+def raman_step_psi(psi: np.ndarray, sm: SpinMatrices, raman: RamanCoupling, grid: Grid, dt: float,
+                   imaginary_time: bool) -> None:
+    """``apply_raman_step!`` (src/raman.jl:8-31) on psi[..., D] in place: per point
+    psi <- V exp(-i Lambda dt) V^dagger psi (exp(-Lambda dt) in imaginary time) from the
+    eigen-decomposition of H_R (``_exp_i_hermitian``, src/spinor_utils.jl:27-38)."""
+    H = _raman_hamiltonians(sm, raman, grid)
+    lam, V = np.linalg.eigh(H)
+    e = np.exp(-lam * dt) if imaginary_time else np.exp(-1j * lam * dt)
+    flat = _flat_spinors(psi)
+    y = np.einsum("pji,pj->pi", np.conj(V), flat)          # V^dagger psi
+    out = np.einsum("pij,pj->pi", V, e * y)
+    _set_flat_spinors(psi, out)
+
+
+def raman_energy(psi: np.ndarray, sm: SpinMatrices, raman: RamanCoupling, grid: Grid) -> float:
+    """``_raman_energy`` (src/energy.jl:123-135): sum over points of Re(psi^dagger H_R psi) dV."""
+    H = _raman_hamiltonians(sm, raman, grid)
+    flat = _flat_spinors(psi)
+    return float(np.sum(np.einsum("pi,pij,pj->p", np.conj(flat), H, flat).real)) * cell_volume(grid)
+
+
+# ----------------------------------------------------------------------------
 # Density-dependent losses  (src/losses.jl:1-97)
 # ----------------------------------------------------------------------------
 
@@ -1179,7 +1229,8 @@ YOSHIDA_W0 = 1.0 - 2.0 * YOSHIDA_W1
 
 def half_potential_step(ws: Workspace, dt_half: float, imaginary_time: bool) -> None:
     """``_half_potential_step!`` (src/split_step.jl:48-133): symmetric inner splitting
-    diag, spin mixing, nematic | tensor, [DDI], nematic | tensor, spin mixing, diag."""
+    diag, spin mixing, nematic | tensor, [Raman], [DDI], [Raman], nematic | tensor, spin
+    mixing, diag."""
     zee = zeeman_at(ws.zeeman, ws.t)
     zd = zeeman_diagonal(zee, ws.F)
     diagonal_step(ws, dt_half / 2, zd, imaginary_time)
@@ -1188,8 +1239,12 @@ def half_potential_step(ws: Workspace, dt_half: float, imaginary_time: bool) -> 
     else:
         apply_spin_mixing_step(ws, dt_half / 2, imaginary_time)
         apply_nematic_step(ws, dt_half / 2, imaginary_time)
+    if ws.raman is not None:
+        raman_step_psi(ws.psi, ws.sm, ws.raman, ws.grid, dt_half / 2, imaginary_time)
     if ws.ddi is not None:
         apply_ddi_step(ws, dt_half, imaginary_time)
+    if ws.raman is not None:
+        raman_step_psi(ws.psi, ws.sm, ws.raman, ws.grid, dt_half / 2, imaginary_time)
     if ws.tensor_cache is not None:
         apply_tensor_interaction_step(ws, dt_half / 2, imaginary_time)
     else:
@@ -1306,15 +1361,18 @@ def energy_terms(ws: Workspace) -> dict:
         c2 = get_cn(ws.interactions, 2)
         if c2 != 0.0:  # _nematic_energy (src/energy.jl:106-109)
             E_tensor = 0.5 * c2 * float(np.sum(np.abs(singlet_pair_amplitude(psi, ws.F)) ** 2)) * dV
-    return dict(kinetic=E_kin, trap=E_trap, zeeman=E_zee, c0=E_c0, c1=E_c1, ddi=E_ddi,
-                lhy=E_lhy, tensor=E_tensor)
+    terms = dict(kinetic=E_kin, trap=E_trap, zeeman=E_zee, c0=E_c0, c1=E_c1, ddi=E_ddi,
+                 lhy=E_lhy, tensor=E_tensor)
+    if ws.raman is not None:  # the Raman term only where the workspace has a coupling
+        terms["raman"] = raman_energy(psi, ws.sm, ws.raman, grid)
+    return terms
 
 
 def total_energy(ws: Workspace) -> float:
     """``total_energy`` (src/energy.jl:6-54): the terms summed in the reference's order."""
     e = energy_terms(ws)
     return (e["kinetic"] + e["trap"] + e["zeeman"] + e["c0"] + e["c1"] + e["ddi"] + e["lhy"]
-            + e["tensor"])
+            + e["tensor"] + e.get("raman", 0.0))
 
 
 # ----------------------------------------------------------------------------
