@@ -419,15 +419,24 @@ def _zeeman_energies(z: ZeemanParams, F: int) -> np.ndarray:
 
 def _validate_itp(zeeman, interactions: InteractionParams, F: int, dt: float, psi, c_dd: float) -> None:
     """``_validate_itp_zeeman`` / ``_validate_itp_interactions`` (src/ground_state.jl:31-78)."""
+    lim = ITP_EXPONENT_LIMIT
     if not callable(zeeman):
-        if float(np.max(np.abs(_zeeman_energies(zeeman, F)))) * dt / 4 > ITP_EXPONENT_LIMIT:
-            raise _lib.ArgumentError(f"Zeeman p={zeeman.p} with F={F} and dt={dt} causes overflow in imaginary time")
+        e = float(np.max(np.abs(_zeeman_energies(zeeman, F)))) * dt / 4
+        if e > lim:
+            raise _lib.ArgumentError(
+                f"Zeeman p={zeeman.p} with F={F} and dt={dt} causes overflow in imaginary time "
+                f"(exponent={e:.1f} > {lim}). Reduce p or dt. For ferromagnetic ground state, p=10 suffices.")
     n_peak = float(np.max(np.sum(np.abs(psi) ** 2, axis=-1))) if psi is not None else 1.0
     max_c = max(abs(interactions.c0), abs(interactions.c1))
-    if max_c > 1e-30 and max_c * n_peak * dt / 4 > ITP_EXPONENT_LIMIT:
-        raise _lib.ArgumentError("Spin interaction may cause overflow in imaginary time; reduce c0/c1 or dt")
-    if c_dd > 0 and c_dd * F * n_peak * dt / 2 > ITP_EXPONENT_LIMIT:
-        raise _lib.ArgumentError("DDI may cause overflow in imaginary time; reduce c_dd or dt")
+    if max_c > 1e-30 and max_c * n_peak * dt / 4 > lim:
+        raise _lib.ArgumentError(
+            f"Spin interaction c0={interactions.c0}, c1={interactions.c1} with n_peak≈{n_peak:.3g} and dt={dt} "
+            f"may cause overflow in imaginary time (estimated exponent={max_c * n_peak * dt / 4:.1f} > {lim}). "
+            "Reduce c0/c1 magnitude or dt.")
+    if c_dd > 0 and c_dd * F * n_peak * dt / 2 > lim:
+        raise _lib.ArgumentError(
+            f"DDI c_dd={c_dd} with F={F}, n_peak≈{n_peak:.3g} and dt={dt} may cause overflow in imaginary "
+            f"time (estimated exponent={c_dd * F * n_peak * dt / 2:.1f} > {lim}). Reduce c_dd or dt.")
 
 
 def find_ground_state(*, grid: Grid, atom: AtomSpecies, interactions: InteractionParams, zeeman=None,

@@ -92,3 +92,24 @@ def test_snapshot_store_blocks():
     outs[0][...] = 0.0
     assert np.array_equal(outs[1], refs[1])
     assert outs[0].base is outs[1].base and outs[2].base is not outs[0].base
+
+
+@pytest.mark.parametrize("case", ["zeeman", "interaction", "ddi"])
+def test_itp_overflow_guards_before_device(case):
+    """find_ground_state rejects parameters whose imaginary-time exponents would overflow
+    (src/ground_state.jl:31-78) before any device work, with the reference's message."""
+    import spinorbec as S
+
+    g = S.make_grid(S.GridConfig((32,), (10.0,)))
+    kw = dict(grid=g, atom=S.AtomSpecies("x", 1), dt=0.01, n_steps=10)
+    if case == "zeeman":
+        kw.update(interactions=S.InteractionParams(1.0, 0.0), zeeman=S.ZeemanParams(50000.0, 0.0))
+        match = "Zeeman p=50000.0 with F=1 and dt=0.01 causes overflow"
+    elif case == "interaction":
+        kw.update(interactions=S.InteractionParams(1e7, 0.0))
+        match = "Spin interaction c0=10000000.0"
+    else:
+        kw.update(interactions=S.InteractionParams(1.0, 0.0), enable_ddi=True, c_dd=1e7)
+        match = "DDI c_dd=10000000.0 with F=1"
+    with pytest.raises(S.ArgumentError, match=match):
+        S.find_ground_state(**kw)
