@@ -147,9 +147,17 @@ class Workspace:
 def make_workspace(*, grid: Grid, atom: AtomSpecies, interactions: InteractionParams, zeeman=None, potential=None,
                    sim_params: SimParams, psi_init: Optional[np.ndarray] = None, enable_ddi: bool = False,
                    c_dd: float = float("nan"), secular_ddi: bool = False, ddi_padding: bool = False,
-                   gS: Optional[dict] = None, precision: str = "fp64", graphs: bool = True) -> Workspace:
+                   gS: Optional[dict] = None, precision: str = "fp64", graphs: bool = True,
+                   raman=None, loss=None) -> Workspace:
     """``make_workspace`` (src/initialization.jl:86-191) with a device-resident state.
-    graphs=False: the workspace launches every kernel eagerly (see Workspace.set_graph_mode)."""
+    graphs=False: the workspace launches every kernel eagerly (see Workspace.set_graph_mode).
+    ``raman`` and ``loss`` (the reference's RamanCoupling and LossParams) are not on the GPU
+    path: passing one raises UnsupportedError, as sbec_ws_create does for other options
+    outside it, so a caller can keep the CPU path for that run."""
+    if raman is not None:
+        raise _lib.UnsupportedError("Raman coupling (src/raman.jl) is not on the GPU path")
+    if loss is not None and (loss.gamma_dr >= 1e-30 or loss.L3 >= 1e-30):
+        raise _lib.UnsupportedError("density-dependent losses (src/losses.jl) are not on the GPU path")
     lib = load()
     zeeman = ZeemanParams() if zeeman is None else zeeman
     if callable(zeeman):

@@ -113,3 +113,19 @@ def test_itp_overflow_guards_before_device(case):
         match = "DDI c_dd=10000000.0 with F=1"
     with pytest.raises(S.ArgumentError, match=match):
         S.find_ground_state(**kw)
+
+
+def test_raman_and_loss_options_are_unsupported_before_device():
+    """The reference's make_workspace options outside the GPU path raise UnsupportedError
+    before any device work; a loss with zero rates is the same as no loss."""
+    import spinorbec as S
+    from collections import namedtuple
+
+    Loss = namedtuple("Loss", "gamma_dr L3")
+    Raman = namedtuple("Raman", "Omega_R delta k_eff")
+    g = S.make_grid(S.GridConfig((32,), (10.0,)))
+    kw = dict(grid=g, atom=S.Rb87, interactions=S.InteractionParams(1.0, 0.0), sim_params=S.SimParams(1e-3, 1))
+    with pytest.raises(S.UnsupportedError, match="Raman"):
+        S.make_workspace(raman=Raman(1.0, 0.0, (0.0,)), **kw)
+    with pytest.raises(S.UnsupportedError, match="losses"):
+        S.make_workspace(loss=Loss(0.1, 0.0), **kw)
