@@ -7,7 +7,10 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <memory>
 #include <string>
 #include <vector>
@@ -49,6 +52,15 @@ thread_local std::string g_err;
 
 namespace sbec {
 void set_last_error(const std::string& msg) { g_err = msg; }
+
+std::mutex& tune_table_mutex() {
+  static std::mutex m;
+  return m;
+}
+std::map<std::string, int>& tune_table_map() {
+  static std::map<std::string, int> t;
+  return t;
+}
 }  // namespace sbec
 
 namespace {
@@ -296,6 +308,39 @@ void normalize_constrained(EngineBase& e, double target) {
   for (int c = 0; c < D; ++c) w[c] = std::exp(lambda * (double)(F - c));
   e.scale_components(w.data());
   e.normalize();
+}
+
+// classify_phase (src/diagnostics.jl:166-206) from the device grid sums.
+void classify_phase(EngineBase& e, int solve, sbec_phase_info* out) {
+  const Setup& s = e.setup();
+  double r[kPhaseSums];
+  e.phase_sums(solve, r);
+  *out = sbec_phase_info{};
+  const int F = s.F, D = s.D;
+  const double dV = s.dV;
+  out->n_channels = F + 1;
+  const double n_sum = r[0] * dV, n_sq = r[1] * dV;
+  if (n_sum < 1e-30) {
+    out->phase = SBEC_PHASE_VACUUM;
+    return;
+  }
+  out->spin_order = F > 0 ? r[2] * dV / ((double)F * F * n_sq) : 0.0;
+  double total = 0.0;
+  for (int k = 0; k <= F; ++k) {
+    out->raw_channel_weights[k] = r[4 + k] * dV;
+    total += out->raw_channel_weights[k];
+  }
+  for (int k = 0; k <= F; ++k) out->channel_weights[k] = total > 0 ? out->raw_channel_weights[k] / total : 0.0;
+  out->nematic_order = out->raw_channel_weights[0] / (n_sq / D);
+  out->magnetization_density = r[3] * dV / n_sum;
+  if (out->spin_order > 0.9)
+    out->phase = SBEC_PHASE_FERROMAGNETIC;
+  else if (out->nematic_order > 0.9)
+    out->phase = F == 1 ? SBEC_PHASE_POLAR : SBEC_PHASE_NEMATIC;
+  else if (out->channel_weights[F] > 0.5)
+    out->phase = SBEC_PHASE_CYCLIC;
+  else
+    out->phase = SBEC_PHASE_MIXED;
 }
 
 // _check_itp_overflow (src/ground_state.jl:4-29)
@@ -772,6 +817,77 @@ sbec_status sbec_ground_state(sbec_ws* ws, int64_t n_steps, double tol, int64_t 
   SBEC_API_END
 }
 
+// _find_ground_state_adaptive (src/ground_state.jl:172-237): blocks of check_every
+// split steps; the block is kept when the energy did not rise (dt grows by 10 %, capped
+// at dt_max), otherwise psi returns to the block's start and dt halves (floor 1e-8).
+// The NaN / DDI-overflow guard runs once, after the very first step (:193).  The
+// backup of psi stays on the device (slot A); _rebuild_workspace_with_dt (:380-392) is
+// a new dt for the ITP kinetic phase.
+sbec_status sbec_ground_state_adaptive(sbec_ws* ws, int64_t n_steps, double tol, double dt_max,
+                                       sbec_gs_result* out, double* final_dt) {
+  SBEC_API_BEGIN
+  EngineBase& e = E(ws);
+  if (!e.itp || e.normalize_every != 1)
+    fail(SBEC_ERR_INVALID, "sbec_ground_state_adaptive needs an imaginary-time workspace with normalize_every=1");
+  if (n_steps <= 0) fail(SBEC_ERR_INVALID, "n_steps must be positive");
+  if (!(dt_max > 0)) fail(SBEC_ERR_INVALID, "dt_max must be positive");
+  const int64_t check_every = std::max<int64_t>(1, n_steps / 100);
+  auto set_dt = [&](double dt) {
+    e.dt = dt;
+    ws->kin_dt = dt;
+    ws->kin_itp = true;
+  };
+  double current_dt = e.dt;
+  double E_prev = total_energy(e);
+  bool converged = false;
+  int64_t total = 0;
+  double final_dE = NAN, final_dpsi = NAN;
+  while (total < n_steps) {
+    e.copy_slot(kSlotA, kPsi);
+    if (total == 0) {
+      split_steps(ws, 1);
+      check_itp_overflow(e, 1);
+      if (check_every > 1) split_steps(ws, check_every - 1);
+    } else {
+      split_steps(ws, check_every);
+    }
+    total += check_every;
+    const double En = total_energy(e);
+    if (std::isnan(En) || En > E_prev) {
+      e.copy_slot(kPsi, kSlotA);
+      current_dt = std::max(current_dt * 0.5, 1e-8);
+      set_dt(current_dt);
+    } else {
+      const double dE = std::fabs(En - E_prev);
+      double pmax = 0, dmax = 0;
+      e.max_abs(kPsi, kSlotA, &pmax, &dmax);
+      const double dpsi = pmax > 0 ? dmax / pmax : 0.0;
+      final_dE = dE;
+      final_dpsi = dpsi;
+      if (dE < tol && dpsi < tol) {
+        converged = true;
+        break;
+      }
+      E_prev = En;
+      const double new_dt = std::min(current_dt * 1.1, dt_max);
+      if (new_dt != current_dt) {
+        current_dt = new_dt;
+        set_dt(current_dt);
+      }
+    }
+  }
+  const double Efin = total_energy(e);
+  if (out) {
+    out->converged = converged ? 1 : 0;
+    out->energy = Efin;
+    out->dE = final_dE;
+    out->dpsi = final_dpsi;
+    out->steps = total;
+  }
+  if (final_dt) *final_dt = current_dt;
+  SBEC_API_END
+}
+
 sbec_status sbec_total_energy(sbec_ws* ws, double* Eout) {
   SBEC_API_BEGIN
   need(Eout, "E");
@@ -816,6 +932,13 @@ sbec_status sbec_ddi_potential(sbec_ws* ws, int32_t padded, double* out) {
   SBEC_API_END
 }
 
+sbec_status sbec_classify_phase(sbec_ws* ws, sbec_phase_info* out) {
+  SBEC_API_BEGIN
+  need(out, "out");
+  classify_phase(E(ws), -1, out);
+  SBEC_API_END
+}
+
 // ---- batches of independent ITP solves (find_ground_state per solve, one schedule)
 sbec_status sbec_batch_create(const sbec_config* cfg, int32_t n_solves, const double* c0, const double* c1,
                               const double* psi, const double* V, sbec_batch** out) {
@@ -857,6 +980,15 @@ sbec_status sbec_batch_get_psi(sbec_batch* b, int32_t solve, double* psi) {
   need(b, "batch");
   need(psi, "psi");
   b->eng->batch_get_psi(solve, psi);
+  SBEC_API_END
+}
+
+sbec_status sbec_batch_classify_phase(sbec_batch* b, int32_t solve, sbec_phase_info* out) {
+  SBEC_API_BEGIN
+  need(b, "batch");
+  need(out, "out");
+  if (solve < 0 || solve >= b->eng->n_solves()) fail(SBEC_ERR_INVALID, "solve index out of range");
+  classify_phase(*b->eng, solve, out);
   SBEC_API_END
 }
 
@@ -997,6 +1129,42 @@ sbec_status sbec_set_graph_mode(sbec_ws* ws, int32_t graphs) {
 sbec_status sbec_tuning_report(sbec_ws* ws, char* buf, int64_t cap, int64_t* len) {
   SBEC_API_BEGIN
   copy_report(E(ws).tuning_report(), buf, cap, len);
+  SBEC_API_END
+}
+
+sbec_status sbec_tune_table_export(char* buf, int64_t cap, int64_t* len) {
+  SBEC_API_BEGIN
+  std::string r;
+  {
+    std::lock_guard<std::mutex> lock(tune_table_mutex());
+    for (const auto& kv : tune_table_map()) r += kv.first + "\t" + std::to_string(kv.second) + "\n";
+  }
+  copy_report(r, buf, cap, len);
+  SBEC_API_END
+}
+
+sbec_status sbec_tune_table_import(const char* text) {
+  SBEC_API_BEGIN
+  need(text, "text");
+  std::map<std::string, int> add;
+  const std::string t(text);
+  size_t pos = 0;
+  while (pos < t.size()) {
+    size_t eol = t.find('\n', pos);
+    if (eol == std::string::npos) eol = t.size();
+    const std::string line = t.substr(pos, eol - pos);
+    pos = eol + 1;
+    if (line.empty()) continue;
+    const size_t tab = line.rfind('\t');
+    if (tab == std::string::npos || tab == 0) fail(SBEC_ERR_INVALID, "tune table line without a tab: " + line);
+    char* end = nullptr;
+    const long v = std::strtol(line.c_str() + tab + 1, &end, 10);
+    if (end == line.c_str() + tab + 1 || *end != 0 || v < 0 || v > 255)
+      fail(SBEC_ERR_INVALID, "tune table line with a bad variant: " + line);
+    add[line.substr(0, tab)] = (int)v;
+  }
+  std::lock_guard<std::mutex> lock(tune_table_mutex());
+  for (const auto& kv : add) tune_table_map()[kv.first] = kv.second;
   SBEC_API_END
 }
 

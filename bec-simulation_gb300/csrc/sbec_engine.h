@@ -5,6 +5,7 @@
 
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -96,6 +97,9 @@ class Profiler {
   std::map<std::string, Stat> stats_;
 };
 
+// Grid sums of classify_phase: n, n^2, |<F>|^2, m|psi|^2 and F_max + 1 = 7 channel weights.
+constexpr int kPhaseSums = 11;
+
 // Buffers a driver can save psi into (adaptive loops, convergence checks).
 enum Slot { kPsi = 0, kSlotA = 1, kSlotB = 2, kSlotC = 3, kNumSlots = 4 };
 
@@ -141,6 +145,9 @@ class EngineBase {
   virtual void max_abs(int a, int b, double* max_a, double* max_diff) = 0;
   virtual double ddi_phi_max() = 0;                                // last periodic Φ (ITP check)
   virtual void spin_density(double* host3N) = 0;
+  // classify_phase grid sums (k_phase_sums): [n, n^2, |<F>|^2, m|psi|^2, W_0, W_2, ..., W_2F]
+  // of the workspace psi (solve < 0) or of one solve of a batch; kPhaseSums doubles.
+  virtual void phase_sums(int solve, double* out) = 0;
   virtual void ddi_potential(bool padded, double* host3N) = 0;
   virtual void sync() = 0;
 
@@ -177,6 +184,11 @@ class EngineBase {
   Setup s_;
   cudaStream_t stream_ = nullptr;
 };
+
+// Process-wide autotuner decisions (line-kernel call shape -> variant), shared by both
+// precisions and every workspace and batch; guarded by tune_table_mutex().
+std::mutex& tune_table_mutex();
+std::map<std::string, int>& tune_table_map();
 
 std::unique_ptr<EngineBase> make_engine_f64(const Setup& s);
 std::unique_ptr<EngineBase> make_engine_f32(const Setup& s);

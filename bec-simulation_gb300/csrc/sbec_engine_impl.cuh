@@ -534,6 +534,41 @@ class Engine final : public EngineBase {
     download_real3(out, host3N);
   }
 
+  void phase_sums(int solve, double* out) override {
+    const cplx<R>* src = psi_[kPsi];
+    if (solve >= 0) {
+      if (!bpsi_ || solve >= nsolve_) fail(SBEC_ERR_INVALID, "solve index out of range");
+      src = bpsi_ + (size_t)solve * nc_;
+    }
+    if (!phase_pairs_) {
+      // pair table of every even channel S <= 2F: rows (S/2, (S,M) index, c1, c2) and CG
+      std::vector<int4> rows;
+      std::vector<double> cgs;
+      const int F = s_.F;
+      int a = 0;
+      for (int S = 0; S <= 2 * F; S += 2)
+        for (int M = -S; M <= S; ++M, ++a)
+          for (int m1 = -F; m1 <= F; ++m1) {
+            const int m2 = M - m1;
+            if (m2 < -F || m2 > F) continue;
+            const double cg = clebsch_gordan(F, m1, F, m2, S, M);
+            if (std::fabs(cg) < 1e-15) continue;
+            rows.push_back(make_int4(S / 2, a, F - m1, F - m2));
+            cgs.push_back(cg);
+          }
+      n_phase_pairs_ = (int)rows.size();
+      phase_pairs_ = alloc<int4>(std::max<size_t>(rows.size(), 1));
+      phase_cg_ = alloc<double>(std::max<size_t>(cgs.size(), 1));
+      upload(phase_pairs_, rows.data(), rows.size());
+      upload(phase_cg_, cgs.data(), cgs.size());
+    }
+    const int nb = red_blocks(N_);
+    SBEC_SWITCH_D(s_.D, launch_phase_sums_d, src, nb);
+    finish<kPhaseSums>(nb, false, 0);
+    fetch(kPhaseSums);
+    for (int k = 0; k < kPhaseSums; ++k) out[k] = host_res_[k];
+  }
+
   void ddi_potential(bool padded, double* host3N) override {
     if (!s_.ddi) fail(SBEC_ERR_INVALID, "DDI is not enabled on this workspace");
     if (padded && !s_.padded) fail(SBEC_ERR_INVALID, "zero-padded DDI is not enabled on this workspace");
@@ -1298,14 +1333,8 @@ class Engine final : public EngineBase {
   // fresh copy (of 8 back-to-back launches for data up to 32 MB).  The fastest is kept in a table shared by all workspaces of the
   // process, so every solve of one shape runs the same kernels (the variants agree
   // to FP32 rounding, not bit for bit).
-  static std::mutex& tune_mutex() {
-    static std::mutex m;
-    return m;
-  }
-  static std::map<std::string, int>& tune_table() {
-    static std::map<std::string, int> t;
-    return t;
-  }
+  static std::mutex& tune_mutex() { return tune_table_mutex(); }
+  static std::map<std::string, int>& tune_table() { return tune_table_map(); }
 
   bool capturing() const {
     cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
@@ -1342,7 +1371,10 @@ class Engine final : public EngineBase {
     if (mine != tuned_.end()) return mine->second;
     std::lock_guard<std::mutex> lock(tune_mutex());
     auto it = tune_table().find(key);
-    if (it != tune_table().end()) return tuned_[key] = it->second;
+    if (it != tune_table().end() && std::find(cands.begin(), cands.end(), it->second) != cands.end()) {
+      tune_log_.push_back(key + " -> v" + std::to_string(it->second) + " (from the process table)");
+      return tuned_[key] = it->second;
+    }
     if (capturing()) return 0;  // never reached: shapes are first met in an eager run
     if (extent > tune_buf_n_) {
       tune_buf_ = alloc<cplx<R>>(extent);
@@ -1838,6 +1870,14 @@ class Engine final : public EngineBase {
   }
 
   template <int D>
+  void launch_phase_sums_d(const cplx<R>* buf, int nb) {
+    pb();
+    k_phase_sums<R, D><<<nb, kRedThreads, 0, stream_>>>(buf, N_, st_, phase_pairs_, phase_cg_, n_phase_pairs_,
+                                                       partials_);
+    done("reduce", (double)sizeof(cplx<R>) * D * (double)N_);
+  }
+
+  template <int D>
   void launch_comp_norms_d(const cplx<R>* buf, int nb) {
     pb();
     k_comp_norms<R, D><<<nb, kRedThreads, 0, stream_>>>(buf, N_, partials_);
@@ -1878,6 +1918,9 @@ class Engine final : public EngineBase {
   SpinTabs<R> st_;
   double* G_ = nullptr;
   int4* pairs_ = nullptr;
+  int4* phase_pairs_ = nullptr;  // classify_phase pair table (built on first use)
+  double* phase_cg_ = nullptr;
+  int n_phase_pairs_ = 0;
   double* pcg_ = nullptr;
   double* gA_ = nullptr;
   R* spin3_ = nullptr;

@@ -1666,6 +1666,71 @@ __global__ void __launch_bounds__(kRedThreads) k_tensor_energy(const cplx<R>* __
   block_reduce_store<1>(acc, partials, false);
 }
 
+// Order parameters of classify_phase (src/diagnostics.jl:166-206) as grid sums in FP64:
+// out[0] = sum n, [1] = sum n^2, [2] = sum |<F>|^2, [3] = sum_m m |psi_m|^2 and
+// [4 + S/2] = sum_M sum_x |A_SM|^2 for every even S <= 2F (pair_amplitude_spectrum,
+// src/observables.jl:118-142,227-246).  Pair table rows (S/2, a = (S,M) index, c1, c2)
+// sorted by a, with CG(F,m1;F,m2|S,M) in pcg (|CG| < 1e-15 dropped).
+template <typename R, int D>
+__global__ void __launch_bounds__(kRedThreads) k_phase_sums(const cplx<R>* __restrict__ psi, int64_t N,
+                                                            SpinTabs<R> st, const int4* __restrict__ pairs,
+                                                            const double* __restrict__ pcg, int n_pairs,
+                                                            double* partials) {
+  double acc[kPhaseSums];
+#pragma unroll
+  for (int k = 0; k < kPhaseSums; ++k) acc[k] = 0.0;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (int64_t)gridDim.x * blockDim.x) {
+    double2 v[D];
+    double n = 0.0, fz = 0.0, fre = 0.0, fim = 0.0;
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      const cplx<R> z = psi[c * N + p];
+      v[c] = make_double2((double)z.x, (double)z.y);
+      const double a2 = v[c].x * v[c].x + v[c].y * v[c].y;
+      n += a2;
+      fz += (double)st.m[c] * a2;
+      if (c >= 1) {
+        fre += (double)st.fp[c] * (v[c - 1].x * v[c].x + v[c - 1].y * v[c].y);
+        fim += (double)st.fp[c] * (v[c - 1].x * v[c].y - v[c - 1].y * v[c].x);
+      }
+    }
+    acc[0] += n;
+    acc[1] += n * n;
+    acc[2] += fre * fre + fim * fim + fz * fz;
+    acc[3] += fz;
+    int cur = -1, cur_s = 0;
+    double2 A = make_double2(0.0, 0.0);
+    double w[kPhaseSums - 4];
+#pragma unroll
+    for (int s = 0; s < kPhaseSums - 4; ++s) w[s] = 0.0;
+    for (int q = 0; q < n_pairs; ++q) {
+      const int4 pr = __ldg(pairs + q);
+      if (pr.y != cur) {
+        if (cur >= 0) {
+#pragma unroll
+          for (int s = 0; s < kPhaseSums - 4; ++s)
+            if (s == cur_s) w[s] += A.x * A.x + A.y * A.y;
+        }
+        cur = pr.y;
+        cur_s = pr.x;
+        A = make_double2(0.0, 0.0);
+      }
+      const double cg = __ldg(pcg + q);
+      const double2 a = v[pr.z], b = v[pr.w];
+      A.x += cg * (a.x * b.x - a.y * b.y);
+      A.y += cg * (a.x * b.y + a.y * b.x);
+    }
+    if (cur >= 0) {
+#pragma unroll
+      for (int s = 0; s < kPhaseSums - 4; ++s)
+        if (s == cur_s) w[s] += A.x * A.x + A.y * A.y;
+    }
+#pragma unroll
+    for (int s = 0; s < kPhaseSums - 4; ++s) acc[4 + s] += w[s];
+  }
+  block_reduce_store<kPhaseSums>(acc, partials, false);
+}
+
 // Kinetic energy sum_k k^2 |psi_hat_c(k)|^2 over all components of a transformed buffer.
 template <typename R>
 __global__ void __launch_bounds__(kRedThreads) k_kinetic_sum(const cplx<R>* __restrict__ a, int64_t N, int D,

@@ -113,6 +113,10 @@ extern "C" sbec_status sbec_component_norms_noalloc(const double* psi_dev, int64
                                  " (the fixed scratch holds one slot per component)");
     if (n_points > SBEC_NOALLOC_MAX_POINTS)
       fail(SBEC_ERR_INVALID, "n_points exceeds SBEC_NOALLOC_MAX_POINTS (" + std::to_string(SBEC_NOALLOC_MAX_POINTS) + ")");
+    // psi is read as complex doubles (16-byte loads); a view at an odd double offset would fault
+    if ((reinterpret_cast<uintptr_t>(psi_dev) & 15) != 0)
+      fail(SBEC_ERR_INVALID, "psi_dev must be 16-byte aligned (whole complex Float64 entries)");
+    if ((reinterpret_cast<uintptr_t>(sums_dev) & 7) != 0) fail(SBEC_ERR_INVALID, "sums_dev must be 8-byte aligned");
     double* part = scratch_for_current_device();
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int64_t want = (n_points + kNaThreads - 1) / kNaThreads;

@@ -1,4 +1,6 @@
 // Persistent 2-D leapfrog segments (FP32): the cooperative launch of k_lf_segment.
+#include <mutex>
+
 #include "sbec_lines_impl.cuh"
 
 namespace sbec {
@@ -10,16 +12,29 @@ void seg_launch(const LineCtx<float>& c, const Tw<float>& twx, const Tw<float>& 
                 long long n_steps, GridBarrier* bar) {
   using Sh = SegShape<float, NN, NN, D, 0>;
   auto kern = k_lf_segment<float, NN, NN, D, 0>;
-  // resident blocks of the whole GPU: a cooperative launch may not exceed them
-  static const int resident = [&] {
-    line_set_smem(kern, Sh::smem_bytes);
-    int dev = 0, sms = 0, occ = 0;
-    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
-    cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
-    cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, Sh::T, Sh::smem_bytes),
-               "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
-    return sms * occ;
-  }();
+  // resident blocks of the whole GPU: a cooperative launch may not exceed them.  The
+  // shared-memory attribute and the occupancy are per device, so they are kept per device
+  // ordinal and set up the first time a segment runs on that device.
+  constexpr int kMaxDev = 64;
+  static std::mutex mu;
+  static int resident_of[kMaxDev] = {};
+  int dev = 0;
+  cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDev) fail(SBEC_ERR_UNSUPPORTED, "device ordinal beyond the segment table");
+  int resident = 0;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (resident_of[dev] == 0) {
+      line_set_smem(kern, Sh::smem_bytes);
+      int sms = 0, occ = 0;
+      cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
+      cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, Sh::T, Sh::smem_bytes),
+                 "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+      resident_of[dev] = std::max(sms * occ, -1);
+      if (resident_of[dev] == 0) resident_of[dev] = -1;
+    }
+    resident = resident_of[dev];
+  }
   if (resident < 1) fail(SBEC_ERR_UNSUPPORTED, "segment kernel does not fit on an SM");
   const int row_units = (int)((a.n_rows + Sh::RPB - 1) / Sh::RPB);
   const int col_units = (NN + Sh::W - 1) / Sh::W * D;

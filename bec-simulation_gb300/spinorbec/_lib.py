@@ -105,6 +105,16 @@ class sbec_energy_terms(C.Structure):
     _fields_ = [(k, C.c_double) for k in ("kinetic", "trap", "zeeman", "c0", "c1", "ddi", "lhy", "tensor")]
 
 
+class sbec_phase_info(C.Structure):
+    _fields_ = [("spin_order", C.c_double), ("nematic_order", C.c_double), ("magnetization_density", C.c_double),
+                ("phase", C.c_int32), ("n_channels", C.c_int32),
+                ("channel_weights", C.c_double * SBEC_MAX_CHANNELS),
+                ("raw_channel_weights", C.c_double * SBEC_MAX_CHANNELS)]
+
+
+PHASE_LABELS = ("vacuum", "ferromagnetic", "polar", "nematic", "cyclic", "mixed")
+
+
 class sbec_kernel_stat(C.Structure):
     _fields_ = [("name", C.c_char * 32), ("launches", C.c_int64), ("ms", C.c_double), ("bytes", C.c_double)]
 
@@ -140,12 +150,15 @@ _PROTOS = {
     "sbec_run_yoshida": (C.c_int, [_P, C.POINTER(sbec_adaptive_params), C.c_double, C.c_double, C.c_int64,
                                    CALLBACK, C.c_void_p, C.POINTER(sbec_adaptive_result)]),
     "sbec_ground_state": (C.c_int, [_P, C.c_int64, C.c_double, C.c_int64, C.c_double, C.POINTER(sbec_gs_result)]),
+    "sbec_ground_state_adaptive": (C.c_int, [_P, C.c_int64, C.c_double, C.c_double, C.POINTER(sbec_gs_result), _D]),
     "sbec_total_energy": (C.c_int, [_P, _D]),
     "sbec_energy_breakdown": (C.c_int, [_P, C.POINTER(sbec_energy_terms)]),
     "sbec_total_norm": (C.c_int, [_P, _D]),
     "sbec_magnetization": (C.c_int, [_P, _D]),
     "sbec_spin_density": (C.c_int, [_P, _D]),
     "sbec_ddi_potential": (C.c_int, [_P, C.c_int32, _D]),
+    "sbec_classify_phase": (C.c_int, [_P, C.POINTER(sbec_phase_info)]),
+    "sbec_batch_classify_phase": (C.c_int, [_P, C.c_int32, C.POINTER(sbec_phase_info)]),
     "sbec_profile_enable": (C.c_int, [_P, C.c_int32]),
     "sbec_profile_read": (C.c_int, [_P, C.POINTER(sbec_kernel_stat), C.c_int32, C.POINTER(C.c_int32)]),
     "sbec_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
@@ -154,6 +167,8 @@ _PROTOS = {
     "sbec_set_graph_mode": (C.c_int, [_P, C.c_int32]),
     "sbec_tuning_report": (C.c_int, [_P, C.c_char_p, C.c_int64, C.POINTER(C.c_int64)]),
     "sbec_batch_tuning_report": (C.c_int, [_P, C.c_char_p, C.c_int64, C.POINTER(C.c_int64)]),
+    "sbec_tune_table_export": (C.c_int, [C.c_char_p, C.c_int64, C.POINTER(C.c_int64)]),
+    "sbec_tune_table_import": (C.c_int, [C.c_char_p]),
     "sbec_batch_create": (C.c_int, [C.POINTER(sbec_config), C.c_int32, _D, _D, _D, _D, C.POINTER(_P)]),
     "sbec_batch_destroy": (C.c_int, [_P]),
     "sbec_batch_ground_state": (C.c_int, [_P, C.c_int64, C.c_double, C.c_int64, C.POINTER(sbec_gs_result)]),

@@ -290,6 +290,23 @@ def ddi_potential(ws: Workspace, padded: bool = False):
     return tuple(out[i * n:(i + 1) * n].reshape(shp, order="F") for i in range(3))
 
 
+def _phase_dict(info) -> dict:
+    nch = int(info.n_channels)
+    return dict(spin_order=info.spin_order, nematic_order=info.nematic_order,
+                channel_weights={2 * k: info.channel_weights[k] for k in range(nch)} if info.phase else {},
+                phase=_lib.PHASE_LABELS[info.phase], magnetization_density=info.magnetization_density,
+                raw_channel_weights={2 * k: info.raw_channel_weights[k] for k in range(nch)})
+
+
+def classify_phase(ws: Workspace) -> dict:
+    """``classify_phase`` (src/diagnostics.jl:166-206) of the device-resident psi: spin order,
+    nematic order, normalised pair-channel weights, the phase label and Mz/N, reduced on the
+    device in FP64 (no psi round trip)."""
+    info = _lib.sbec_phase_info()
+    check(ws._lib.sbec_classify_phase(ws.handle, C.byref(info)))
+    return _phase_dict(info)
+
+
 # ---- drivers -------------------------------------------------------------------
 
 class _SnapshotStore:
@@ -475,65 +492,93 @@ def find_ground_state(*, grid: Grid, atom: AtomSpecies, interactions: Interactio
 
 def _find_ground_state_adaptive(grid, atom, interactions, zeeman, potential, dt, n_steps, tol, psi0, enable_ddi,
                                 c_dd, secular_ddi, dt_max, precision, graphs=True):
-    """``_find_ground_state_adaptive`` (src/ground_state.jl:172-237): host loop over device blocks."""
-    current_dt = dt
+    """``_find_ground_state_adaptive`` (src/ground_state.jl:172-237), run by the library's
+    driver (sbec_ground_state_adaptive): the backup of psi stays on the device, and the
+    NaN / DDI-overflow guard after the first step raises NumericError as the reference
+    raises ArgumentError."""
     check_every = max(1, n_steps // 100)
-    sp = SimParams(current_dt, check_every, True, 1, check_every)
+    sp = SimParams(dt, check_every, True, 1, check_every)
     ws = make_workspace(grid=grid, atom=atom, interactions=interactions, zeeman=zeeman, potential=potential,
                         sim_params=sp, psi_init=psi0, enable_ddi=enable_ddi, c_dd=c_dd, secular_ddi=secular_ddi,
                         precision=precision, graphs=graphs)
-    E_prev = total_energy(ws)
-    converged = False
-    total = 0
-    final_dE = final_dpsi = float("nan")
-    while total < n_steps:
-        backup = ws.psi
-        split_step(ws, check_every)
-        total += check_every
-        E = total_energy(ws)
-        if math.isnan(E) or E > E_prev:
-            ws.psi = backup
-            current_dt = max(current_dt * 0.5, 1e-8)
-            ws.set_dt(current_dt)
-        else:
-            psi = ws.psi
-            dE = abs(E - E_prev)
-            pmax = float(np.max(np.abs(psi)))
-            dpsi = float(np.max(np.abs(psi - backup))) / pmax if pmax > 0 else 0.0
-            final_dE, final_dpsi = dE, dpsi
-            if dE < tol and dpsi < tol:
-                converged = True
-                break
-            E_prev = E
-            new_dt = min(current_dt * 1.1, dt_max)
-            if new_dt != current_dt:
-                current_dt = new_dt
-                ws.set_dt(current_dt)
-    return dict(workspace=ws, converged=converged, energy=total_energy(ws), dE=final_dE, dpsi=final_dpsi,
-                steps=total)
+    r = _lib.sbec_gs_result()
+    final_dt = C.c_double()
+    check(ws._lib.sbec_ground_state_adaptive(ws.handle, int(n_steps), float(tol), float(dt_max), C.byref(r),
+                                             C.byref(final_dt)))
+    ws.sim_params = SimParams(final_dt.value, sp.n_steps, True, sp.normalize_every, sp.save_every)
+    return dict(workspace=ws, converged=bool(r.converged), energy=r.energy, dE=r.dE, dpsi=r.dpsi, steps=r.steps,
+                final_dt=final_dt.value)
+
+
+def _batch_eligible(atom: AtomSpecies, interactions: InteractionParams, kw: dict) -> bool:
+    """Whether every start of a multistart search can run as one GroundStateBatch: the batch
+    takes contact couplings (c0, c1, c_lhy) with a static Zeeman term and the plain
+    find_ground_state loop (no DDI, adaptive dt or magnetisation constraint)."""
+    if atom.F > 2 or any(abs(float(v)) > 1e-30 for v in interactions.c_extra):
+        return False
+    if kw.get("enable_ddi") or kw.get("adaptive_dt") or kw.get("target_magnetization") is not None:
+        return False
+    if callable(kw.get("zeeman")) or kw.get("psi_init") is not None:
+        return False
+    return True
 
 
 def find_ground_state_multistart(*, initial_states=("polar", "ferromagnetic", "uniform", "antiferromagnetic"),
-                                 n_random: int = 3, seed: int = 42, grid, atom, interactions, **kw) -> dict:
-    """``find_ground_state_multistart`` (src/ground_state.jl:239-277); random seeds are seed+i."""
-    results = []
+                                 n_random: int = 3, seed: int = 42, grid, atom, interactions, batched=None,
+                                 **kw) -> dict:
+    """``find_ground_state_multistart`` (src/ground_state.jl:239-277); random seeds are seed+i.
+
+    batched=None (default) runs all starts as one GroundStateBatch when they are eligible
+    (contact couplings, static Zeeman, plain ITP loop); each solve follows find_ground_state's
+    loop and convergence test, so the results are those of the one-at-a-time loop.  Only the
+    lowest-energy start gets a workspace (rebuilt from its psi); every entry of all_results
+    carries its psi."""
+    starts = []
     for state in initial_states:
         if state == "random":
             for i in range(1, n_random + 1):
-                psi0 = init_psi(grid, atom.F, "random", seed=seed + i)
-                r = find_ground_state(grid=grid, atom=atom, interactions=interactions, psi_init=psi0, **kw)
-                results.append(dict(initial_state="random", idx=i, **r))
+                starts.append(("random", i, init_psi(grid, atom.F, "random", seed=seed + i)))
         else:
-            r = find_ground_state(grid=grid, atom=atom, interactions=interactions, initial_state=state, **kw)
-            results.append(dict(initial_state=state, idx=0, **r))
-    best = min(results, key=lambda r: r["energy"])
+            starts.append((state, 0, init_psi(grid, atom.F, state)))
+    use_batch = _batch_eligible(atom, interactions, kw) if batched is None else bool(batched)
+    if use_batch and len(starts) > 1:
+        dt = kw.get("dt", 0.001)
+        zeeman = ZeemanParams() if kw.get("zeeman") is None else kw["zeeman"]
+        for _, _, p0 in starts:
+            _validate_itp(zeeman, interactions, atom.F, dt, p0, 0.0)
+        b = GroundStateBatch(grid=grid, atom=atom, c0s=[interactions.c0] * len(starts),
+                             c1s=[interactions.c1] * len(starts), psi_inits=[p for _, _, p in starts],
+                             zeeman=zeeman, potential=kw.get("potential"), dt=dt, c_lhy=interactions.c_lhy,
+                             precision=kw.get("precision", "fp64"))
+        n_steps = kw.get("n_steps", 10000)
+        res = b.ground_state(n_steps, kw.get("tol", 1e-10))
+        results = []
+        for (state, idx, _), r in zip(starts, res):
+            results.append(dict(initial_state=state, idx=idx, workspace=None, psi=None, **r))
+        ib = min(range(len(results)), key=lambda i: results[i]["energy"])
+        for i, r in enumerate(results):
+            r["psi"] = b.psi(i)
+        b.close()
+        best = results[ib]
+        sp = SimParams(dt, n_steps, True, 1, max(1, n_steps // 10))
+        best["workspace"] = make_workspace(grid=grid, atom=atom, interactions=interactions, zeeman=zeeman,
+                                           potential=kw.get("potential"), sim_params=sp, psi_init=best["psi"],
+                                           precision=kw.get("precision", "fp64"), graphs=kw.get("graphs", True))
+    else:
+        results = []
+        for state, idx, p0 in starts:
+            r = find_ground_state(grid=grid, atom=atom, interactions=interactions, psi_init=p0, **kw)
+            results.append(dict(initial_state=state, idx=idx, **r))
+        best = min(results, key=lambda r: r["energy"])
     return dict(workspace=best["workspace"], converged=best["converged"], energy=best["energy"],
                 initial_state=best["initial_state"], all_results=results)
 
 
 def scan_continuation(*, param_values, make_interactions: Callable, grid, atom, initial_state="polar",
                       energy_jump_threshold=0.1, n_steps_continuation=500, n_steps_fresh=5000, **kw) -> list:
-    """``scan_continuation`` (src/ground_state.jl:328-378), phase classification left to the caller."""
+    """``scan_continuation`` (src/ground_state.jl:328-378): each point warm-starts from the
+    previous ground state, an energy jump above the threshold falls back to a multistart search
+    (batched when eligible), and each point is labelled by ``classify_phase`` on the device."""
     results = []
     prev_psi = None
     prev_E = float("nan")
@@ -545,10 +590,17 @@ def scan_continuation(*, param_values, make_interactions: Callable, grid, atom, 
         else:
             r = find_ground_state(grid=grid, atom=atom, interactions=inter, initial_state=initial_state,
                                   n_steps=n_steps_fresh, **kw)
+        multistart = False
         if not math.isnan(prev_E) and abs(r["energy"] - prev_E) / max(abs(prev_E), 1e-30) > energy_jump_threshold:
+            r["workspace"].close()
             r = find_ground_state_multistart(grid=grid, atom=atom, interactions=inter, n_steps=n_steps_fresh, **kw)
-        psi = r["workspace"].psi
-        results.append(dict(param=val, energy=r["energy"], converged=r["converged"], psi=psi))
+            multistart = True
+        ws = r["workspace"]
+        phase = classify_phase(ws)["phase"]
+        psi = ws.psi
+        results.append(dict(param=val, energy=r["energy"], converged=r["converged"], phase=phase, psi=psi,
+                            multistart=multistart))
+        ws.close()
         prev_psi = psi
         prev_E = r["energy"]
     return results
@@ -629,9 +681,31 @@ class GroundStateBatch:
         check(self._lib.sbec_batch_energies(self._h, dptr(E)))
         return E
 
+    def classify_phase(self, i: int) -> dict:
+        """``classify_phase`` (src/diagnostics.jl:166-206) of solve i, reduced on the device."""
+        info = _lib.sbec_phase_info()
+        check(self._lib.sbec_batch_classify_phase(self._h, int(i), C.byref(info)))
+        return _phase_dict(info)
+
     @property
     def tuning_report(self) -> str:
         return _report(self._lib.sbec_batch_tuning_report, self._h)
+
+
+def tune_table_export() -> str:
+    """The autotuner's process-wide decisions (shape<TAB>variant lines), for saving."""
+    lib = load()
+    n = C.c_int64()
+    check(lib.sbec_tune_table_export(None, 0, C.byref(n)))
+    buf = C.create_string_buffer(n.value + 1)
+    check(lib.sbec_tune_table_export(buf, n.value + 1, C.byref(n)))
+    return buf.value.decode()
+
+
+def tune_table_import(text: str) -> None:
+    """Load saved autotuner decisions: shapes found there are not timed again, so FP32 results
+    are the same in every process that loads the same table."""
+    check(load().sbec_tune_table_import(text.encode()))
 
 
 def _report(fn, handle) -> str:

@@ -173,6 +173,13 @@ sbec_status sbec_run_yoshida(sbec_ws* ws, const sbec_adaptive_params* p, double 
  * convergence checked every check_every steps; target_Mz = NaN disables the constraint. */
 sbec_status sbec_ground_state(sbec_ws* ws, int64_t n_steps, double tol, int64_t check_every,
                               double target_Mz, sbec_gs_result* out);
+/* _find_ground_state_adaptive (src/ground_state.jl:172-237) on an existing ITP workspace with
+ * normalize_every = 1: blocks of max(1, n_steps/100) steps; a block whose energy rose (or is NaN)
+ * is undone and dt halves (floor 1e-8), otherwise dt grows by 10 % up to dt_max.  The NaN /
+ * DDI-overflow guard runs after the first step (SBEC_ERR_NUMERIC).  *final_dt receives the dt
+ * the workspace ends with (may be NULL). */
+sbec_status sbec_ground_state_adaptive(sbec_ws* ws, int64_t n_steps, double tol, double dt_max,
+                                       sbec_gs_result* out, double* final_dt);
 
 /* ---- reductions --------------------------------------------------------- */
 /* total_energy (src/energy.jl:6-54) and its terms. */
@@ -186,6 +193,28 @@ sbec_status sbec_spin_density(sbec_ws* ws, double* out);
 /* Dipolar potential (Φx, Φy, Φz) on the grid for the current psi (src/ddi.jl:108-163,
  * src/ddi_padded.jl:55-85); padded selects the zero-padded convolution. */
 sbec_status sbec_ddi_potential(sbec_ws* ws, int32_t padded, double* out);
+
+/* classify_phase (src/diagnostics.jl:166-206) on the device-resident psi: FP64 grid sums of
+ * n, n^2, |<F>|^2, m|psi_m|^2 and the pair-amplitude channel weights sum_M int |A_SM|^2 dV
+ * (pair_amplitude_spectrum, src/observables.jl:227-246), then the reference's labelling. */
+typedef enum sbec_phase_label {
+  SBEC_PHASE_VACUUM = 0,
+  SBEC_PHASE_FERROMAGNETIC = 1,
+  SBEC_PHASE_POLAR = 2,
+  SBEC_PHASE_NEMATIC = 3,
+  SBEC_PHASE_CYCLIC = 4,
+  SBEC_PHASE_MIXED = 5
+} sbec_phase_label;
+typedef struct sbec_phase_info {
+  double spin_order;             /* int |<F>|^2 / (F^2 int n^2) */
+  double nematic_order;          /* W_0 / (int n^2 / (2F+1)) */
+  double magnetization_density;  /* Mz / N */
+  int32_t phase;                 /* sbec_phase_label */
+  int32_t n_channels;            /* F + 1: S = 0, 2, ..., 2F */
+  double channel_weights[SBEC_MAX_CHANNELS];  /* W_S / sum W, index S/2 */
+  double raw_channel_weights[SBEC_MAX_CHANNELS];  /* W_S = sum_M int |A_SM|^2 dV */
+} sbec_phase_info;
+sbec_status sbec_classify_phase(sbec_ws* ws, sbec_phase_info* out);
 
 /* ---- batches of independent ground-state solves ---------------------------
  * The multistart / continuation / phase-boundary callers of find_ground_state
@@ -203,6 +232,8 @@ sbec_status sbec_batch_ground_state(sbec_batch* b, int64_t n_steps, double tol, 
                                     sbec_gs_result* out);
 sbec_status sbec_batch_get_psi(sbec_batch* b, int32_t solve, double* psi);
 sbec_status sbec_batch_energies(sbec_batch* b, double* E);
+/* classify_phase of one solve of the batch (as sbec_classify_phase). */
+sbec_status sbec_batch_classify_phase(sbec_batch* b, int32_t solve, sbec_phase_info* out);
 
 /* ---- tracing (the reference's @timeit_debug substep timers, src/split_step.jl:15-131) ---- */
 typedef struct sbec_kernel_stat {
@@ -235,6 +266,15 @@ sbec_status sbec_set_graph_mode(sbec_ws* ws, int32_t graphs);
  * counterpart in the reference (FFTW plans are chosen inside FFTW). */
 sbec_status sbec_tuning_report(sbec_ws* ws, char* buf, int64_t cap, int64_t* len);
 sbec_status sbec_batch_tuning_report(sbec_batch* b, char* buf, int64_t cap, int64_t* len);
+/* The autotuner's process-wide decisions as text, one "shape<TAB>variant" line each; *len
+ * receives the full length.  No counterpart in the reference. */
+sbec_status sbec_tune_table_export(char* buf, int64_t cap, int64_t* len);
+/* Loads decisions in the export format.  A shape found in the table is never timed again, so
+ * processes that load the same table run the same line kernels and give bit-identical FP32
+ * results; without it, the variant of a shape is the fastest in a timing of this process, and
+ * FP32 results may differ between processes at the level of FP32 rounding.  Entries whose
+ * variant is not compiled for a shape are ignored there.  No counterpart in the reference. */
+sbec_status sbec_tune_table_import(const char* text);
 
 /* ---- allocation-free reduction --------------------------------------------
  * No counterpart in the reference: an extra entry point for callers that cannot
@@ -252,7 +292,8 @@ sbec_status sbec_batch_tuning_report(sbec_batch* b, char* buf, int64_t cap, int6
  * array's address (no allocation, but make it before any stream capture).  All
  * calls on a device share the array: calls whose kernels overlap on the GPU race.
  * Limits: 1 <= n_components <= SBEC_NOALLOC_MAX_COMPONENTS,
- * 1 <= n_points <= SBEC_NOALLOC_MAX_POINTS; otherwise SBEC_ERR_INVALID. */
+ * 1 <= n_points <= SBEC_NOALLOC_MAX_POINTS, psi_dev 16-byte aligned (whole complex
+ * entries) and sums_dev 8-byte aligned; otherwise SBEC_ERR_INVALID. */
 #define SBEC_NOALLOC_MAX_COMPONENTS 16
 #define SBEC_NOALLOC_MAX_POINTS (1LL << 31)
 sbec_status sbec_component_norms_noalloc(const double* psi_dev, int64_t n_points, int32_t n_components,

@@ -1320,6 +1320,69 @@ def magnetization(psi: np.ndarray, grid: Grid, F: int) -> float:
     return Mz
 
 
+def pair_amplitude(psi: np.ndarray, F: int, S: int, M: int, cg_table: dict) -> np.ndarray:
+    """``pair_amplitude`` (src/observables.jl:118-142):
+    A_SM = sum_m1 CG(F,m1;F,M-m1|S,M) psi_m1 psi_(M-m1), pairs with |CG| < 1e-15 skipped."""
+    A = np.zeros(psi.shape[:-1], dtype=np.complex128)
+    for m1 in range(-F, F + 1):
+        m2 = M - m1
+        if abs(m2) > F:
+            continue
+        cg = cg_table.get((S, M, m1, m2), 0.0)
+        if abs(cg) < 1e-15:
+            continue
+        A = A + cg * psi[..., F - m1] * psi[..., F - m2]
+    return A
+
+
+def pair_amplitude_spectrum(psi: np.ndarray, F: int, grid: Grid) -> dict:
+    """``pair_amplitude_spectrum`` (src/observables.jl:227-246): (S, M) -> int |A_SM|^2 dV and
+    S -> sum over M, for every even S <= 2F."""
+    cg_table = precompute_cg_table(F)
+    dV = cell_volume(grid)
+    amplitudes, weights = {}, {}
+    for S in range(0, 2 * F + 1, 2):
+        w = 0.0
+        for M in range(-S, S + 1):
+            val = float(np.sum(np.abs(pair_amplitude(psi, F, S, M, cg_table)) ** 2)) * dV
+            amplitudes[(S, M)] = val
+            w += val
+        weights[S] = w
+    return dict(amplitudes=amplitudes, channel_weights=weights)
+
+
+def classify_phase(psi: np.ndarray, F: int, grid: Grid) -> dict:
+    """``classify_phase`` (src/diagnostics.jl:166-206): spin order |<F>|^2 / (F^2 n^2), nematic
+    order (S = 0 pair weight over n^2 / D), normalised channel weights, the phase label and
+    Mz / N.  Thresholds 0.9 / 0.9 / 0.5 and the label order are the reference's."""
+    D = 2 * F + 1
+    dV = cell_volume(grid)
+    n = total_density(psi)
+    n_sum = float(np.sum(n)) * dV
+    n_sq_sum = float(np.sum(n ** 2)) * dV
+    if n_sum < 1e-30:
+        return dict(spin_order=0.0, nematic_order=0.0, channel_weights={}, phase="vacuum",
+                    magnetization_density=0.0)
+    fx, fy, fz = spin_density(psi, F)
+    f_sq = float(np.sum(fx ** 2 + fy ** 2 + fz ** 2)) * dV
+    spin_order = f_sq / (float(F) ** 2 * n_sq_sum)
+    spec = pair_amplitude_spectrum(psi, F, grid)
+    total_w = sum(spec["channel_weights"].values())
+    cw = {S: (w / total_w if total_w > 0 else 0.0) for S, w in spec["channel_weights"].items()}
+    nematic_order = spec["channel_weights"].get(0, 0.0) / (n_sq_sum / D)
+    Mz = magnetization(psi, grid, F) / n_sum
+    if spin_order > 0.9:
+        phase = "ferromagnetic"
+    elif nematic_order > 0.9:
+        phase = "polar" if F == 1 else "nematic"
+    elif cw.get(2 * F, 0.0) > 0.5:
+        phase = "cyclic"
+    else:
+        phase = "mixed"
+    return dict(spin_order=spin_order, nematic_order=nematic_order, channel_weights=cw, phase=phase,
+                magnetization_density=Mz)
+
+
 def energy_terms(ws: Workspace) -> dict:
     """The terms of ``total_energy`` (src/energy.jl:6-135)."""
     psi = ws.psi
@@ -1824,7 +1887,7 @@ def _find_ground_state_adaptive(*, grid, atom, interactions, zeeman, V, dt, n_st
                 current_dt = new_dt
                 _rebuild_with_dt(ws, current_dt)
     return dict(workspace=ws, converged=converged, energy=total_energy(ws), dE=final_dE,
-                dpsi=final_dpsi, steps=total_steps)
+                dpsi=final_dpsi, steps=total_steps, final_dt=current_dt)
 
 
 def _rebuild_with_dt(ws: Workspace, new_dt: float) -> None:
@@ -1854,7 +1917,8 @@ def find_ground_state_multistart(*, initial_states=("polar", "ferromagnetic", "u
 
 def scan_continuation(*, param_values, make_interactions: Callable, grid, atom, initial_state="polar",
                       energy_jump_threshold=0.1, n_steps_continuation=500, n_steps_fresh=5000, **kw) -> list:
-    """``scan_continuation`` (src/ground_state.jl:328-378) without ``classify_phase``."""
+    """``scan_continuation`` (src/ground_state.jl:328-378), each point labelled by
+    ``classify_phase`` (:363)."""
     results = []
     prev_psi = None
     prev_E = float("nan")
@@ -1869,7 +1933,9 @@ def scan_continuation(*, param_values, make_interactions: Callable, grid, atom, 
         if not math.isnan(prev_E) and abs(r["energy"] - prev_E) / max(abs(prev_E), 1e-30) > energy_jump_threshold:
             r = find_ground_state_multistart(grid=grid, atom=atom, interactions=inter, n_steps=n_steps_fresh, **kw)
         psi = r["workspace"].psi
-        results.append(dict(param=val, energy=r["energy"], converged=r["converged"], psi=psi.copy(order="F")))
+        phase = classify_phase(psi, atom.F, grid)["phase"]
+        results.append(dict(param=val, energy=r["energy"], converged=r["converged"], phase=phase,
+                            psi=psi.copy(order="F"), multistart=r.get("initial_state") is not None))
         prev_psi = psi.copy(order="F")
         prev_E = r["energy"]
     return results

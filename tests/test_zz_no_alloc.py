@@ -51,6 +51,19 @@ def test_noalloc_matches_workspace_on_two_calls(gpu):
         ws.close()
 
 
+def test_noalloc_counts_planted_nan(gpu):
+    """One NaN entry in psi: the component sums of the other entries are unaffected in the
+    NaN-free components and the NaN count slot reads 1."""
+    og = O.make_grid(O.GridConfig((32, 32), (10.0, 10.0)))
+    psi = O.init_psi(og, 1, "random", seed=3)
+    clean = _noalloc_sums(psi, 3)
+    psi[5, 7, 1] = complex(np.nan, 0.0)
+    sums = _noalloc_sums(psi, 3)
+    assert sums[3] == 1.0
+    assert sums[0] == clean[0] and sums[2] == clean[2]
+    assert np.isnan(sums[1])
+
+
 def test_noalloc_rejects_sizes_beyond_limits(gpu):
     torch = pytest.importorskip("torch")
     buf = torch.zeros(64, dtype=torch.float64, device="cuda")
@@ -60,6 +73,11 @@ def test_noalloc_rejects_sizes_beyond_limits(gpu):
     with pytest.raises(S.ArgumentError):
         S._lib.check(st)
     st = lib.sbec_component_norms_noalloc(ctypes.c_void_p(buf.data_ptr()), (1 << 31) + 1, 3,
+                                          ctypes.c_void_p(buf.data_ptr()), None)
+    with pytest.raises(S.ArgumentError):
+        S._lib.check(st)
+    # psi at an odd double offset (a view that splits a complex entry) is refused
+    st = lib.sbec_component_norms_noalloc(ctypes.c_void_p(buf.data_ptr() + 8), 4, 3,
                                           ctypes.c_void_p(buf.data_ptr()), None)
     with pytest.raises(S.ArgumentError):
         S._lib.check(st)
