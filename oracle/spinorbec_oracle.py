@@ -896,9 +896,18 @@ def euler_spin_rotation(spinor: np.ndarray, phi_x, phi_y, phi_z, dt: float, sm: 
 
 def _rodrigues(spinor: np.ndarray, sm: SpinMatrices, c1: float, dt_frac: float,
                imaginary_time: bool) -> np.ndarray:
-    """``_apply_rodrigues_rotation`` (src/spin_mixing.jl:71-98), vectorised over points."""
+    """``_apply_rodrigues_rotation`` (src/spin_mixing.jl:71-98), vectorised over points: the
+    same U = I - i sin(θ) n·F + (cos θ - 1)(n·F)^2 (sinh / cosh in imaginary time) built
+    entry by entry, then U ψ."""
     Fs = (sm.Fx, sm.Fy, sm.Fz)
-    f = [np.real(np.einsum("pi,ij,pj->p", spinor.conj(), Fm, spinor)) for Fm in Fs]
+    sc = spinor.conj()
+    f = []
+    for Fm in Fs:
+        acc = np.zeros(spinor.shape[0], dtype=np.complex128)
+        for i in range(3):
+            row = Fm[i, 0] * spinor[:, 0] + Fm[i, 1] * spinor[:, 1] + Fm[i, 2] * spinor[:, 2]
+            acc = acc + sc[:, i] * row
+        f.append(acc.real)
     fx, fy, fz = f
     f_mag = np.sqrt(fx ** 2 + fy ** 2 + fz ** 2)
     out = spinor.copy()
@@ -906,15 +915,21 @@ def _rodrigues(spinor: np.ndarray, sm: SpinMatrices, c1: float, dt_frac: float,
     if not np.any(act):
         return out
     fx, fy, fz, fm, s = fx[act], fy[act], fz[act], f_mag[act], spinor[act]
-    nF = (fx[:, None, None] * sm.Fx + fy[:, None, None] * sm.Fy + fz[:, None, None] * sm.Fz) / fm[:, None, None]
-    nF2 = nF @ nF
+    nF = [[(fx * sm.Fx[i, j] + fy * sm.Fy[i, j] + fz * sm.Fz[i, j]) / fm for j in range(3)] for i in range(3)]
+    nF2 = [[nF[i][0] * nF[0][k] + nF[i][1] * nF[1][k] + nF[i][2] * nF[2][k] for k in range(3)] for i in range(3)]
     theta = c1 * fm * dt_frac
-    eye = np.eye(3, dtype=np.complex128)
     if imaginary_time:
-        U = eye - np.sinh(theta)[:, None, None] * nF + (np.cosh(theta) - 1)[:, None, None] * nF2
+        a, b = -np.sinh(theta), np.cosh(theta) - 1
     else:
-        U = eye - 1j * np.sin(theta)[:, None, None] * nF + (np.cos(theta) - 1)[:, None, None] * nF2
-    out[act] = np.einsum("pij,pj->pi", U, s)
+        a, b = -1j * np.sin(theta), np.cos(theta) - 1
+    res = np.empty_like(s)
+    for i in range(3):
+        acc = np.zeros(s.shape[0], dtype=np.complex128)
+        for j in range(3):
+            U = (1.0 if i == j else 0.0) + a * nF[i][j] + b * nF2[i][j]
+            acc = acc + U * s[:, j]
+        res[:, i] = acc
+    out[act] = res
     return out
 
 
@@ -1126,11 +1141,17 @@ def apply_tensor_interaction_step(ws: Workspace, dt: float, imaginary_time: bool
         return
     s = flat[act]
     P = s.shape[0]
-    h = np.zeros((P, D, D), dtype=np.complex128)
-    coef = g[ch] * cgp
-    sc = np.conj(s)
-    for e in range(len(cgp)):
-        h[:, cm[e], cmp[e]] += coef[e] * sc[:, cmu[e]] * s[:, cnu[e]]
+    # h[m, m'] = sum_e coef_e conj(psi_mu) psi_nu over the HFEntry terms e targeting (m, m'):
+    # one product matrix (conj(psi_mu) psi_nu for every (mu, nu)) times a fixed (D^2 x D^2)
+    # coefficient map, the same sum as the reference's entry loop in another order.
+    W = getattr(cache, "_h_map", None)
+    if W is None:
+        W = np.zeros((D * D, D * D))
+        coef = g[ch] * cgp
+        np.add.at(W, (cmu * D + cnu, cm * D + cmp), coef)
+        cache._h_map = W
+    prod = (np.conj(s)[:, :, None] * s[:, None, :]).reshape(P, D * D)
+    h = (prod @ W).reshape(P, D, D)
     vals, vecs = np.linalg.eigh(h, UPLO="U")
     proj = np.einsum("pjk,pj->pk", vecs.conj(), s)
     if imaginary_time:

@@ -129,3 +129,17 @@ def test_raman_and_loss_options_are_unsupported_before_device():
         S.make_workspace(raman=Raman(1.0, 0.0, (0.0,)), **kw)
     with pytest.raises(S.UnsupportedError, match="losses"):
         S.make_workspace(loss=Loss(0.1, 0.0), **kw)
+
+
+def test_tune_table_import_export(libsbec):
+    """The autotuner's process table round-trips through its text form (host only), and a
+    malformed line is refused with SBEC_ERR_INVALID."""
+    import spinorbec as S
+
+    S.tune_table_import("fp32 test-shape D=3 grid=8x8x1 solves=1\t5\n")
+    text = S.tune_table_export()
+    assert "fp32 test-shape D=3 grid=8x8x1 solves=1\t5\n" in text
+    with pytest.raises(S.ArgumentError):
+        S.tune_table_import("no tab here\n")
+    with pytest.raises(S.ArgumentError):
+        S.tune_table_import("shape\tx\n")
