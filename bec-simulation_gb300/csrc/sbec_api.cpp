@@ -112,6 +112,7 @@ void split_step_once(sbec_ws* ws) {
   e.half_potential(dt / 2, it);
   e.kinetic(ws->kin_dt, ws->kin_itp);
   e.half_potential(dt / 2, it);
+  if (!it) e.apply_loss(dt);  // src/split_step.jl:21-23
   e.t += it ? 0.0 : dt;
   e.step += 1;
   if (it && e.normalize_every > 0 && e.step % e.normalize_every == 0) e.normalize();
@@ -166,7 +167,7 @@ void yoshida_core(sbec_ws* ws, double dt) {
 
 double total_energy(EngineBase& e) {
   const sbec_energy_terms t = e.energy_terms();
-  return t.kinetic + t.trap + t.zeeman + t.c0 + t.c1 + t.ddi + t.lhy + t.tensor;
+  return t.kinetic + t.trap + t.zeeman + t.c0 + t.c1 + t.ddi + t.lhy + t.tensor + t.raman;
 }
 
 void norm_and_mz(EngineBase& e, double* norm, double* mz) {
@@ -193,7 +194,7 @@ int snapshot(sbec_ws* ws, sbec_callback cb, void* user) {
   const Setup& s = e.setup();
   std::vector<double> sums(s.D);
   const sbec_energy_terms t = e.energy_terms_and_norms(sums.data());
-  sn.energy = t.kinetic + t.trap + t.zeeman + t.c0 + t.c1 + t.ddi + t.lhy + t.tensor;
+  sn.energy = t.kinetic + t.trap + t.zeeman + t.c0 + t.c1 + t.ddi + t.lhy + t.tensor + t.raman;
   double n = 0.0, m = 0.0;
   for (int c = 0; c < s.D; ++c) {
     n += sums[c];
@@ -229,7 +230,7 @@ void run_leapfrog_pipelined(sbec_ws* ws, int64_t n_steps, int64_t save_every, sb
     sn.psi = e.snapshot_wait(k, &t, sums.data());
     sn.t = meta[k & 1].t;
     sn.step = meta[k & 1].step;
-    sn.energy = t.kinetic + t.trap + t.zeeman + t.c0 + t.c1 + t.ddi + t.lhy + t.tensor;
+    sn.energy = t.kinetic + t.trap + t.zeeman + t.c0 + t.c1 + t.ddi + t.lhy + t.tensor + t.raman;
     double n = 0.0, m = 0.0;
     for (int c = 0; c < s.D; ++c) {
       n += sums[c];
@@ -574,6 +575,7 @@ sbec_status sbec_run_simulation(sbec_ws* ws, int64_t n_steps, int64_t save_every
       e.unfused_lf_steps(nseg - 1, dt, ws->kin_dt, ws->kin_itp);
       e.kinetic(ws->kin_dt, ws->kin_itp);
       e.half_potential(dt / 2, false);
+      e.apply_loss(dt);  // src/simulation.jl:74-76
       for (int64_t i = 0; i < nseg; ++i) {
         e.t += dt;
         e.step += 1;
@@ -641,6 +643,7 @@ sbec_status sbec_run_adaptive(sbec_ws* ws, const sbec_adaptive_params* p, double
       }
       fsal_deferred = true;
       fsal_dt = dt_step;
+      e.apply_loss(dt_step);  // src/adaptive.jl:151-153
       e.t += dt_step;
       e.step += 1;
       ++n_acc;
@@ -686,6 +689,7 @@ sbec_status sbec_run_adaptive(sbec_ws* ws, const sbec_adaptive_params* p, double
         ++n_rej;
         continue;
       }
+      e.apply_loss(dt_step);  // src/adaptive.jl:262-264
       e.t += dt_step;
       e.step += 1;
       ++n_acc;
@@ -740,6 +744,7 @@ sbec_status sbec_run_yoshida(sbec_ws* ws, const sbec_adaptive_params* p, double 
       ++n_rej;
       continue;
     }
+    e.apply_loss(dt_step);  // src/yoshida.jl:64-66
     e.t += dt_step;
     e.step += 1;
     ++n_acc;
@@ -951,8 +956,10 @@ sbec_status sbec_batch_create(const sbec_config* cfg, int32_t n_solves, const do
   *out = nullptr;
   if (!cfg->imaginary_time || cfg->normalize_every != 1)
     fail(SBEC_ERR_INVALID, "batched ground states need imaginary_time=1 and normalize_every=1");
-  if (cfg->n_c_extra != 0 || cfg->gS_direct || cfg->enable_ddi)
-    fail(SBEC_ERR_UNSUPPORTED, "batched ground states support contact c0/c1 (+LHY) couplings without DDI");
+  if (cfg->n_c_extra != 0 || cfg->gS_direct || cfg->enable_ddi || cfg->raman ||
+      !(cfg->loss_gamma_dr < 1e-30 && cfg->loss_L3 < 1e-30))
+    fail(SBEC_ERR_UNSUPPORTED,
+         "batched ground states support contact c0/c1 (+LHY) couplings without DDI, Raman or losses");
   Setup s = build_setup(*cfg);
   if (sbec_device_count() < 1) fail(SBEC_ERR_DEVICE, "no CUDA device available (the GPU path has no CPU fallback)");
   auto b = std::make_unique<sbec_batch>();

@@ -126,6 +126,7 @@ class EngineBase {
   virtual void half_potential(double dt_half, bool imaginary_time) = 0;
   virtual void kinetic(double dt, bool imaginary_time) = 0;
   virtual void normalize() = 0;                         // device-side _normalize_psi!
+  virtual void apply_loss(double dt) = 0;               // apply_loss_step! (no-op without losses)
   virtual void scale_components(const double* w) = 0;   // host weights, D values
   virtual void copy_slot(int dst, int src) = 0;
 

@@ -227,6 +227,35 @@ class Engine final : public EngineBase {
     PotArgs<R> a = pot_args(tau_d, imaginary_time);
     a.tau_s = (R)tau_s;
     a.tau_ddi = (R)dt_half;
+    a.tau_r = (R)(dt_half / 2);
+    const int rm = s_.raman ? 1 : 0;
+    if (s_.tensor && rm) {
+      // tensor(tau/2), Raman(tau/2), [DDI(tau)], Raman(tau/2), tensor(tau/2) (src/split_step.jl:58-131)
+      TensorArgs<R> ta = tensor_args(tau_d, tau_s, imaginary_time);
+      ta.pre_diag = 1;
+      ta.post_diag = 0;
+      ta.n_apply = 1;
+      launch_tensor(ta);
+      PotArgs<R> r1 = a;
+      r1.raman_a = 1;
+      if (s_.ddi) {
+        r1.spin_out = spin3_;
+        launch_potential(r1);
+        ddi_conv(s_.padded ? 1 : 0, spin3_, phi3_);
+        PotArgs<R> r2 = a;
+        r2.ddi_rot = 1;
+        r2.phi = phi3_;
+        r2.raman_b = 1;
+        launch_potential(r2);
+      } else {
+        r1.raman_b = 1;
+        launch_potential(r1);
+      }
+      ta.pre_diag = 0;
+      ta.post_diag = 1;
+      launch_tensor(ta);
+      return;
+    }
     if (s_.tensor) {
       TensorArgs<R> ta = tensor_args(tau_d, tau_s, imaginary_time);
       ta.pre_diag = 1;
@@ -255,6 +284,7 @@ class Engine final : public EngineBase {
       a.pre_diag = 1;
       a.rot_a = sm;
       a.nem_a = a.nem_b = nematic();
+      a.raman_a = a.raman_b = rm;
       a.rot_b = sm;
       a.post_diag = 1;
       launch_potential(a);
@@ -264,16 +294,26 @@ class Engine final : public EngineBase {
     first.pre_diag = 1;
     first.rot_a = sm;
     first.nem_a = nematic();
+    first.raman_a = rm;
     first.spin_out = spin3_;
     launch_potential(first);
     ddi_conv(s_.padded ? 1 : 0, spin3_, phi3_);
     PotArgs<R> second = a;
     second.ddi_rot = 1;
     second.phi = phi3_;
+    second.raman_b = rm;
     second.nem_b = nematic();
     second.rot_b = sm;
     second.post_diag = 1;
     launch_potential(second);
+  }
+
+  // apply_loss_step! (src/losses.jl:25-45) for a step of dt; no-op without losses.
+  void apply_loss(double dt) override {
+    if (!s_.loss) return;
+    LossRates<R> lr{};
+    for (int c = 0; c < s_.D; ++c) lr.r[c] = (R)s_.loss_rates[c];
+    SBEC_SWITCH_D(s_.D, launch_loss_d, lr, (R)(dt / 2));
   }
 
   void kinetic(double dt_k, bool imaginary_time) override {
@@ -458,6 +498,11 @@ class Engine final : public EngineBase {
       SBEC_SWITCH_D(s_.D, launch_pair_energy_d, nb);
       finish<1>(nb, false, 29);
     }
+    if (s_.raman) {
+      const int nb = red_blocks(N_);
+      SBEC_SWITCH_D(s_.D, launch_raman_energy_d, nb);
+      finish<1>(nb, false, 24);
+    }
     if (s_.ddi) {
       SBEC_SWITCH_D(s_.D, launch_spin_density_d, spin3_);
       ddi_conv(0, spin3_, phi_per_);
@@ -491,6 +536,7 @@ class Engine final : public EngineBase {
     if (s_.c_lhy != 0.0) e.lhy = (2.0 / 5.0) * s_.c_lhy * res[23] * dV;
     if (s_.tensor) e.tensor = res[30] * dV;
     if (nematic()) e.tensor = 0.5 * s_.c2 * res[29] * dV;  // _nematic_energy (src/energy.jl:106-109)
+    if (s_.raman) e.raman = res[24] * dV;                    // _raman_energy (src/energy.jl:123-135)
     if (comp_sums)
       for (int c = 0; c < s_.D; ++c) comp_sums[c] = res[1 + c];
     return e;
@@ -579,7 +625,7 @@ class Engine final : public EngineBase {
 
   // ---------------- fused paths ----------------
   bool fused_path() const override {
-    if (s_.ddi || s_.tensor) return false;
+    if (s_.ddi || s_.tensor || s_.raman || s_.loss) return false;
     if (!(s_.D == 1 || s_.D == 3 || s_.D == 5)) return false;
     const int nx = s_.n[0];
     if (nx < 16 || nx > 4096) return false;
@@ -775,6 +821,7 @@ class Engine final : public EngineBase {
       half_potential(dtv / 2, it);
       kinetic(kin_dt, kin_itp);
       half_potential(dtv / 2, it);
+      if (!it) apply_loss(dtv);  // src/split_step.jl:21-23
       if (normalize) this->normalize();
     });
   }
@@ -783,6 +830,7 @@ class Engine final : public EngineBase {
     graph_chunks(6, n, dtv, kin_dt, kin_itp, kin_itp ? 1 : 0, [&] {
       kinetic(kin_dt, kin_itp);
       half_potential(dtv, false);
+      apply_loss(dtv);  // src/simulation.jl:74-76
     });
   }
 
@@ -1761,7 +1809,22 @@ class Engine final : public EngineBase {
     a.c_lhy = (R)s_.c_lhy;
     a.c2 = (R)s_.c2;
     zeeman_factors(tau_d, it, a.zee, a.zee_lo);
+    a.rg = raman_geom();
     return a;
+  }
+
+  RamanGeom raman_geom() const {
+    RamanGeom g{};
+    g.omega = s_.raman_omega;
+    g.delta = s_.raman_delta;
+    for (int d = 0; d < 3; ++d) {
+      g.k[d] = s_.raman_k[d];
+      g.x0[d] = s_.x0[d];
+      g.dx[d] = s_.dx[d];
+    }
+    g.n0 = s_.n[0];
+    g.n1 = s_.n[1];
+    return g;
   }
 
   // Zeeman factors (src/propagators.jl:95-116): cis(-E_c tau) or exp(-(E_c - min E) tau).
@@ -1866,6 +1929,20 @@ class Engine final : public EngineBase {
     pb();
     k_tensor_energy<R, D><<<nb, kRedThreads, 0, stream_>>>(psi_[kPsi], N_, pairs_, pcg_, (int)s_.pair_a.size(), gA_,
                                                           (int)s_.gA.size(), partials_);
+    done("reduce", (double)sizeof(cplx<R>) * D * (double)N_);
+  }
+
+  template <int D>
+  void launch_loss_d(LossRates<R> lr, R half_dt) {
+    pb();
+    k_loss<R, D><<<(unsigned)((N_ + 255) / 256), 256, 0, stream_>>>(psi_[kPsi], N_, lr, half_dt);
+    done("loss", 2.0 * (double)sizeof(cplx<R>) * D * (double)N_);
+  }
+
+  template <int D>
+  void launch_raman_energy_d(int nb) {
+    pb();
+    k_raman_energy<R, D><<<nb, kRedThreads, 0, stream_>>>(psi_[kPsi], N_, st_, raman_geom(), partials_);
     done("reduce", (double)sizeof(cplx<R>) * D * (double)N_);
   }
 

@@ -480,6 +480,29 @@ struct SpinTabs {
   R m[kMaxD];                  // m_c = F - c
 };
 
+// Raman coupling H_R(r) = delta Fz + (Omega/2)(e^{ik.r} F+ + e^{-ik.r} F-) (src/raman.jl:1-31).
+// With F+- = Fx +- iFy this is b(r)·F, b = (Omega cos k.r, -Omega sin k.r, delta), so its
+// exponential is a spin rotation about b(r) (the reference exponentiates the same Hermitian
+// matrix by eigen-decomposition, src/spinor_utils.jl:27-38).  Grid coordinates
+// x_d = x0_d + i_d dx_d (src/grid.jl:2-7), point index p = i0 + n0 (i1 + n1 i2).
+struct RamanGeom {
+  double omega, delta;
+  double k[3], x0[3], dx[3];
+  int n0, n1;
+};
+
+__device__ __forceinline__ void raman_field(const RamanGeom& g, int64_t p, double& bx, double& by, double& bz) {
+  const int64_t i0 = p % g.n0, r = p / g.n0;
+  const int64_t i1 = r % g.n1, i2 = r / g.n1;
+  const double kr = g.k[0] * (g.x0[0] + (double)i0 * g.dx[0]) + g.k[1] * (g.x0[1] + (double)i1 * g.dx[1]) +
+                    g.k[2] * (g.x0[2] + (double)i2 * g.dx[2]);
+  double sn, cs;
+  sincos(kr, &sn, &cs);
+  bx = g.omega * cs;
+  by = -g.omega * sn;
+  bz = g.delta;
+}
+
 template <typename R>
 struct PotArgs {
   cplx<R>* psi;
@@ -494,6 +517,10 @@ struct PotArgs {
   R c0, c1, c_lhy, c2;
   cplx<R> zee[kMaxD];          // per-component Zeeman factor for diag(tau_d)
   cplx<R> zee_lo[kMaxD];       // FP32 tails of the Zeeman factors
+  // Raman rotation exp(-i tau_r b(r)·F) after nem_a (raman_a) / before nem_b (raman_b)
+  int raman_a, raman_b;
+  R tau_r;
+  RamanGeom rg;
 };
 
 // Upper bound of the Taylor sub-steps of one exponential (rotation or tensor step):
@@ -941,9 +968,13 @@ __global__ void __launch_bounds__(256) k_potential(PotArgs<R> a, SpinTabs<R> st)
   if (a.pre_diag) diag_point<R, D>(v, Vp, a, a.c0);
   if (a.rot_a) spin_mixing_point<R, D>(v, a.c1, a.tau_s, a.itp, st);
   if (a.nem_a) nematic_point<R, D>(v, a.c2, a.tau_s, a.itp);
+  double bx = 0, by = 0, bz = 0;
+  if (a.raman_a | a.raman_b) raman_field(a.rg, p, bx, by, bz);
+  if (a.raman_a) spin_rotate<R, D>(v, (R)bx, (R)by, (R)bz, a.tau_r, a.itp, st);
   if (a.ddi_rot) {
     spin_rotate<R, D>(v, a.phi[p], a.phi[a.N + p], a.phi[2 * a.N + p], a.tau_ddi, a.itp, st);
   }
+  if (a.raman_b) spin_rotate<R, D>(v, (R)bx, (R)by, (R)bz, a.tau_r, a.itp, st);
   if (a.nem_b) nematic_point<R, D>(v, a.c2, a.tau_s, a.itp);
   if (a.rot_b) spin_mixing_point<R, D>(v, a.c1, a.tau_s, a.itp, st);
   if (a.post_diag) diag_point<R, D>(v, Vp, a, a.c0);
@@ -1516,6 +1547,31 @@ __global__ void __launch_bounds__(256) k_spin_density(const cplx<R>* __restrict_
   out[2 * N + p] = fz;
 }
 
+// Density-dependent loss (src/losses.jl:25-45): psi_c *= exp(-rate_c n dt/2) with n the total
+// density before the step; components with rate_c < 1e-30 are left as they are.
+template <typename R>
+struct LossRates {
+  R r[kMaxD];
+};
+template <typename R, int D>
+__global__ void __launch_bounds__(256) k_loss(cplx<R>* __restrict__ psi, int64_t N, LossRates<R> rates, R half_dt) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= N) return;
+  cplx<R> v[D];
+  R n = 0;
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    v[c] = psi[c * N + p];
+    n += v[c].x * v[c].x + v[c].y * v[c].y;
+  }
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    if (!(rates.r[c] >= (R)1e-30)) continue;
+    const R f = exp(-rates.r[c] * n * half_dt);
+    psi[c * N + p] = mk<R>(v[c].x * f, v[c].y * f);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Reductions: per-block partial results (double), then a fixed-order finish.
 // ---------------------------------------------------------------------------
@@ -1729,6 +1785,32 @@ __global__ void __launch_bounds__(kRedThreads) k_phase_sums(const cplx<R>* __res
     for (int s = 0; s < kPhaseSums - 4; ++s) acc[4 + s] += w[s];
   }
   block_reduce_store<kPhaseSums>(acc, partials, false);
+}
+
+// Raman energy sum_x Re(psi^dagger H_R psi) = sum_x b(x)·<F>(x) (src/energy.jl:123-135), FP64.
+template <typename R, int D>
+__global__ void __launch_bounds__(kRedThreads) k_raman_energy(const cplx<R>* __restrict__ psi, int64_t N,
+                                                              SpinTabs<R> st, RamanGeom g, double* partials) {
+  double acc[1] = {0.0};
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (int64_t)gridDim.x * blockDim.x) {
+    double fz = 0.0, fre = 0.0, fim = 0.0;
+    double2 prev = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      const cplx<R> z0 = psi[c * N + p];
+      const double2 z = make_double2((double)z0.x, (double)z0.y);
+      fz += (double)st.m[c] * (z.x * z.x + z.y * z.y);
+      if (c >= 1) {
+        fre += (double)st.fp[c] * (prev.x * z.x + prev.y * z.y);
+        fim += (double)st.fp[c] * (prev.x * z.y - prev.y * z.x);
+      }
+      prev = z;
+    }
+    double bx, by, bz;
+    raman_field(g, p, bx, by, bz);
+    acc[0] += bx * fre + by * fim + bz * fz;
+  }
+  block_reduce_store<1>(acc, partials, false);
 }
 
 // Kinetic energy sum_k k^2 |psi_hat_c(k)|^2 over all components of a transformed buffer.

@@ -171,6 +171,7 @@ Setup build_setup(const sbec_config& cfg) {
   }
   s.dV = 1.0;
   for (int d = 0; d < s.ndim; ++d) s.dV *= s.dx[d];
+  for (int d = 0; d < s.ndim; ++d) s.x0[d] = -cfg.L[d] / 2 + s.dx[d] / 2;
   if (cfg.F < 0) fail(SBEC_ERR_INVALID, "F must be non-negative");
   if (cfg.F > 6) fail(SBEC_ERR_UNSUPPORTED, "spin F > 6 is not supported by the GPU path");
   s.F = cfg.F;
@@ -179,6 +180,40 @@ Setup build_setup(const sbec_config& cfg) {
   if (cfg.precision != SBEC_FP64 && cfg.precision != SBEC_FP32_BULK) fail(SBEC_ERR_INVALID, "unknown precision");
   if (cfg.n_c_extra < 0 || cfg.n_c_extra > SBEC_MAX_C_EXTRA) fail(SBEC_ERR_INVALID, "n_c_extra out of range");
   const int F = s.F, D = s.D;
+
+  // --- Raman coupling and losses
+  if (cfg.raman) {
+    if (!std::isfinite(cfg.raman_omega) || !std::isfinite(cfg.raman_delta))
+      fail(SBEC_ERR_INVALID, "Raman Omega_R and delta must be finite");
+    s.raman = true;
+    s.raman_omega = cfg.raman_omega;
+    s.raman_delta = cfg.raman_delta;
+    for (int d = 0; d < 3; ++d) s.raman_k[d] = d < s.ndim ? cfg.raman_k[d] : 0.0;
+  }
+  if (!(cfg.loss_gamma_dr < 1e-30 && cfg.loss_L3 < 1e-30)) {
+    // _dipolar_relaxation_rates (src/losses.jl:68-97): gamma_m = gamma_dr raw_m / (sum raw / D)
+    // with raw_m = sum over q in {-1,-2}, |m+q| <= F, of CG(F,m; 2,q | F,m+q)^2
+    std::vector<double> raw(D, 0.0);
+    double raw_sum = 0.0;
+    for (int c = 0; c < D; ++c) {
+      const int m = F - c;
+      double acc = 0.0;
+      for (int q : {-1, -2}) {
+        const int mp = m + q;
+        if (mp < -F || mp > F) continue;
+        const double cg = clebsch_gordan(F, m, 2, q, F, mp);
+        acc += cg * cg;
+      }
+      raw[c] = acc;
+      raw_sum += acc;
+    }
+    s.loss = true;
+    s.loss_rates.assign(D, 0.0);
+    for (int c = 0; c < D; ++c) {
+      const double g = raw_sum < 1e-30 ? 0.0 : cfg.loss_gamma_dr * raw[c] / (raw_sum / D);
+      s.loss_rates[c] = g + cfg.loss_L3;
+    }
+  }
 
   // --- interactions and tensor activation (src/initialization.jl:164-185)
   auto get_cn = [&](int k) -> double {

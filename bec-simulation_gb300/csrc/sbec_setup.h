@@ -41,6 +41,13 @@ struct Setup {
   // spin tables
   std::vector<std::complex<double>> FyV, FyVt;  // D*D row-major
   std::vector<double> fp, m;
+  // Raman coupling H_R = delta Fz + (Omega/2)(e^{ik.r} F+ + h.c.) (src/raman.jl:1-31)
+  bool raman = false;
+  double raman_omega = 0, raman_delta = 0, raman_k[3] = {0, 0, 0};
+  double x0[3] = {0, 0, 0};  // first grid coordinate per axis, -L/2 + dx/2 (src/grid.jl:2-7)
+  // density-dependent losses: rate_c = gamma_m + L3 per component (src/losses.jl:25-97)
+  bool loss = false;
+  std::vector<double> loss_rates;
   // DDI
   bool ddi = false, secular = false, padded = false;
   double c_dd = 0;

@@ -79,6 +79,12 @@ class sbec_config(C.Structure):
         ("imaginary_time", C.c_int32),
         ("normalize_every", C.c_int32),
         ("precision", C.c_int32),
+        ("raman", C.c_int32),
+        ("raman_omega", C.c_double),
+        ("raman_delta", C.c_double),
+        ("raman_k", C.c_double * 3),
+        ("loss_gamma_dr", C.c_double),
+        ("loss_L3", C.c_double),
     ]
 
 
@@ -102,7 +108,7 @@ class sbec_gs_result(C.Structure):
 
 
 class sbec_energy_terms(C.Structure):
-    _fields_ = [(k, C.c_double) for k in ("kinetic", "trap", "zeeman", "c0", "c1", "ddi", "lhy", "tensor")]
+    _fields_ = [(k, C.c_double) for k in ("kinetic", "trap", "zeeman", "c0", "c1", "ddi", "lhy", "tensor", "raman")]
 
 
 class sbec_phase_info(C.Structure):

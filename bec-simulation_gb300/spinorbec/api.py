@@ -151,13 +151,9 @@ def make_workspace(*, grid: Grid, atom: AtomSpecies, interactions: InteractionPa
                    raman=None, loss=None) -> Workspace:
     """``make_workspace`` (src/initialization.jl:86-191) with a device-resident state.
     graphs=False: the workspace launches every kernel eagerly (see Workspace.set_graph_mode).
-    ``raman`` and ``loss`` (the reference's RamanCoupling and LossParams) are not on the GPU
-    path: passing one raises UnsupportedError, as sbec_ws_create does for other options
-    outside it, so a caller can keep the CPU path for that run."""
-    if raman is not None:
-        raise _lib.UnsupportedError("Raman coupling (src/raman.jl) is not on the GPU path")
-    if loss is not None and (loss.gamma_dr >= 1e-30 or loss.L3 >= 1e-30):
-        raise _lib.UnsupportedError("density-dependent losses (src/losses.jl) are not on the GPU path")
+    ``raman`` (RamanCoupling: a per-point spin rotation inside the half potential,
+    src/raman.jl) and ``loss`` (LossParams: a pointwise decay after each real-time step,
+    src/losses.jl) run on the device."""
     lib = load()
     zeeman = ZeemanParams() if zeeman is None else zeeman
     if callable(zeeman):
@@ -197,6 +193,16 @@ def make_workspace(*, grid: Grid, atom: AtomSpecies, interactions: InteractionPa
     if precision not in PRECISIONS:
         raise _lib.ArgumentError(f"unknown precision {precision!r}")
     cfg.precision = PRECISIONS[precision]
+    if raman is not None:
+        k = tuple(float(v) for v in raman.k_eff)
+        if len(k) != nd:
+            raise _lib.ArgumentError("RamanCoupling.k_eff must have one entry per grid axis")
+        cfg.raman = 1
+        cfg.raman_omega, cfg.raman_delta = float(raman.Omega_R), float(raman.delta)
+        for d in range(nd):
+            cfg.raman_k[d] = k[d]
+    if loss is not None:
+        cfg.loss_gamma_dr, cfg.loss_L3 = float(loss.gamma_dr), float(loss.L3)
     psi = init_psi(grid, F) if psi_init is None else psi_init
     pbuf = to_interleaved(psi)
     if pbuf.size != 2 * int(np.prod(grid.config.n_points)) * (2 * F + 1):

@@ -130,6 +130,23 @@ class ZeemanParams:
 
 
 @dataclass
+class RamanCoupling:
+    """``RamanCoupling{N}(Omega_R, delta, k_eff)`` (src/types.jl:179-183)."""
+
+    Omega_R: float
+    delta: float
+    k_eff: tuple
+
+
+@dataclass
+class LossParams:
+    """``LossParams(gamma_dr, L3)`` (src/types.jl:291-296)."""
+
+    gamma_dr: float
+    L3: float = 0.0
+
+
+@dataclass
 class AtomSpecies:
     name: str
     F: int

@@ -34,7 +34,7 @@ extern "C" {
 typedef enum sbec_status {
   SBEC_OK = 0,
   SBEC_ERR_INVALID = 1,      /* invalid argument / configuration (ArgumentError in the reference) */
-  SBEC_ERR_UNSUPPORTED = 2,  /* option outside the GPU path (Raman, loss, non power-of-two n, F > 6) */
+  SBEC_ERR_UNSUPPORTED = 2,  /* option outside the GPU path (non power-of-two n, F > 6, ...) */
   SBEC_ERR_OOM = 3,          /* device allocation failed */
   SBEC_ERR_NUMERIC = 4,      /* NaN / ITP overflow detected (src/ground_state.jl:4-29) */
   SBEC_ERR_DEVICE = 5,       /* CUDA error or no device */
@@ -71,6 +71,10 @@ typedef struct sbec_config {
   int32_t imaginary_time;    /* SimParams.imaginary_time */
   int32_t normalize_every;   /* SimParams.normalize_every (ITP renormalisation period) */
   int32_t precision;         /* sbec_precision */
+  int32_t raman;             /* 1: RamanCoupling (src/types.jl:179-183) on the half potential */
+  double raman_omega, raman_delta;  /* Omega_R, delta */
+  double raman_k[3];         /* k_eff per axis */
+  double loss_gamma_dr, loss_L3;  /* LossParams (src/types.jl:291-296); both < 1e-30: no loss */
 } sbec_config;
 
 typedef struct sbec_ws sbec_ws;
@@ -104,8 +108,10 @@ typedef struct sbec_gs_result {
   int64_t steps;
 } sbec_gs_result;
 
+/* Terms of total_energy (src/energy.jl:6-54); `tensor` also carries the singlet-pair
+ * (nematic) energy of a c2 workspace, `raman` the Raman term (src/energy.jl:123-135). */
 typedef struct sbec_energy_terms {
-  double kinetic, trap, zeeman, c0, c1, ddi, lhy, tensor;
+  double kinetic, trap, zeeman, c0, c1, ddi, lhy, tensor, raman;
 } sbec_energy_terms;
 
 /* ---- diagnostics ------------------------------------------------------- */

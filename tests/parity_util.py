@@ -18,7 +18,9 @@ def rel_psi_err(a: np.ndarray, b: np.ndarray) -> float:
 
 def make_pair(n, L, F, c0=0.0, c1=0.0, *, omega=None, zeeman=(0.0, 0.0), dt=1e-3, itp=False, c_extra=(),
               c_lhy=0.0, ddi=False, c_dd=0.0, padded=False, secular=False, psi=None, seed=7,
-              precision="fp64", state="random", normalize_every=None, gS=None):
+              precision="fp64", state="random", normalize_every=None, gS=None, raman=None, loss=None):
+    """raman = (Omega_R, delta, k_eff), loss = (gamma_dr, L3): the same RamanCoupling /
+    LossParams on both sides."""
     n = tuple(n)
     L = tuple(L)
     og = O.make_grid(O.GridConfig(n, L))
@@ -30,12 +32,15 @@ def make_pair(n, L, F, c0=0.0, c1=0.0, *, omega=None, zeeman=(0.0, 0.0), dt=1e-3
     sp_h = S.SimParams(dt, 10, itp, normalize_every)
     ws_o = O.make_workspace(grid=og, atom=O.AtomSpecies("x", F), interactions=O.InteractionParams(c0, c1, c_lhy,
                             tuple(c_extra)), zeeman=O.ZeemanParams(*zeeman), V=V, sim_params=sp_o, psi_init=psi,
-                            enable_ddi=ddi, c_dd=c_dd, secular_ddi=secular, ddi_padding=padded)
+                            enable_ddi=ddi, c_dd=c_dd, secular_ddi=secular, ddi_padding=padded,
+                            raman=O.RamanCoupling(*raman) if raman else None,
+                            loss=O.LossParams(*loss) if loss else None)
     if gS is not None:
         ws_o.tensor_cache = O.make_tensor_cache_from_channels(F, gS)
         ws_o.interactions = O.InteractionParams(0.0, 0.0, c_lhy, ())
     ws_g = S.make_workspace(grid=hg, atom=S.AtomSpecies("x", F), interactions=S.InteractionParams(c0, c1, c_lhy,
                             tuple(c_extra)), zeeman=S.ZeemanParams(*zeeman), potential=V, sim_params=sp_h,
                             psi_init=psi, enable_ddi=ddi, c_dd=c_dd, secular_ddi=secular, ddi_padding=padded,
-                            precision=precision, gS=gS)
+                            precision=precision, gS=gS, raman=S.RamanCoupling(*raman) if raman else None,
+                            loss=S.LossParams(*loss) if loss else None)
     return ws_o, ws_g

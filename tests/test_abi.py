@@ -115,20 +115,20 @@ def test_itp_overflow_guards_before_device(case):
         S.find_ground_state(**kw)
 
 
-def test_raman_and_loss_options_are_unsupported_before_device():
-    """The reference's make_workspace options outside the GPU path raise UnsupportedError
-    before any device work; a loss with zero rates is the same as no loss."""
+def test_raman_and_loss_options_reach_the_library():
+    """RamanCoupling and LossParams are carried to sbec_ws_create (no UnsupportedError); a
+    k_eff of the wrong length is an ArgumentError before any device work, and on a host
+    without a GPU the workspace fails with DeviceError (no CPU fallback)."""
     import spinorbec as S
-    from collections import namedtuple
 
-    Loss = namedtuple("Loss", "gamma_dr L3")
-    Raman = namedtuple("Raman", "Omega_R delta k_eff")
     g = S.make_grid(S.GridConfig((32,), (10.0,)))
     kw = dict(grid=g, atom=S.Rb87, interactions=S.InteractionParams(1.0, 0.0), sim_params=S.SimParams(1e-3, 1))
-    with pytest.raises(S.UnsupportedError, match="Raman"):
-        S.make_workspace(raman=Raman(1.0, 0.0, (0.0,)), **kw)
-    with pytest.raises(S.UnsupportedError, match="losses"):
-        S.make_workspace(loss=Loss(0.1, 0.0), **kw)
+    with pytest.raises(S.ArgumentError, match="k_eff"):
+        S.make_workspace(raman=S.RamanCoupling(1.0, 0.0, (0.0, 1.0)), **kw)
+    if S.device_count() > 0:
+        pytest.skip("a GPU is visible: the no-device path is exercised only on CPU hosts")
+    with pytest.raises(S.DeviceError):
+        S.make_workspace(raman=S.RamanCoupling(1.0, 0.1, (2.0,)), loss=S.LossParams(0.1, 0.01), **kw)
 
 
 def test_tune_table_import_export(libsbec):
