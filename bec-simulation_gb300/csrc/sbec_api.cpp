@@ -42,6 +42,8 @@ struct sbec_ws {
   bool kin_itp = false;
   bool pipelined_snapshots = false;  // sbec_set_snapshot_mode
   std::vector<double> host_psi;
+  sbec_zeeman_fn zfn = nullptr;      // sbec_set_zeeman_fn (TimeDependentZeeman)
+  void* zuser = nullptr;
 };
 
 namespace {
@@ -93,6 +95,18 @@ EngineBase& E(sbec_ws* ws) {
 
 // ---- operator sequences shared by the drivers -----------------------------
 
+// zeeman_at(ws.zeeman, ws.state.t) (src/zeeman.jl:20-21) when a time-dependent Zeeman
+// function is set; a no-op for the static (p, q).
+void zee(sbec_ws* ws) {
+  if (!ws->zfn) return;
+  EngineBase& e = *ws->eng;
+  double p = e.zeeman_p, q = e.zeeman_q;
+  ws->zfn(ws->zuser, e.t, &p, &q);
+  if (!std::isfinite(p) || !std::isfinite(q)) fail(SBEC_ERR_INVALID, "Zeeman function returned a non-finite p or q");
+  e.zeeman_p = p;
+  e.zeeman_q = q;
+}
+
 void kinetic(sbec_ws* ws, double dt, bool itp) {
   ws->kin_dt = dt;
   ws->kin_itp = itp;
@@ -120,6 +134,14 @@ void split_step_once(sbec_ws* ws) {
 
 void split_steps(sbec_ws* ws, long long n) {
   EngineBase& e = *ws->eng;
+  if (ws->zfn) {
+    // the Zeeman factors change with t: one step at a time, launched eagerly
+    for (long long i = 0; i < n; ++i) {
+      zee(ws);
+      split_step_once(ws);
+    }
+    return;
+  }
   const bool it = e.itp;
   const bool norm_each = it && e.normalize_every == 1;
   const bool no_norm = !it || e.normalize_every <= 0;
@@ -144,6 +166,7 @@ void split_steps(sbec_ws* ws, long long n) {
 
 // _strang_core! (src/split_step.jl:146-152)
 void strang_core(sbec_ws* ws, double dt) {
+  zee(ws);
   ws->eng->half_potential(dt / 2, false);
   kinetic(ws, dt, false);
   ws->eng->half_potential(dt / 2, false);
@@ -156,6 +179,7 @@ const double kW0 = 1.0 - 2.0 * kW1;
 void yoshida_core(sbec_ws* ws, double dt) {
   const double w1 = kW1, w0 = kW0, wm = (w1 + w0) / 2;
   EngineBase& e = *ws->eng;
+  zee(ws);
   e.half_potential(w1 * dt / 2, false);
   kinetic(ws, w1 * dt, false);
   e.half_potential(wm * dt, false);
@@ -187,6 +211,7 @@ void norm_and_mz(EngineBase& e, double* norm, double* mz) {
 // _record_snapshot! (src/simulation_utils.jl:9-15) delivered to the callback.
 int snapshot(sbec_ws* ws, sbec_callback cb, void* user) {
   if (!cb) return 0;
+  zee(ws);  // total_energy evaluates zeeman_at(ws.zeeman, ws.state.t) (src/energy.jl:15)
   EngineBase& e = *ws->eng;
   sbec_snapshot sn{};
   sn.t = e.t;
@@ -446,6 +471,14 @@ sbec_status sbec_set_zeeman(sbec_ws* ws, double p, double q) {
   SBEC_API_END
 }
 
+sbec_status sbec_set_zeeman_fn(sbec_ws* ws, sbec_zeeman_fn fn, void* user) {
+  SBEC_API_BEGIN
+  E(ws);
+  ws->zfn = fn;
+  ws->zuser = fn ? user : nullptr;
+  SBEC_API_END
+}
+
 sbec_status sbec_set_potential(sbec_ws* ws, const double* V) {
   SBEC_API_BEGIN
   need(V, "V");
@@ -476,6 +509,8 @@ sbec_status sbec_tensor_channels(sbec_ws* ws, int32_t* active, int32_t* n_channe
 
 sbec_status sbec_half_potential(sbec_ws* ws, double dt_half, int32_t imaginary_time) {
   SBEC_API_BEGIN
+  E(ws);
+  zee(ws);
   E(ws).half_potential(dt_half, imaginary_time != 0);
   E(ws).sync();
   SBEC_API_END
@@ -542,6 +577,26 @@ sbec_status sbec_run_simulation(sbec_ws* ws, int64_t n_steps, int64_t save_every
       step = nxt;
       if (step % save_every == 0) check_cb(snapshot(ws, cb, user));
     }
+  } else if (ws->zfn) {
+    // the leapfrog with the Zeeman term evaluated at the state time before every potential
+    // step (src/simulation.jl:49-94), one step at a time
+    const double dt = e.dt;
+    zee(ws);
+    e.half_potential(dt / 2, false);
+    for (int64_t step = 1; step <= n_steps; ++step) {
+      e.kinetic(ws->kin_dt, ws->kin_itp);
+      const bool is_save = step % save_every == 0, is_last = step == n_steps;
+      zee(ws);
+      e.half_potential(is_save || is_last ? dt / 2 : dt, false);
+      e.apply_loss(dt);
+      e.t += dt;
+      e.step += 1;
+      if (is_save) check_cb(snapshot(ws, cb, user));
+      if ((is_save || is_last) && !is_last) {
+        zee(ws);
+        e.half_potential(dt / 2, false);
+      }
+    }
   } else if (e.fused_path() && !ws->kin_itp && ws->kin_dt == e.dt && ws->pipelined_snapshots && cb) {
     run_leapfrog_pipelined(ws, n_steps, save_every, cb, user);
   } else if (e.fused_path() && !ws->kin_itp && ws->kin_dt == e.dt) {
@@ -607,6 +662,7 @@ sbec_status sbec_run_adaptive(sbec_ws* ws, const sbec_adaptive_params* p, double
     bool fsal_deferred = false;
     double fsal_dt = 0.0;
     while (e.t < t_end - 1e-14) {
+      zee(ws);
       double dt_step = std::min(dt, t_end - e.t);
       const double rem = next_save - e.t;
       if (rem > 1e-14 && rem < dt_step) dt_step = rem;
@@ -653,13 +709,17 @@ sbec_status sbec_run_adaptive(sbec_ws* ws, const sbec_adaptive_params* p, double
         dt = std::min(std::max(dt * factor, p->dt_min), p->dt_max);
       }
       if (e.t >= next_save - 1e-14) {
+        zee(ws);
         e.half_potential(fsal_dt / 2, false);
         fsal_deferred = false;
         check_cb(snapshot(ws, cb, user));
         next_save += save_interval;
       }
     }
-    if (fsal_deferred) e.half_potential(fsal_dt / 2, false);
+    if (fsal_deferred) {
+      zee(ws);
+      e.half_potential(fsal_dt / 2, false);
+    }
   } else {
     // _adaptive_richardson_loop! (src/adaptive.jl:204-296)
     while (e.t < t_end - 1e-14) {
@@ -669,6 +729,7 @@ sbec_status sbec_run_adaptive(sbec_ws* ws, const sbec_adaptive_params* p, double
       dt_step = std::max(dt_step, p->dt_min);
       const bool is_clamped = dt_step < dt * 0.99;
       const bool may_reject = !is_clamped && dt_step > p->dt_min * 1.01;
+      zee(ws);
       e.copy_slot(kSlotA, kPsi);
       e.half_potential(dt_step / 2, false);
       kinetic(ws, dt_step, false);
@@ -896,6 +957,8 @@ sbec_status sbec_ground_state_adaptive(sbec_ws* ws, int64_t n_steps, double tol,
 sbec_status sbec_total_energy(sbec_ws* ws, double* Eout) {
   SBEC_API_BEGIN
   need(Eout, "E");
+  E(ws);
+  zee(ws);
   *Eout = total_energy(E(ws));
   SBEC_API_END
 }
@@ -903,6 +966,8 @@ sbec_status sbec_total_energy(sbec_ws* ws, double* Eout) {
 sbec_status sbec_energy_breakdown(sbec_ws* ws, sbec_energy_terms* out) {
   SBEC_API_BEGIN
   need(out, "out");
+  E(ws);
+  zee(ws);
   *out = E(ws).energy_terms();
   SBEC_API_END
 }

@@ -1572,6 +1572,16 @@ __global__ void __launch_bounds__(256) k_loss(cplx<R>* __restrict__ psi, int64_t
   }
 }
 
+// f+(m_c) = sqrt(F(F+1) - m_c(m_c+1)) in FP64 for the FP64 reductions: the SpinTabs copy
+// is rounded to the working precision, which in the FP32 form would put a 1e-8 relative
+// error into every <Fx>, <Fy> sum.
+template <int D>
+__device__ __forceinline__ double fp_exact(int c) {
+  constexpr int F = (D - 1) / 2;
+  const int m = F - c;
+  return sqrt((double)(F * (F + 1) - m * (m + 1)));
+}
+
 // ---------------------------------------------------------------------------
 // Reductions: per-block partial results (double), then a fixed-order finish.
 // ---------------------------------------------------------------------------
@@ -1650,8 +1660,8 @@ __global__ void __launch_bounds__(kRedThreads) k_energy_local(const cplx<R>* __r
       if (c >= 1) {
         const double pr = (double)prev.x * z.x + (double)prev.y * z.y;
         const double pi = (double)prev.x * z.y - (double)prev.y * z.x;
-        fre += (double)st.fp[c] * pr;
-        fim += (double)st.fp[c] * pi;
+        fre += fp_exact<D>(c) * pr;
+        fim += fp_exact<D>(c) * pi;
       }
       prev = z;
     }
@@ -1746,8 +1756,8 @@ __global__ void __launch_bounds__(kRedThreads) k_phase_sums(const cplx<R>* __res
       n += a2;
       fz += (double)st.m[c] * a2;
       if (c >= 1) {
-        fre += (double)st.fp[c] * (v[c - 1].x * v[c].x + v[c - 1].y * v[c].y);
-        fim += (double)st.fp[c] * (v[c - 1].x * v[c].y - v[c - 1].y * v[c].x);
+        fre += fp_exact<D>(c) * (v[c - 1].x * v[c].x + v[c - 1].y * v[c].y);
+        fim += fp_exact<D>(c) * (v[c - 1].x * v[c].y - v[c - 1].y * v[c].x);
       }
     }
     acc[0] += n;
@@ -1801,8 +1811,8 @@ __global__ void __launch_bounds__(kRedThreads) k_raman_energy(const cplx<R>* __r
       const double2 z = make_double2((double)z0.x, (double)z0.y);
       fz += (double)st.m[c] * (z.x * z.x + z.y * z.y);
       if (c >= 1) {
-        fre += (double)st.fp[c] * (prev.x * z.x + prev.y * z.y);
-        fim += (double)st.fp[c] * (prev.x * z.y - prev.y * z.x);
+        fre += fp_exact<D>(c) * (prev.x * z.x + prev.y * z.y);
+        fim += fp_exact<D>(c) * (prev.x * z.y - prev.y * z.x);
       }
       prev = z;
     }
@@ -1979,8 +1989,8 @@ __global__ void __launch_bounds__(kRedThreads) k_batch_energy_local(const cplx<R
       n += a2;
       fz += (double)st.m[c] * a2;
       if (c >= 1) {
-        fre += (double)st.fp[c] * ((double)prev.x * z.x + (double)prev.y * z.y);
-        fim += (double)st.fp[c] * ((double)prev.x * z.y - (double)prev.y * z.x);
+        fre += fp_exact<D>(c) * ((double)prev.x * z.x + (double)prev.y * z.y);
+        fim += fp_exact<D>(c) * ((double)prev.x * z.y - (double)prev.y * z.x);
       }
       prev = z;
     }

@@ -126,6 +126,7 @@ class sbec_kernel_stat(C.Structure):
 
 
 CALLBACK = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(sbec_snapshot))
+ZEEMAN_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double))
 
 _P = C.c_void_p
 _D = C.POINTER(C.c_double)
@@ -140,6 +141,7 @@ _PROTOS = {
     "sbec_set_time": (C.c_int, [_P, C.c_double, C.c_int64]),
     "sbec_get_time": (C.c_int, [_P, _D, C.POINTER(C.c_int64)]),
     "sbec_set_zeeman": (C.c_int, [_P, C.c_double, C.c_double]),
+    "sbec_set_zeeman_fn": (C.c_int, [_P, ZEEMAN_FN, C.c_void_p]),
     "sbec_set_potential": (C.c_int, [_P, _D]),
     "sbec_set_dt": (C.c_int, [_P, C.c_double]),
     "sbec_tensor_channels": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32), _D]),

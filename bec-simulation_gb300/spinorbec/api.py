@@ -97,6 +97,26 @@ class Workspace:
     def set_zeeman(self, p: float, q: float) -> None:
         check(self._lib.sbec_set_zeeman(self.handle, float(p), float(q)))
 
+    def set_zeeman_function(self, fn) -> None:
+        """TimeDependentZeeman: fn(t) -> ZeemanParams is evaluated by the library at the state
+        time before every half potential (sbec_set_zeeman_fn); None restores the static term."""
+        if fn is None:
+            check(self._lib.sbec_set_zeeman_fn(self.handle, _lib.ZEEMAN_FN(), None))
+            self._zfn = None
+            self.zeeman = ZeemanParams() if not isinstance(self.zeeman, ZeemanParams) else self.zeeman
+            return
+
+        def _cb(user, t, pp, qp):
+            try:
+                z = fn(t)
+                pp[0], qp[0] = float(z.p), float(z.q)
+            except Exception:  # reported by the library as a non-finite Zeeman term
+                pp[0] = qp[0] = float("nan")
+
+        self._zfn = _lib.ZEEMAN_FN(_cb)
+        check(self._lib.sbec_set_zeeman_fn(self.handle, self._zfn, None))
+        self.zeeman = fn
+
     def set_dt(self, dt: float) -> None:
         check(self._lib.sbec_set_dt(self.handle, float(dt)))
         self.sim_params = SimParams(dt, self.sim_params.n_steps, self.sim_params.imaginary_time,
@@ -211,6 +231,8 @@ def make_workspace(*, grid: Grid, atom: AtomSpecies, interactions: InteractionPa
     h = C.c_void_p()
     check(lib.sbec_ws_create(C.byref(cfg), dptr(pbuf), dptr(V), C.byref(h)))
     ws = Workspace(h, grid, F, sim_params, precision, zeeman)
+    if callable(zeeman):
+        ws.set_zeeman_function(zeeman)
     if not graphs:
         ws.set_graph_mode(False)
     return ws
@@ -218,14 +240,9 @@ def make_workspace(*, grid: Grid, atom: AtomSpecies, interactions: InteractionPa
 
 # ---- operators ---------------------------------------------------------------
 
-def _zeeman_now(ws: Workspace) -> None:
-    if callable(ws.zeeman):
-        z = ws.zeeman(ws.t)
-        ws.set_zeeman(z.p, z.q)
-
-
 def half_potential_step(ws: Workspace, dt_half: float, imaginary_time: bool = False) -> None:
-    _zeeman_now(ws)
+    """``_half_potential_step!`` (src/split_step.jl:48-133); a time-dependent Zeeman term is
+    evaluated by the library at the workspace time."""
     check(ws._lib.sbec_half_potential(ws.handle, float(dt_half), int(bool(imaginary_time))))
 
 

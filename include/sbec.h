@@ -137,6 +137,14 @@ sbec_status sbec_set_time(sbec_ws* ws, double t, int64_t step);
 sbec_status sbec_get_time(sbec_ws* ws, double* t, int64_t* step);
 /* zeeman_at(z, t) evaluated by the host for TimeDependentZeeman (src/zeeman.jl:20-21). */
 sbec_status sbec_set_zeeman(sbec_ws* ws, double p, double q);
+/* TimeDependentZeeman (src/types.jl:172-178) for every entry point that steps: fn(user, t, &p, &q)
+ * is called with the state time before each half potential, as _half_potential_step! evaluates
+ * zeeman_at(ws.zeeman, ws.state.t) (src/split_step.jl:49); the leapfrog's merged V(dt) uses the
+ * time at the start of its step, as in src/simulation.jl:66-72.  fn = NULL restores the static
+ * (p, q) of sbec_set_zeeman.  While a function is set, steps launch eagerly (the Zeeman factors
+ * change from step to step).  fn runs on the calling thread and must not call into this workspace. */
+typedef void (*sbec_zeeman_fn)(void* user, double t, double* p, double* q);
+sbec_status sbec_set_zeeman_fn(sbec_ws* ws, sbec_zeeman_fn fn, void* user);
 /* Replaces the potential values (evaluate_potential, src/potentials.jl:1-32). */
 sbec_status sbec_set_potential(sbec_ws* ws, const double* V);
 /* _rebuild_workspace_with_dt (src/ground_state.jl:380-392): new dt for split_step!. */
