@@ -13,6 +13,7 @@
 #include <mutex>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "sbec.h"
@@ -32,8 +33,12 @@ void cuda_check(cudaError_t e, const char* what) {
 
 using namespace sbec;
 
+// A batch: solves grouped by grid, one engine (device buffers, stream) per group; solve i
+// lives in group grp[i] at local index loc[i].  Groups advance concurrently.
 struct sbec_batch {
-  std::unique_ptr<EngineBase> eng;
+  std::vector<std::unique_ptr<EngineBase>> groups;
+  std::vector<int> grp, loc;
+  int n() const { return (int)grp.size(); }
 };
 
 struct sbec_ws {
@@ -1010,82 +1015,35 @@ sbec_status sbec_classify_phase(sbec_ws* ws, sbec_phase_info* out) {
 }
 
 // ---- batches of independent ITP solves (find_ground_state per solve, one schedule)
-sbec_status sbec_batch_create(const sbec_config* cfg, int32_t n_solves, const double* c0, const double* c1,
-                              const double* psi, const double* V, sbec_batch** out) {
-  SBEC_API_BEGIN
-  need(cfg, "config");
-  need(c0, "c0");
-  need(c1, "c1");
-  need(psi, "psi");
-  need(out, "out");
-  *out = nullptr;
+namespace {
+
+void check_batch_config(const sbec_config* cfg) {
   if (!cfg->imaginary_time || cfg->normalize_every != 1)
     fail(SBEC_ERR_INVALID, "batched ground states need imaginary_time=1 and normalize_every=1");
   if (cfg->n_c_extra != 0 || cfg->gS_direct || cfg->enable_ddi || cfg->raman ||
       !(cfg->loss_gamma_dr < 1e-30 && cfg->loss_L3 < 1e-30))
     fail(SBEC_ERR_UNSUPPORTED,
          "batched ground states support contact c0/c1 (+LHY) couplings without DDI, Raman or losses");
-  Setup s = build_setup(*cfg);
-  if (sbec_device_count() < 1) fail(SBEC_ERR_DEVICE, "no CUDA device available (the GPU path has no CPU fallback)");
-  auto b = std::make_unique<sbec_batch>();
-  b->eng = cfg->precision == SBEC_FP32_BULK ? make_engine_f32(s) : make_engine_f64(s);
-  EngineBase& e = *b->eng;
-  e.zeeman_p = cfg->zeeman_p;
-  e.zeeman_q = cfg->zeeman_q;
-  e.dt = cfg->dt;
-  e.itp = true;
-  e.normalize_every = 1;
-  if (V) e.set_potential(V);
-  e.batch_init(n_solves, c0, c1, psi);
-  *out = b.release();
-  SBEC_API_END
 }
 
-sbec_status sbec_batch_destroy(sbec_batch* b) {
-  SBEC_API_BEGIN
-  delete b;
-  SBEC_API_END
+std::unique_ptr<EngineBase> make_batch_group(const sbec_config& cfg, int n, const double* c0, const double* c1,
+                                             const double* psi, const double* V) {
+  Setup s = build_setup(cfg);
+  auto e = cfg.precision == SBEC_FP32_BULK ? make_engine_f32(s) : make_engine_f64(s);
+  e->zeeman_p = cfg.zeeman_p;
+  e->zeeman_q = cfg.zeeman_q;
+  e->dt = cfg.dt;
+  e->itp = true;
+  e->normalize_every = 1;
+  if (V) e->set_potential(V);
+  e->batch_init(n, c0, c1, psi);
+  return e;
 }
 
-sbec_status sbec_batch_get_psi(sbec_batch* b, int32_t solve, double* psi) {
-  SBEC_API_BEGIN
-  need(b, "batch");
-  need(psi, "psi");
-  b->eng->batch_get_psi(solve, psi);
-  SBEC_API_END
-}
-
-sbec_status sbec_batch_classify_phase(sbec_batch* b, int32_t solve, sbec_phase_info* out) {
-  SBEC_API_BEGIN
-  need(b, "batch");
-  need(out, "out");
-  if (solve < 0 || solve >= b->eng->n_solves()) fail(SBEC_ERR_INVALID, "solve index out of range");
-  classify_phase(*b->eng, solve, out);
-  SBEC_API_END
-}
-
-sbec_status sbec_batch_energies(sbec_batch* b, double* E) {
-  SBEC_API_BEGIN
-  need(b, "batch");
-  need(E, "E");
-  EngineBase& e = *b->eng;
-  std::vector<int> all(e.n_solves());
-  for (int i = 0; i < e.n_solves(); ++i) all[i] = i;
-  e.batch_set_active(all);
-  e.batch_energies(E);
-  SBEC_API_END
-}
-
-// The find_ground_state ITP loop (src/ground_state.jl:116-169) for every solve of
-// the batch; a solve leaves the active set at the check where it converges.  The
-// NaN guard of steps 1-10 (src/ground_state.jl:4-29) is evaluated once, at step 10.
-sbec_status sbec_batch_ground_state(sbec_batch* b, int64_t n_steps, double tol, int64_t check_every,
-                                    sbec_gs_result* out) {
-  SBEC_API_BEGIN
-  need(b, "batch");
-  need(out, "out");
-  if (n_steps <= 0 || check_every <= 0) fail(SBEC_ERR_INVALID, "n_steps and check_every must be positive");
-  EngineBase& e = *b->eng;
+// The find_ground_state ITP loop (src/ground_state.jl:116-169) for every solve of one group;
+// a solve leaves the active set at the check where it converges.  The NaN guard of steps
+// 1-10 (src/ground_state.jl:4-29) is evaluated once, at step 10.  out: the group's solves.
+void batch_ground_state(EngineBase& e, int64_t n_steps, double tol, int64_t check_every, sbec_gs_result* out) {
   const int n = e.n_solves();
   std::vector<int> active(n);
   for (int i = 0; i < n; ++i) active[i] = i;
@@ -1133,6 +1091,184 @@ sbec_status sbec_batch_ground_state(sbec_batch* b, int64_t n_steps, double tol, 
     }
   }
   e.sync();
+}
+
+EngineBase& batch_solve(sbec_batch* b, int32_t solve, int* local) {
+  need(b, "batch");
+  if (solve < 0 || solve >= b->n()) fail(SBEC_ERR_INVALID, "solve index out of range");
+  *local = b->loc[solve];
+  return *b->groups[b->grp[solve]];
+}
+
+}  // namespace
+
+sbec_status sbec_batch_create(const sbec_config* cfg, int32_t n_solves, const double* c0, const double* c1,
+                              const double* psi, const double* V, sbec_batch** out) {
+  SBEC_API_BEGIN
+  need(cfg, "config");
+  need(c0, "c0");
+  need(c1, "c1");
+  need(psi, "psi");
+  need(out, "out");
+  *out = nullptr;
+  check_batch_config(cfg);
+  build_setup(*cfg);  // argument errors before the device check
+  if (sbec_device_count() < 1) fail(SBEC_ERR_DEVICE, "no CUDA device available (the GPU path has no CPU fallback)");
+  auto b = std::make_unique<sbec_batch>();
+  b->groups.push_back(make_batch_group(*cfg, n_solves, c0, c1, psi, V));
+  for (int i = 0; i < n_solves; ++i) {
+    b->grp.push_back(0);
+    b->loc.push_back(i);
+  }
+  *out = b.release();
+  SBEC_API_END
+}
+
+sbec_status sbec_batch_create_grids(const sbec_config* cfg, int32_t n_solves, const int32_t* n, const double* L,
+                                    const double* c0, const double* c1, const double* const* psi,
+                                    const double* const* V, sbec_batch** out) {
+  SBEC_API_BEGIN
+  need(cfg, "config");
+  need(n, "n");
+  need(L, "L");
+  need(c0, "c0");
+  need(c1, "c1");
+  need(psi, "psi");
+  need(out, "out");
+  *out = nullptr;
+  if (n_solves < 1) fail(SBEC_ERR_INVALID, "n_solves must be >= 1");
+  check_batch_config(cfg);
+  // group the solves by grid (first appearance order); all solves of a grid share its potential
+  std::vector<sbec_config> gcfg;
+  std::vector<std::vector<int>> members;
+  std::vector<int> grp(n_solves), loc(n_solves);
+  for (int i = 0; i < n_solves; ++i) {
+    sbec_config c = *cfg;
+    for (int d = 0; d < 3; ++d) {
+      c.n[d] = d < cfg->ndim ? n[3 * i + d] : 1;
+      c.L[d] = d < cfg->ndim ? L[3 * i + d] : 1.0;
+    }
+    int g = -1;
+    for (size_t k = 0; k < gcfg.size(); ++k) {
+      bool same = true;
+      for (int d = 0; d < cfg->ndim; ++d) same = same && gcfg[k].n[d] == c.n[d] && gcfg[k].L[d] == c.L[d];
+      if (same) g = (int)k;
+    }
+    if (g < 0) {
+      build_setup(c);  // argument errors before any device work
+      g = (int)gcfg.size();
+      gcfg.push_back(c);
+      members.emplace_back();
+    }
+    need(psi[i], "psi[i]");
+    if (V && !members[g].empty()) {
+      const double* v0 = V[members[g][0]];
+      long long N = 1;
+      for (int d = 0; d < cfg->ndim; ++d) N *= c.n[d];
+      const bool same = (V[i] == v0) || (V[i] && v0 && std::memcmp(V[i], v0, sizeof(double) * N) == 0);
+      if (!same) fail(SBEC_ERR_INVALID, "solves on the same grid must share one potential");
+    }
+    grp[i] = g;
+    loc[i] = (int)members[g].size();
+    members[g].push_back(i);
+  }
+  if (sbec_device_count() < 1) fail(SBEC_ERR_DEVICE, "no CUDA device available (the GPU path has no CPU fallback)");
+  auto b = std::make_unique<sbec_batch>();
+  b->grp = grp;
+  b->loc = loc;
+  for (size_t g = 0; g < gcfg.size(); ++g) {
+    const auto& m = members[g];
+    long long N = 1;
+    for (int d = 0; d < cfg->ndim; ++d) N *= gcfg[g].n[d];
+    const size_t per = (size_t)2 * N * (2 * cfg->F + 1);
+    std::vector<double> gc0, gc1, gpsi(per * m.size());
+    for (size_t k = 0; k < m.size(); ++k) {
+      gc0.push_back(c0[m[k]]);
+      gc1.push_back(c1[m[k]]);
+      std::memcpy(gpsi.data() + k * per, psi[m[k]], sizeof(double) * per);
+    }
+    b->groups.push_back(make_batch_group(gcfg[g], (int)m.size(), gc0.data(), gc1.data(), gpsi.data(),
+                                         V ? V[m[0]] : nullptr));
+  }
+  *out = b.release();
+  SBEC_API_END
+}
+
+sbec_status sbec_batch_destroy(sbec_batch* b) {
+  SBEC_API_BEGIN
+  delete b;
+  SBEC_API_END
+}
+
+sbec_status sbec_batch_get_psi(sbec_batch* b, int32_t solve, double* psi) {
+  SBEC_API_BEGIN
+  need(psi, "psi");
+  int l = 0;
+  EngineBase& e = batch_solve(b, solve, &l);
+  e.batch_get_psi(l, psi);
+  SBEC_API_END
+}
+
+sbec_status sbec_batch_classify_phase(sbec_batch* b, int32_t solve, sbec_phase_info* out) {
+  SBEC_API_BEGIN
+  need(out, "out");
+  int l = 0;
+  EngineBase& e = batch_solve(b, solve, &l);
+  classify_phase(e, l, out);
+  SBEC_API_END
+}
+
+sbec_status sbec_batch_energies(sbec_batch* b, double* E) {
+  SBEC_API_BEGIN
+  need(b, "batch");
+  need(E, "E");
+  for (size_t g = 0; g < b->groups.size(); ++g) {
+    EngineBase& e = *b->groups[g];
+    std::vector<int> all(e.n_solves());
+    for (int i = 0; i < e.n_solves(); ++i) all[i] = i;
+    e.batch_set_active(all);
+    std::vector<double> Eg(e.n_solves());
+    e.batch_energies(Eg.data());
+    for (int i = 0; i < b->n(); ++i)
+      if (b->grp[i] == (int)g) E[i] = Eg[b->loc[i]];
+  }
+  SBEC_API_END
+}
+
+// The groups' ITP loops run concurrently, one host thread per group (each group has its own
+// stream, buffers and graphs); results in the caller's solve order.
+sbec_status sbec_batch_ground_state(sbec_batch* b, int64_t n_steps, double tol, int64_t check_every,
+                                    sbec_gs_result* out) {
+  SBEC_API_BEGIN
+  need(b, "batch");
+  need(out, "out");
+  if (n_steps <= 0 || check_every <= 0) fail(SBEC_ERR_INVALID, "n_steps and check_every must be positive");
+  const size_t G = b->groups.size();
+  std::vector<std::vector<sbec_gs_result>> res(G);
+  for (size_t g = 0; g < G; ++g) res[g].resize(b->groups[g]->n_solves());
+  if (G == 1) {
+    batch_ground_state(*b->groups[0], n_steps, tol, check_every, res[0].data());
+  } else {
+    int dev = 0;
+    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    std::vector<std::thread> th;
+    std::vector<SbecError> err(G, SbecError{SBEC_OK, ""});
+    for (size_t g = 0; g < G; ++g)
+      th.emplace_back([&, g] {
+        try {
+          cuda_check(cudaSetDevice(dev), "cudaSetDevice");
+          batch_ground_state(*b->groups[g], n_steps, tol, check_every, res[g].data());
+        } catch (const SbecError& e) {
+          err[g] = e;
+        } catch (const std::exception& e) {
+          err[g] = SbecError{SBEC_ERR_DEVICE, e.what()};
+        }
+      });
+    for (auto& t : th) t.join();
+    for (const auto& e : err)
+      if (e.status != SBEC_OK) throw e;
+  }
+  for (int i = 0; i < b->n(); ++i) out[i] = res[b->grp[i]][b->loc[i]];
   SBEC_API_END
 }
 
@@ -1243,7 +1379,9 @@ sbec_status sbec_tune_table_import(const char* text) {
 sbec_status sbec_batch_tuning_report(sbec_batch* b, char* buf, int64_t cap, int64_t* len) {
   SBEC_API_BEGIN
   need(b, "batch");
-  copy_report(b->eng->tuning_report(), buf, cap, len);
+  std::string r;
+  for (const auto& g : b->groups) r += g->tuning_report() + "\n";
+  copy_report(r, buf, cap, len);
   SBEC_API_END
 }
 

@@ -10,6 +10,8 @@ from ._lib import (ArgumentError, CallbackStop, DeviceError, NumericError, OutOf
                    UnsupportedError, load)
 from .api import *  # noqa: F401,F403
 from .host import *  # noqa: F401,F403
+from .experiment import (ExperimentConfig, ExperimentResult, parse_experiment,  # noqa: F401
+                         run_experiment)
 
 
 def device_count() -> int:

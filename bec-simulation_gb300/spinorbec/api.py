@@ -231,6 +231,8 @@ def make_workspace(*, grid: Grid, atom: AtomSpecies, interactions: InteractionPa
     h = C.c_void_p()
     check(lib.sbec_ws_create(C.byref(cfg), dptr(pbuf), dptr(V), C.byref(h)))
     ws = Workspace(h, grid, F, sim_params, precision, zeeman)
+    ws.atom, ws.interactions = atom, interactions
+    ws.c_dd = 0.0 if not enable_ddi or math.isnan(c_dd) else float(c_dd)
     if callable(zeeman):
         ws.set_zeeman_function(zeeman)
     if not graphs:
@@ -365,6 +367,7 @@ class _Recorder:
         self.callback = callback
         self.keep_psi = keep_psi
         self.first = True
+        self.step0 = 0
         self.count = 0
         self.err = None
         store = _SnapshotStore(ws.grid.config.n_points, ws.D) if keep_psi else None
@@ -380,9 +383,10 @@ class _Recorder:
                     self.res.psi_snapshots.append(store.take(s.psi))
                 if self.first:
                     self.first = False
+                    self.step0 = s.step
                 elif self.callback is not None:
                     self.count += 1
-                    self.callback(ws, s.step if not use_count_arg else self.count)
+                    self.callback(ws, s.step - self.step0 if not use_count_arg else self.count)
                 return 0
             except Exception as e:  # surface Python errors after the C call returns
                 self.err = e
@@ -408,6 +412,68 @@ def run_simulation(ws: Workspace, callback: Optional[Callable] = None, keep_psi:
     rec.raise_pending()
     check(st)
     return rec.res
+
+
+def save_state(filename: str, ws: Workspace) -> None:
+    """``save_state`` (src/io.jl:1-28): psi, t, step and the parameters that define the run, in
+    a NumPy .npz archive with the reference's field names (JLD2 is the Julia side's format)."""
+    z = ws.zeeman if isinstance(ws.zeeman, ZeemanParams) else None
+    ip = getattr(ws, "interactions", None)
+    np.savez(filename, psi=ws.psi, t=ws.t, step=ws.step,
+             grid_n_points=np.array(ws.grid.config.n_points), grid_box_size=np.array(ws.grid.config.box_size),
+             atom_name=getattr(getattr(ws, "atom", None), "name", ""),
+             c0=ip.c0 if ip else np.nan, c1=ip.c1 if ip else np.nan, c_lhy=ip.c_lhy if ip else np.nan,
+             c_extra=np.array(ip.c_extra if ip else (), dtype=np.float64),
+             zeeman_p=z.p if z else np.nan, zeeman_q=z.q if z else np.nan, c_dd=getattr(ws, "c_dd", 0.0),
+             dt=ws.sim_params.dt, imaginary_time=bool(ws.sim_params.imaginary_time))
+
+
+def load_state(filename: str) -> dict:
+    """``load_state`` (src/io.jl): the fields written by save_state."""
+    with np.load(filename) as d:
+        out = {k: d[k] for k in d.files}
+    for k in ("t", "c0", "c1", "c_lhy", "zeeman_p", "zeeman_q", "c_dd", "dt"):
+        out[k] = float(out[k])
+    out["step"] = int(out["step"])
+    out["imaginary_time"] = bool(out["imaginary_time"])
+    out["atom_name"] = str(out["atom_name"])
+    out["psi"] = np.asfortranarray(out["psi"])
+    return out
+
+
+def run_simulation_checkpointed(ws: Workspace, checkpoint_dir: str = "checkpoints", checkpoint_every: int = 1000,
+                                callback: Optional[Callable] = None, resume: bool = False) -> SimulationResult:
+    """``run_simulation_checkpointed!`` (src/simulation.jl:96-148): with resume, psi, t and step
+    come from the latest step_*.npz in checkpoint_dir; the remaining n_steps - step steps run
+    through run_simulation, and every save point whose global step is a multiple of
+    checkpoint_every writes step_<8-digit step>.npz before the user's callback runs."""
+    import os
+
+    os.makedirs(checkpoint_dir, exist_ok=True)
+    if resume:
+        existing = sorted(f for f in os.listdir(checkpoint_dir) if f.startswith("step_") and f.endswith(".npz"))
+        if existing:
+            data = load_state(os.path.join(checkpoint_dir, existing[-1]))
+            ws.psi = data["psi"]
+            ws.set_time(data["t"], data["step"])
+    start_step = ws.step
+    remaining = ws.sim_params.n_steps - start_step
+    if remaining <= 0:
+        return run_simulation(ws, callback=callback)
+
+    def checkpoint_cb(ws_cb, step):
+        global_step = start_step + step
+        if global_step % checkpoint_every == 0:
+            save_state(os.path.join(checkpoint_dir, f"step_{global_step:08d}.npz"), ws_cb)
+        if callback is not None:
+            callback(ws_cb, step)
+
+    sp = ws.sim_params
+    ws.sim_params = SimParams(sp.dt, remaining, sp.imaginary_time, sp.normalize_every, sp.save_every)
+    try:
+        return run_simulation(ws, callback=checkpoint_cb)
+    finally:
+        ws.sim_params = sp
 
 
 def _adaptive_params(adaptive: AdaptiveDtParams) -> _lib.sbec_adaptive_params:
@@ -650,29 +716,59 @@ def _config(grid: Grid, F: int, zeeman, sim_params: SimParams, precision: str, i
 
 
 class GroundStateBatch:
-    """Independent ITP solves that share grid, F, V, dt and Zeeman, stepped together.
+    """Independent ITP solves that share F, dt and Zeeman, stepped together.
 
     Each solve follows ``find_ground_state``'s loop and convergence test
     (src/ground_state.jl:116-169) with its own c0, c1 and initial psi; solves leave
-    the batch at the check where they converge.
+    the batch at the check where they converge.  ``grid`` puts every solve on one grid;
+    ``grids`` gives one grid per solve (sbec_batch_create_grids: solves are grouped by grid
+    and the groups advance concurrently), with ``potential`` evaluated on each grid.
     """
 
-    def __init__(self, *, grid: Grid, atom: AtomSpecies, c0s, c1s, psi_inits, zeeman=None, potential=None,
-                 dt: float = 0.005, c_lhy: float = 0.0, precision: str = "fp32"):
+    def __init__(self, *, grid: Optional[Grid] = None, atom: AtomSpecies, c0s, c1s, psi_inits, zeeman=None,
+                 potential=None, dt: float = 0.005, c_lhy: float = 0.0, precision: str = "fp32", grids=None):
         lib = load()
-        self.grid, self.F, self.D = grid, atom.F, 2 * atom.F + 1
+        if (grid is None) == (grids is None):
+            raise _lib.ArgumentError("give either grid (one grid for every solve) or grids (one per solve)")
+        self.F, self.D = atom.F, 2 * atom.F + 1
         self.n = len(psi_inits)
         if len(c0s) != self.n or len(c1s) != self.n:
             raise _lib.ArgumentError("c0s, c1s and psi_inits must have the same length")
+        self.grids = [grid] * self.n if grids is None else list(grids)
+        if len(self.grids) != self.n:
+            raise _lib.ArgumentError("grids and psi_inits must have the same length")
+        self.grid = grid if grid is not None else self.grids[0]
         zeeman = ZeemanParams() if zeeman is None else zeeman
-        cfg = _config(grid, atom.F, zeeman, SimParams(dt, 1, True, 1, 1), precision,
+        cfg = _config(self.grid, atom.F, zeeman, SimParams(dt, 1, True, 1, 1), precision,
                       InteractionParams(0.0, 0.0, c_lhy))
-        psi = np.concatenate([to_interleaved(p) for p in psi_inits])
-        V = np.ascontiguousarray(evaluate_potential(potential, grid).ravel(order="F"))
         c0 = np.ascontiguousarray(c0s, dtype=np.float64)
         c1 = np.ascontiguousarray(c1s, dtype=np.float64)
         h = C.c_void_p()
-        check(lib.sbec_batch_create(C.byref(cfg), self.n, dptr(c0), dptr(c1), dptr(psi), dptr(V), C.byref(h)))
+        if grids is None:
+            psi = np.concatenate([to_interleaved(p) for p in psi_inits])
+            V = np.ascontiguousarray(evaluate_potential(potential, grid).ravel(order="F"))
+            check(lib.sbec_batch_create(C.byref(cfg), self.n, dptr(c0), dptr(c1), dptr(psi), dptr(V), C.byref(h)))
+        else:
+            nd = self.grid.config.ndim
+            n = np.ones(3 * self.n, dtype=np.int32)
+            L = np.ones(3 * self.n, dtype=np.float64)
+            keep, Vs = [], {}
+            psi_p = (C.POINTER(C.c_double) * self.n)()
+            V_p = (C.POINTER(C.c_double) * self.n)()
+            for i, (g, p) in enumerate(zip(self.grids, psi_inits)):
+                if g.config.ndim != nd:
+                    raise _lib.ArgumentError("every grid of a batch has the same number of axes")
+                n[3 * i:3 * i + nd] = g.config.n_points
+                L[3 * i:3 * i + nd] = g.config.box_size
+                buf = to_interleaved(p)
+                keep.append(buf)
+                psi_p[i] = dptr(buf)
+                key = (tuple(g.config.n_points), tuple(g.config.box_size))
+                if key not in Vs:
+                    Vs[key] = np.ascontiguousarray(evaluate_potential(potential, g).ravel(order="F"))
+                V_p[i] = dptr(Vs[key])
+            check(lib.sbec_batch_create_grids(C.byref(cfg), self.n, n.ctypes.data_as(C.POINTER(C.c_int32)),
+                                              dptr(L), dptr(c0), dptr(c1), psi_p, V_p, C.byref(h)))
         self._h = h
         self._lib = lib
 
@@ -694,10 +790,11 @@ class GroundStateBatch:
         return [dict(converged=bool(r.converged), energy=r.energy, dE=r.dE, dpsi=r.dpsi, steps=r.steps) for r in out]
 
     def psi(self, i: int) -> np.ndarray:
-        n = int(np.prod(self.grid.config.n_points)) * self.D
+        g = self.grids[int(i)]
+        n = int(np.prod(g.config.n_points)) * self.D
         buf = np.empty(2 * n)
         check(self._lib.sbec_batch_get_psi(self._h, int(i), dptr(buf)))
-        return from_interleaved(buf, self.grid.config.n_points, self.D)
+        return from_interleaved(buf, g.config.n_points, self.D)
 
     def energies(self) -> np.ndarray:
         E = np.empty(self.n)

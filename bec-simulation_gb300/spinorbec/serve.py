@@ -123,6 +123,20 @@ def run_request(req: SolveRequest) -> dict:
     return out
 
 
+def pretune(requests: list) -> int:
+    """Fix the autotuner's decisions for every call shape of `requests` before any is served:
+    one two-step run per distinct (grid, F, DDI, kind, precision).  Served results then do not
+    depend on which request met a shape first; returns the number of shapes run."""
+    seen = set()
+    for r in requests:
+        key = (tuple(r.n_points), r.F, r.enable_ddi, r.kind, r.precision)
+        if key in seen:
+            continue
+        seen.add(key)
+        run_request(SolveRequest(**{**r.__dict__, "steps": 2, "tol": 0.0}))
+    return len(seen)
+
+
 class Server:
     """Admission by HBM budget and slots; concurrent resident workspaces."""
 

@@ -363,35 +363,55 @@ def bench_quickstart(S, reps: int = 3) -> dict:
 
 
 # ----------------------------------------------------------------------------- serving
-def bench_serving(S, n_requests: int, fp64_probe_steps: int = 20) -> dict:
+def bench_serving(S, n_requests: int, fp64_probe_steps: int = 20, check_budget_s: float = 45.0) -> dict:
     """Poisson request stream (seeded, mean 200 req/s) served with continuous batching in the
-    FP32-bulk form under a 150 GB HBM budget; the plain FP64 form one request at a time is
-    estimated per request from a timed probe of the same grid (per-step time x the steps the
-    served solve took, plus its measured setup)."""
+    FP32-bulk form under a 150 GB HBM budget, after the autotuner's decisions are fixed for
+    every call shape of the stream.  The plain FP64 form one request at a time is estimated
+    per request from a timed probe of the same grid (per-step time x the steps the served solve
+    took, plus its measured setup).  Served energies are checked against the FP64 form by
+    rerunning requests in FP64, cheapest first, within a time budget."""
     from spinorbec import serve
 
     reqs = serve.poisson_requests(n_requests, rate=200.0, seed=5)
+    n_shapes = serve.pretune(reqs)
+    log(f"serving: autotuner fixed for {n_shapes} shapes")
     srv = serve.Server(hbm_budget_bytes=150e9, max_slots=32, runner=_logged(serve.run_request))
     out = srv.run(reqs, realtime=True)
     log(f"serving: {len(reqs)} requests in {out['wall_s']:.1f} s")
     est64 = 0.0
     probes = {}
+    cost = {}
     for r, res in zip(reqs, out["results"]):
         key = (r.n_points, r.F, r.enable_ddi, r.kind)
         if key not in probes:
             probes[key] = fp64_probe(S, r, fp64_probe_steps)
         setup, per_step = probes[key]
-        est64 += setup + per_step * res.steps
+        cost[r.rid] = setup + per_step * res.steps
+        est64 += cost[r.rid]
+    # accuracy of served energies against the plain FP64 form (same request, same steps / tol)
+    t0 = time.perf_counter()
+    errs = []
+    for r in sorted(reqs, key=lambda q: cost[q.rid]):
+        if time.perf_counter() - t0 + cost[r.rid] > check_budget_s:
+            break
+        e64 = serve.run_request(serve.SolveRequest(**{**r.__dict__, "precision": "fp64"}))["energy"]
+        e32 = out["results"][r.rid].energy
+        errs.append(abs(e32 - e64) / abs(e64))
+    lat = sorted(x.latency for x in out["results"])
     return {"workload": f"{n_requests} requests of the seeded Poisson stream (mean 200 req/s): 1-D 256..4096, "
                         "2-D 64^2..512^2, 3-D 32^3..128^3, F in {1,2,6}, DDI for F=6, 500-5000 steps, "
                         "half ground states (tol 1e-8) half real-time runs",
             "hbm_budget_gb": 150, "max_slots": 32, "peak_concurrent": srv.peak_active,
-            "peak_admitted_gb": srv.peak_used / 1e9,
+            "peak_admitted_gb": srv.peak_used / 1e9, "tuned_shapes_before_serving": n_shapes,
             "fp32_served_solves_per_s": out["solves_per_s"], "wall_s": out["wall_s"],
             "p50_latency_s": out["p50_latency_s"], "p99_latency_s": out["p99_latency_s"],
+            "max_latency_s": lat[-1] if lat else None,
             "fp64_one_at_a_time_solves_per_s": len(reqs) / est64,
             "fp64_estimate": f"per grid/F/kind: setup + {fp64_probe_steps}-step timed probe x steps of the served solve",
-            "speedup_vs_fp64_one_at_a_time": est64 / out["wall_s"]}
+            "speedup_vs_fp64_one_at_a_time": est64 / out["wall_s"],
+            "accuracy_vs_fp64": {"checked": len(errs), "of": len(reqs), "max_energy_rel_err": max(errs) if errs else None,
+                                 "above_1e-6": sum(1 for e in errs if e > 1e-6),
+                                 "selection": f"cheapest FP64 reruns first within {check_budget_s:.0f} s"}}
 
 
 def _logged(runner):
@@ -429,11 +449,12 @@ def fp64_probe(S, r, k: int) -> tuple:
 
 
 # ----------------------------------------------------------------------------- 3D spin-6 dipolar
-def bench_3d_f6(S, n: int = 128, steps32: int = 20, steps64: int = 2) -> dict:
+def bench_3d_f6(S, n: int = 128, steps32: int = 200, steps64: int = 20, fp32_peak: float = None) -> dict:
     """3D spin-6 Eu151 (c_total 4689, c1/c0 1/36, tensor c_extra (0,0,50)), zero-padded DDI
     c_dd=100, trap (1,1,1.2), polarised m=+6 with 0.01 rad seeded phase noise; adaptive
-    Yoshida from dt=1e-3.  A bounded sample of the 2000-step run: the first accepted steps
-    of each form, timed, and the FP32 energy against the FP64 one after fixed-dt steps."""
+    Yoshida from dt=1e-3.  The first 200 (FP32) / 20 (FP64) accepted steps of the 2000-step
+    run, measured with their rejections; the FP32 energy against the FP64 one after fixed-dt
+    steps; the tensor step's time share and FLOP rate (the reference's operation count)."""
     ip = S.interaction_params_from_constraint(c_total=4689.0, c1_ratio=1 / 36, F=6, c_extra=(0.0, 0.0, 50.0))
     g = S.make_grid(S.GridConfig((n, n, n), (24.0, 24.0, 24.0)))
     rng = np.random.Generator(np.random.PCG64(11))
@@ -463,8 +484,31 @@ def bench_3d_f6(S, n: int = 128, steps32: int = 20, steps64: int = 2) -> dict:
         ws.close()
         out[prec] = {"seconds": secs, "accepted_steps": acc, "rejected_steps": int(r["n_rejected"]),
                      "steps_per_s": acc / secs, "value": units * acc / secs, "unit": UNIT,
-                     "est_2000_step_solves_per_s": acc / secs / 2000.0}
+                     "accepted_per_attempt": acc / max(acc + int(r["n_rejected"]), 1)}
     out["speedup_fp32_vs_fp64"] = out["fp32"]["steps_per_s"] / out["fp64"]["steps_per_s"]
+    # tensor step: per-call time from one profiled fixed-dt Yoshida step (12 tensor calls:
+    # 6 half potentials, each tensor(tau/2) before and after the DDI), against the FP32 peak at
+    # the reference's count of h-build work (HFEntry terms x 10 flops per point and call)
+    wp = make("fp32")
+    S.yoshida_core(wp, 1e-3)
+    wp.profile(True)
+    S.yoshida_core(wp, 1e-3)
+    prof = wp.profile_read()
+    wp.profile(False)
+    wp.close()
+    tot = sum(v["ms"] for v in prof.values())
+    ten = prof.get("tensor", {"ms": 0.0, "launches": 0})
+    hf_terms = 7497  # _precompute_hf_entries for F=6 with all seven channels active
+    if ten["launches"]:
+        per_call_s = ten["ms"] / 1e3 / ten["launches"]
+        tflops = hf_terms * 10.0 * n ** 3 / per_call_s / 1e12
+        out["tensor_step"] = {"calls_per_step": ten["launches"], "ms_per_call": per_call_s * 1e3,
+                              "share_of_step": ten["ms"] / tot if tot else None,
+                              "reference_flops_per_point_call": hf_terms * 10,
+                              "achieved_tflops_reference_count": tflops, "fp32_peak_tflops_measured": fp32_peak,
+                              "frac_of_fp32_peak": tflops / fp32_peak if fp32_peak else None,
+                              "timing": "per-launch CUDA events, one profiled Yoshida step"}
+        out["kernel_time_share"] = {k: round(v["ms"] / tot, 4) for k, v in prof.items()} if tot else None
     # accuracy: same fixed-dt Yoshida steps in both forms
     w32, w64 = make("fp32"), make("fp64")
     for _ in range(steps64):
@@ -480,6 +524,20 @@ def bench_3d_f6(S, n: int = 128, steps32: int = 20, steps64: int = 2) -> dict:
 
 
 # ----------------------------------------------------------------------------- GPU arm
+def tuned_launch_us(report: list, kind: str):
+    """The autotuner's burst time (us per launch) of the variant it chose for the first call
+    shape of the given kind ("row" or "strided"), or None when the shape was not timed."""
+    import re
+    for line in report:
+        if not line.startswith(("fp32 " + kind, "fp64 " + kind)) or " chosen v" not in line:
+            continue
+        chosen = line.rsplit(" chosen v", 1)[1].strip()
+        m = re.search(rf" v{chosen}=([0-9.]+)us", line)
+        if m:
+            return float(m.group(1))
+    return None
+
+
 def measured_peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -521,31 +579,39 @@ def main_gpu(args) -> None:
                                 sim_params=S.SimParams(DT, steps, False, None, save_every), psi_init=psi0,
                                 precision=precision)
 
+    lib = S._lib.load()
+    noop = S._lib.CALLBACK(lambda user, snap: 0)  # save points are produced; the caller keeps none
+
     def timed_runs(ws, n_runs: int, warm: int) -> tuple:
+        """Full runs with their save points: at each one the energy, norm and Mz reductions and a
+        copy of psi into pinned host memory (pipelined behind the next segment)."""
         ext = torch.cuda.ExternalStream(ws.stream_ptr)
+        S._lib.check(lib.sbec_set_snapshot_mode(ws.handle, 1))
+        run = lambda: S._lib.check(lib.sbec_run_simulation(ws.handle, ws.sim_params.n_steps,  # noqa: E731
+                                                           ws.sim_params.save_every, noop, None))
         for _ in range(warm):
-            S.run_simulation(ws, keep_psi=False)
+            ws.set_time(0.0, 0)
+            run()
         total_ms = 0.0
         l0 = ws.launch_count
         for _ in range(n_runs):
+            ws.set_time(0.0, 0)
             flush.fill_(1.0)
             torch.cuda.synchronize()
             dist.barrier()
             a = torch.cuda.Event(enable_timing=True)
             b = torch.cuda.Event(enable_timing=True)
             a.record(ext)
-            st = S._lib.load().sbec_run_simulation(ws.handle, ws.sim_params.n_steps, ws.sim_params.save_every,
-                                                   S._lib.CALLBACK(), None)
-            S._lib.check(st)
+            run()
             b.record(ext)
             b.synchronize()
             total_ms += a.elapsed_time(b)
         launches = ws.launch_count - l0
         return total_ms, launches
 
-    # ---- chosen form, device resident
+    # ---- chosen form, device resident: the run as the workload names it (save every 50)
     steps = args.run_steps
-    ws32 = make("fp32", steps, steps + 1)
+    ws32 = make("fp32", steps, SAVE_EVERY)
     clocks = ClockSampler()
     clocks.start()
     ms32, launches = timed_runs(ws32, args.steps, args.warmup)
@@ -553,9 +619,14 @@ def main_gpu(args) -> None:
     ms32 = dist.max(ms32)
     value = dist.world * units_per_run(steps) * args.steps / (ms32 / 1e3)
 
-    # ---- roofline of the dominant kernel (profiled pass, CUDA events on the engine stream)
+    # ---- roofline of the dominant kernel.  Bytes per launch from the engine's counters (one
+    # profiled run, CUDA events around every launch on the engine stream); the duration of a
+    # launch from the autotuner's burst timing of the chosen variant (eight back-to-back
+    # launches, median of three), which keeps the launch overlap of the step graph that
+    # per-launch events take away.  The profiled (perturbed) duration is kept beside it.
+    ws32.set_time(0.0, 0)
     ws32.profile(True)
-    S.run_simulation(ws32, keep_psi=False)
+    S._lib.check(lib.sbec_run_simulation(ws32.handle, steps, SAVE_EVERY, noop, None))
     prof = ws32.profile_read()
     ws32.profile(False)
     dom_name, dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
@@ -563,8 +634,11 @@ def main_gpu(args) -> None:
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "MEASURED_PEAKS.json hbm_gbs (of measured)" if "hbm_gbs" in peaks else "fallback 6800 GB/s"
     per_launch_bytes = dom["bytes"] / max(dom["launches"], 1)
-    per_launch_s = dom["ms"] / 1e3 / max(dom["launches"], 1)
+    profiled_s = dom["ms"] / 1e3 / max(dom["launches"], 1)
+    burst_us = tuned_launch_us(ws32.tuning_report.splitlines(), "row" if dom_name == "row_pass" else "strided")
+    per_launch_s = burst_us * 1e-6 if burst_us else profiled_s
     achieved = per_launch_bytes / per_launch_s / 1e9
+    run_bytes = sum(v["bytes"] for v in prof.values())  # algorithmic bytes of every launch of one run
     traffic = None
     tfile = ROOT / "profiles" / "traffic_2d_256_fp32.json"
     if tfile.exists():
@@ -600,16 +674,33 @@ def main_gpu(args) -> None:
            "h2d_bytes_per_step": psi_bytes, "d2h_bytes_per_step": psi_bytes * (n_snap + 2),
            "includes": "psi H2D, 5000 steps, 101 save points (energy, norm, Mz, psi D2H), final psi D2H"}
 
+    # ---- measured FMA peaks (the compute-roofline denominators)
+    fp_peaks = {}
+    for prec, key in ((1, "fp32_tflops"), (0, "fp64_tflops")):
+        v = __import__("ctypes").c_double()
+        S._lib.check(lib.sbec_measure_fma_peak(prec, __import__("ctypes").byref(v)))
+        fp_peaks[key] = v.value
+    fp_peaks["how"] = "sbec_measure_fma_peak: register-resident FMA chains, 2048 threads/SM, CUDA events"
+
     # ---- plain FP64 form on the same workload
     plain = None
     if not args.no_plain:
         p_steps = max(50, steps // 5)
-        ws64 = make("fp64", p_steps, p_steps + 1)
+        ws64 = make("fp64", p_steps, SAVE_EVERY)
         ms64, _ = timed_runs(ws64, max(1, args.steps // 2), 1)
         ws64.close()
         ms64 = dist.max(ms64)
         v64 = dist.world * units_per_run(p_steps) * max(1, args.steps // 2) / (ms64 / 1e3)
-        plain = {"value": v64, "unit": UNIT, "steps_per_run": p_steps}
+        steps_per_s = p_steps * max(1, args.steps // 2) / (ms64 / 1e3)
+        # FFT flops per step by the 5 N log2 N convention: a forward and an inverse 2-D
+        # transform of each component (the pointwise stages are not counted)
+        npts = N_GRID[0] * N_GRID[1]
+        fft_flops = 2 * 5.0 * (2 * F + 1) * npts * math.log2(npts)
+        plain = {"value": v64, "unit": UNIT, "steps_per_run": p_steps,
+                 "fft_tflops": fft_flops * steps_per_s / 1e12,
+                 "fp64_peak_tflops_measured": fp_peaks.get("fp64_tflops"),
+                 "fft_frac_of_fp64_peak": (fft_flops * steps_per_s / 1e12 / fp_peaks["fp64_tflops"])
+                 if fp_peaks.get("fp64_tflops") else None}
 
     # ---- error of the FP32-bulk run against the plain FP64 form (itself within 1e-10 of
     # the oracle in the parity tests) after the full 5000-step run
@@ -641,7 +732,7 @@ def main_gpu(args) -> None:
         log("serving done")
     dipolar = None
     if not args.no_3d:
-        dipolar = bench_3d_f6(S, n=args.grid_3d)
+        dipolar = bench_3d_f6(S, n=args.grid_3d, fp32_peak=fp_peaks.get("fp32_tflops"))
         log("3d f6 done")
 
     cpu = None
@@ -654,6 +745,8 @@ def main_gpu(args) -> None:
             "warmup": args.warmup, "ms_per_step": ms32 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "grid": list(N_GRID), "components": 2 * F + 1, "steps_per_run": steps,
+                       "save_every": SAVE_EVERY,
+                       "save_points": "energy, norm, Mz and a pinned host copy of psi at each (pipelined)",
                        "precision": "fp32 bulk (FFTs, phases), fp64 reductions", "parallelism": "replicas",
                        "l2": "flushed (256 MB write) between timed runs; psi (1.5 MB) stays L2-resident within a run"},
             "e2e": e2e,
@@ -668,7 +761,16 @@ def main_gpu(args) -> None:
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": traffic, "peak_source": peak_src,
                          "bytes_per_launch": per_launch_bytes, "us_per_launch": per_launch_s * 1e6,
-                         "step_algorithmic_gbs": value * 49.3 / 1e9, "kernel_time_share": kernel_share},
+                         "timing": "autotuner burst: 8 back-to-back launches of the chosen variant, median of 3"
+                                   if burst_us else "per-launch CUDA events (profiled run)",
+                         "us_per_launch_profiled": profiled_s * 1e6,
+                         "run_algorithmic_bytes": run_bytes,
+                         "step_algorithmic_gbs": run_bytes / (ms32 / args.steps / 1e3) / 1e9,
+                         "step_frac": run_bytes / (ms32 / args.steps / 1e3) / 1e9 / hbm,
+                         "kernel_time_share": kernel_share,
+                         "note": "the 1.5 MB state is L2-resident within a run: a latency figure, not HBM"},
+            "roofline_batched": batched["row_pass_roofline"] if batched else None,
+            "fp_peaks_measured": fp_peaks,
             "cpu_baseline": cpu,
             "clocks": clk,
             "gpu_launches": launches,
@@ -748,7 +850,7 @@ def main():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-quickstart", action="store_true")
     ap.add_argument("--no-3d", action="store_true")
-    ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--serve-requests", type=int, default=200)
     ap.add_argument("--only", default=None, choices=["batched", "serving", "3d", "quickstart"],
                     help="run one optional section alone and print its JSON")
     ap.add_argument("--grid-3d", type=int, default=128)

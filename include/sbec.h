@@ -241,6 +241,14 @@ sbec_status sbec_classify_phase(sbec_ws* ws, sbec_phase_info* out);
 typedef struct sbec_batch sbec_batch;
 sbec_status sbec_batch_create(const sbec_config* cfg, int32_t n_solves, const double* c0, const double* c1,
                               const double* psi, const double* V, sbec_batch** out);
+/* A batch of solves on different grids (cfg->ndim axes each): solve i has n[3i..3i+2] points and
+ * box L[3i..3i+2], couplings c0[i], c1[i], host psi[i] (reference layout of its grid) and potential
+ * V[i] (n points, or V = NULL for none).  Solves are grouped by grid inside the batch; solves of one
+ * grid must pass the same potential values.  The groups advance concurrently (own stream each) in
+ * sbec_batch_ground_state; every other batch call addresses solves by their index i. */
+sbec_status sbec_batch_create_grids(const sbec_config* cfg, int32_t n_solves, const int32_t* n, const double* L,
+                                    const double* c0, const double* c1, const double* const* psi,
+                                    const double* const* V, sbec_batch** out);
 sbec_status sbec_batch_destroy(sbec_batch* b);
 sbec_status sbec_batch_ground_state(sbec_batch* b, int64_t n_steps, double tol, int64_t check_every,
                                     sbec_gs_result* out);
@@ -289,6 +297,12 @@ sbec_status sbec_tune_table_export(char* buf, int64_t cap, int64_t* len);
  * FP32 results may differ between processes at the level of FP32 rounding.  Entries whose
  * variant is not compiled for a shape are ignored there.  No counterpart in the reference. */
 sbec_status sbec_tune_table_import(const char* text);
+
+/* Measured FMA throughput of the current device in TFLOP/s (2 flops per FMA), FP32
+ * (precision = SBEC_FP32_BULK) or FP64 (SBEC_FP64): eight register-resident FMA chains per
+ * thread, 2048 threads per SM, best of three CUDA-event timings.  The denominators of the
+ * compute rooflines; no counterpart in the reference. */
+sbec_status sbec_measure_fma_peak(int32_t precision, double* tflops);
 
 /* ---- allocation-free reduction --------------------------------------------
  * No counterpart in the reference: an extra entry point for callers that cannot

@@ -1974,3 +1974,95 @@ def psi_to_interleaved(psi: np.ndarray) -> np.ndarray:
 def interleaved_to_psi(buf: np.ndarray, n_points: Sequence[int], D: int) -> np.ndarray:
     c = np.asarray(buf, dtype=np.float64).view(np.complex128)
     return np.asfortranarray(c.reshape(tuple(n_points) + (D,), order="F"))
+
+
+# ----------------------------------------------------------------------------
+# Experiment runner  (src/experiment.jl, src/experiment_runner.jl:36-168)
+# ----------------------------------------------------------------------------
+
+def _exp_ramp(v):
+    """``_parse_ramp_or_constant`` (src/experiment.jl:201-209): (from, to) or a constant."""
+    if isinstance(v, dict):
+        return (float(v["from"]), float(v["to"])) if "to" in v else (float(v["from"]), float(v["from"]))
+    return (float(v), float(v))
+
+
+def _exp_potential(pc: dict, grid: Grid):
+    t = str(pc.get("type", "none"))
+    if t == "none":
+        return None
+    return harmonic_potential(grid, tuple(float(w) for w in pc["omega"]))
+
+
+def run_experiment(d: dict, seed: int = 42) -> dict:
+    """``run_experiment`` (src/experiment_runner.jl:54-155) on the parsed YAML mapping: an optional
+    ground state, then each phase in a new workspace that starts from the previous psi at the
+    running time offset, with ``_build_zeeman`` ramps (:36-52) and ``_add_noise!`` (:157-168,
+    noise from PCG64(seed + phase index), complex normal of unit variance)."""
+    d = d.get("experiment", d)
+    sd = d["system"]
+    atom = {"Rb87": Rb87, "Na23": Na23, "Eu151": Eu151}[str(sd["atom"])]
+    npts = tuple(int(v) for v in sd["grid"]["n_points"])
+    box = tuple(float(v) for v in sd["grid"]["box_size"])
+    grid = make_grid(GridConfig(npts, box))
+    inter = sd["interactions"]
+    ks = [int(k[1:]) for k in inter if k[0] == "c" and k[1:].isdigit() and int(k[1:]) >= 2]
+    c_extra = tuple(float(inter.get(f"c{n}", 0.0)) for n in range(2, max(ks) + 1)) if ks else ()
+    ip = InteractionParams(float(inter["c0"]), float(inter["c1"]), float(inter.get("c_lhy", 0.0)), c_extra)
+    loss = None
+    if "losses" in sd:
+        loss = LossParams(float(sd["losses"].get("gamma_dr", 0.0)), float(sd["losses"].get("L3", 0.0)))
+    psi = None
+    gs_E = gs_conv = None
+    prev_pot = None
+    if "ground_state" in d:
+        g = d["ground_state"]
+        z = g.get("zeeman", {})
+        prev_pot = g.get("potential", {"type": "none"})
+        r = find_ground_state(grid=grid, atom=atom, interactions=ip,
+                              zeeman=ZeemanParams(float(z.get("p", 0.0)), float(z.get("q", 0.0))),
+                              V=_exp_potential(prev_pot, grid), dt=float(g["dt"]), n_steps=int(g["n_steps"]),
+                              tol=float(g["tol"]), initial_state=str(g.get("initial_state", "polar")))
+        gs_E, gs_conv = r["energy"], r["converged"]
+        psi = r["workspace"].psi.copy(order="F")
+    results = []
+    t_offset = 0.0
+    for i, ph in enumerate(d.get("sequence", [])):
+        pc = ph.get("potential", prev_pot)
+        prev_pot = pc
+        dt, duration = float(ph["dt"]), float(ph["duration"])
+        save_every = int(ph.get("save_every", 1))
+        z = ph.get("zeeman", {})
+        (p0, p1), (q0, q1) = _exp_ramp(z.get("p", 0.0)), _exp_ramp(z.get("q", 0.0))
+        if p0 == p1 and q0 == q1:
+            zee = ZeemanParams(p0, q0)
+        else:
+            def zee(t, t0=t_offset, dur=duration, p0=p0, p1=p1, q0=q0, q1=q1):
+                f = min(max((t - t0) / dur if dur > 0 else 0.0, 0.0), 1.0)
+                return ZeemanParams(p0 + (p1 - p0) * f, q0 + (q1 - q0) * f)
+        n_steps = int(round(duration / dt))
+        ws = make_workspace(grid=grid, atom=atom, interactions=ip, zeeman=zee, V=_exp_potential(pc, grid),
+                            sim_params=SimParams(dt, n_steps, False, None, save_every), psi_init=psi, loss=loss)
+        ws.t = t_offset
+        amp = ph.get("noise_amplitude")
+        if amp is not None and float(amp) > 0:
+            D = ws.psi.shape[-1]
+            dom = int(np.argmax([float(np.sum(np.abs(ws.psi[..., c]) ** 2)) for c in range(D)]))
+            rng = np.random.Generator(np.random.PCG64(seed + i))
+            shp = ws.psi.shape[:-1]
+            for c in range(D):
+                if c != dom:
+                    ws.psi[..., c] += float(amp) * (rng.standard_normal(shp) + 1j * rng.standard_normal(shp)) / math.sqrt(2.0)
+            ws.psi /= math.sqrt(float(np.sum(np.abs(ws.psi) ** 2)) * cell_volume(grid))
+        if "adaptive_dt" in ph:
+            a = ph["adaptive_dt"]
+            ad = AdaptiveDtParams(dt_init=float(a.get("dt_init", dt)), dt_min=float(a.get("dt_min", 1e-5)),
+                                  dt_max=float(a.get("dt_max", 10 * dt)), tol=float(a.get("tol", 1e-3)),
+                                  error_mode=str(a.get("error_mode", "step_change")))
+            res = run_simulation_adaptive(ws, ad, t_offset + duration, dt * save_every)["result"]
+        else:
+            res = run_simulation(ws)
+        psi = ws.psi.copy(order="F")
+        t_offset += duration
+        results.append(res)
+    return dict(ground_state_energy=gs_E, ground_state_converged=gs_conv, phase_results=results, psi=psi)
