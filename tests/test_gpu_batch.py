@@ -82,3 +82,37 @@ def test_batch_fp32_merged_step_energy(gpu):
         ro = O.find_ground_state(grid=og, atom=O.Rb87, interactions=O.InteractionParams(10.0, c1),
                                  V=O.harmonic_potential(og, (1.0, 1.0)), psi_init=p0, **kw)
         assert abs(r["energy"] - ro["energy"]) / abs(ro["energy"]) < 1e-6
+
+
+def test_batch_on_mixed_grids_matches_per_grid_batches(gpu):
+    """One batch object over solves on three grids (sbec_batch_create_grids: grouped by grid,
+    the groups advance concurrently) gives each solve the result of a batch of its own grid,
+    and the FP64 results match the oracle's find_ground_state per solve."""
+    sizes = [32, 16, 32, 64, 16, 64]
+    grids_o = {n: O.make_grid(O.GridConfig((n, n), (16.0, 16.0))) for n in set(sizes)}
+    grids_s = {n: S.make_grid(S.GridConfig((n, n), (16.0, 16.0))) for n in set(sizes)}
+    states = ["polar", "ferromagnetic", "random", "uniform", "random", "antiferromagnetic"]
+    c1s = [-0.5, 0.3, 0.1, -0.2, 0.6, 0.0]
+    psis = [O.init_psi(grids_o[n], 1, st, seed=40 + i) for i, (n, st) in enumerate(zip(sizes, states))]
+    kw = dict(zeeman=S.ZeemanParams(0.1, 0.05), potential=S.HarmonicTrap(1.0, 1.0), dt=0.005, precision="fp64")
+    mixed = S.GroundStateBatch(grids=[grids_s[n] for n in sizes], atom=S.Rb87, c0s=[10.0] * 6, c1s=c1s,
+                               psi_inits=psis, **kw)
+    rm = mixed.ground_state(200, 1e-9)
+    pm = [mixed.psi(i) for i in range(6)]
+    mixed.close()
+    for n in set(sizes):
+        idx = [i for i, m in enumerate(sizes) if m == n]
+        b = S.GroundStateBatch(grid=grids_s[n], atom=S.Rb87, c0s=[10.0] * len(idx), c1s=[c1s[i] for i in idx],
+                               psi_inits=[psis[i] for i in idx], **kw)
+        rb = b.ground_state(200, 1e-9)
+        for k, i in enumerate(idx):
+            assert rb[k] == rm[i]
+            assert np.array_equal(b.psi(k), pm[i])
+        b.close()
+    for i, n in enumerate(sizes):
+        ro = O.find_ground_state(grid=grids_o[n], atom=O.Rb87, interactions=O.InteractionParams(10.0, c1s[i]),
+                                 zeeman=O.ZeemanParams(0.1, 0.05), V=O.harmonic_potential(grids_o[n], (1.0, 1.0)),
+                                 psi_init=psis[i], dt=0.005, n_steps=200, tol=1e-9)
+        assert rm[i]["steps"] == ro["steps"] and rm[i]["converged"] == ro["converged"]
+        assert abs(rm[i]["energy"] - ro["energy"]) <= ENERGY_TOL_FP64 * 10 * abs(ro["energy"])
+        assert rel_psi_err(pm[i], ro["workspace"].psi) < PSI_TOL_FP64

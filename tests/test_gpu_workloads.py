@@ -217,6 +217,9 @@ def test_batch_256_fp32_converged_energy(gpu):
     # both forms at the end of their runs.
     worst = max(abs(a["energy"] - b["energy"]) / abs(b["energy"]) for a, b in zip(r32, r64))
     n32, n64 = sum(a["converged"] for a in r32), sum(b["converged"] for b in r64)
+    for a, b in zip(r32, r64):
+        print(f"  fp32 steps {a['steps']} dE {a['dE']:.2e} dpsi {a['dpsi']:.2e} | "
+              f"fp64 steps {b['steps']} dE {b['dE']:.2e} dpsi {b['dpsi']:.2e}")
     print(f"FP32 vs FP64 batched 256^2 ground states: converged {n32} (FP32) / {n64} (FP64) of 8, "
           f"max energy error {worst:.2e}")
     assert worst < ENERGY_TOL_FP32
