@@ -156,6 +156,9 @@ class EngineBase {
   // row pass plus the last-axis pass; an ITP split_step defers its renormalisation
   // into the next row pass.
   virtual bool fused_path() const = 0;
+  // Smallest relative change of psi the form can resolve: 0 in FP64; in FP32 eight units in
+  // the last place (2^-21), below which max|psi - psi_prev| / max|psi| is rounding noise.
+  virtual double psi_resolution() const = 0;
   virtual std::string tuning_report() const = 0;  // autotuner decisions of this engine
   virtual void lf_open(double dt) = 0;               // V(dt/2), forward x
   virtual void lf_steps(long long n, double dt) = 0;  // n x [K(dt) with merged V(dt)]

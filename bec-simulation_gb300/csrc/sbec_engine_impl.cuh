@@ -623,6 +623,8 @@ class Engine final : public EngineBase {
     download_real3(phi_per_, host3N);
   }
 
+  double psi_resolution() const override { return sizeof(R) == 4 ? std::ldexp(1.0, -21) : 0.0; }
+
   // ---------------- fused paths ----------------
   bool fused_path() const override {
     if (s_.ddi || s_.tensor || s_.raman || s_.loss) return false;
