@@ -116,3 +116,43 @@ def test_batch_on_mixed_grids_matches_per_grid_batches(gpu):
         assert rm[i]["steps"] == ro["steps"] and rm[i]["converged"] == ro["converged"]
         assert abs(rm[i]["energy"] - ro["energy"]) <= ENERGY_TOL_FP64 * 10 * abs(ro["energy"])
         assert rel_psi_err(pm[i], ro["workspace"].psi) < PSI_TOL_FP64
+
+
+def test_batch_spin2_fp64_against_oracle(gpu):
+    """Spin-2 solves (five components, spin mixing by the Euler rotation) in one batch."""
+    og = O.make_grid(O.GridConfig((32, 32), (16.0, 16.0)))
+    hg = S.make_grid(S.GridConfig((32, 32), (16.0, 16.0)))
+    states = ["polar", "ferromagnetic", "random", "uniform"]
+    c1s = [0.5, -0.5, 0.2, -0.1]
+    psis = [O.init_psi(og, 2, st, seed=70 + i) for i, st in enumerate(states)]
+    b = S.GroundStateBatch(grid=hg, atom=S.AtomSpecies("f2", 2), c0s=[10.0] * 4, c1s=c1s, psi_inits=psis,
+                           potential=S.HarmonicTrap(1.0, 1.0), dt=0.005, precision="fp64")
+    res = b.ground_state(200, 1e-9)
+    for i, (p0, c1, r) in enumerate(zip(psis, c1s, res)):
+        ro = O.find_ground_state(grid=og, atom=O.AtomSpecies("f2", 2), interactions=O.InteractionParams(10.0, c1),
+                                 V=O.harmonic_potential(og, (1.0, 1.0)), psi_init=p0, dt=0.005, n_steps=200, tol=1e-9)
+        assert r["steps"] == ro["steps"] and r["converged"] == ro["converged"]
+        assert abs(r["energy"] - ro["energy"]) <= ENERGY_TOL_FP64 * 10 * abs(ro["energy"])
+        assert rel_psi_err(b.psi(i), ro["workspace"].psi) < PSI_TOL_FP64
+    b.close()
+
+
+def test_tune_table_import_fixes_the_variant(gpu):
+    """A shape found in an imported tune table is not timed again: the workspace reports the
+    table's variant, and an exported table loads back unchanged."""
+    g = S.make_grid(S.GridConfig((64, 64), (16.0, 16.0)))
+    ws = S.make_workspace(grid=g, atom=S.Rb87, interactions=S.InteractionParams(10.0, 0.5),
+                          potential=S.HarmonicTrap(1.0, 1.0), sim_params=S.SimParams(1e-3, 20, False, None, 10),
+                          precision="fp32")
+    S.run_simulation(ws, keep_psi=False)
+    table = S.tune_table_export()
+    ws.close()
+    assert "fp32 row" in table
+    S.tune_table_import(table)
+    ws2 = S.make_workspace(grid=g, atom=S.Rb87, interactions=S.InteractionParams(10.0, 0.5),
+                           potential=S.HarmonicTrap(1.0, 1.0), sim_params=S.SimParams(1e-3, 20, False, None, 10),
+                           precision="fp32")
+    S.run_simulation(ws2, keep_psi=False)
+    assert "from the process table" in ws2.tuning_report
+    assert " chosen v" not in ws2.tuning_report  # nothing was timed
+    ws2.close()
