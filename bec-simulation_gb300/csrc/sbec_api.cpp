@@ -869,7 +869,8 @@ sbec_status sbec_ground_state(sbec_ws* ws, int64_t n_steps, double tol, int64_t 
       const double dpsi = pmax > 0 ? dmax / pmax : 0.0;
       final_dE = dE;
       final_dpsi = dpsi;
-      if (dE < tol && dpsi < std::max(tol, e.psi_resolution())) {
+      if (dE < std::max(tol, 0.5 * e.psi_resolution() * std::fabs(En)) &&
+          dpsi < std::max(tol, e.psi_resolution())) {
         converged = true;
         break;
       }
@@ -935,7 +936,8 @@ sbec_status sbec_ground_state_adaptive(sbec_ws* ws, int64_t n_steps, double tol,
       const double dpsi = pmax > 0 ? dmax / pmax : 0.0;
       final_dE = dE;
       final_dpsi = dpsi;
-      if (dE < tol && dpsi < std::max(tol, e.psi_resolution())) {
+      if (dE < std::max(tol, 0.5 * e.psi_resolution() * std::fabs(En)) &&
+          dpsi < std::max(tol, e.psi_resolution())) {
         converged = true;
         break;
       }
@@ -1069,7 +1071,8 @@ void batch_ground_state(EngineBase& e, int64_t n_steps, double tol, int64_t chec
         const double dpsi = pmax[s] > 0 ? dmax[s] / pmax[s] : 0.0;
         out[s].dE = dE;
         out[s].dpsi = dpsi;
-        if (dE < tol && dpsi < std::max(tol, e.psi_resolution())) {
+        if (dE < std::max(tol, 0.5 * e.psi_resolution() * std::fabs(E[s])) &&
+            dpsi < std::max(tol, e.psi_resolution())) {
           out[s].converged = 1;
           out[s].energy = E[s];
           out[s].steps = step;

@@ -245,9 +245,43 @@ struct DdiGeom {
   int ndim;
 };
 
+// FP32 form: Q from k in FP32 (the FP64 pipe, ~1/64 of the FP32 rate here, had bound the
+// last-axis DDI pass); Q_ab = k_a k_b / k^2 - delta_ab/3 to FP32 rounding.
+__device__ __forceinline__ void ddi_contract_f32(float2& fx, float2& fy, float2& fz, float kx, float ky, float kz,
+                                                 const DdiGeom& g) {
+  const float k2 = kx * kx + ky * ky + kz * kz;
+  if (k2 == 0.0f) {
+    fx = fy = fz = make_float2(0.f, 0.f);
+    return;
+  }
+  const float inv = 1.0f / k2;
+  const float C = (float)g.C;
+  if (g.secular) {
+    const float qzz = kz * kz * inv - (1.0f / 3.0f);
+    const float qxx = -0.5f * qzz;
+    fx = (C * qxx) * fx;
+    fy = (C * qxx) * fy;
+    fz = (C * qzz) * fz;
+    return;
+  }
+  const float qxx = kx * kx * inv - (1.0f / 3.0f), qyy = ky * ky * inv - (1.0f / 3.0f),
+              qzz = kz * kz * inv - (1.0f / 3.0f);
+  const float qxy = kx * ky * inv, qxz = kx * kz * inv, qyz = ky * kz * inv;
+  const float2 px = C * (qxx * fx + qxy * fy + qxz * fz);
+  const float2 py = C * (qxy * fx + qyy * fy + qyz * fz);
+  const float2 pz = C * (qxz * fx + qyz * fy + qzz * fz);
+  fx = px;
+  fy = py;
+  fz = pz;
+}
+
 template <typename R>
 __device__ __forceinline__ void ddi_contract(cplx<R>& fx, cplx<R>& fy, cplx<R>& fz, double kx, double ky,
                                              double kz, const DdiGeom& g) {
+  if constexpr (sizeof(R) == 4) {
+    ddi_contract_f32(fx, fy, fz, (float)kx, (float)ky, (float)kz, g);
+    return;
+  }
   const double k2 = kx * kx + ky * ky + kz * kz;
   if (k2 == 0.0) {
     fx = fy = fz = mk<R>(0, 0);
@@ -443,20 +477,36 @@ k_ddi_last(cplx<R>* __restrict__ spec, DdiGeom g, int64_t S, int64_t inner, int 
   for (int f = tid; f < W * M; f += blockDim.x) {
     const int i = f / W, w = f % W;
     const int64_t pos = i0 + w;
-    double kx, ky, kz;
-    if (g.ndim == 2) {
-      kx = (double)pos * g.kmx;
-      ky = (double)freq_index(i, M) * g.kmy;
-      kz = 0.0;
-    } else {
-      kx = (double)(pos % g.Hx) * g.kmx;
-      ky = (double)freq_index((int)(pos / g.Hx), g.My) * g.kmy;
-      kz = (double)freq_index(i, M) * g.kmz;
-    }
     cplx<R>& ax = s[i * NL + 0 * W + w];
     cplx<R>& ay = s[i * NL + 1 * W + w];
     cplx<R>& az = s[i * NL + 2 * W + w];
-    ddi_contract<R>(ax, ay, az, kx, ky, kz, g);
+    if constexpr (sizeof(R) == 4) {
+      // frequency indices times the k multipliers, all in FP32 (the FP64 pipe is slow here)
+      float kx, ky, kz;
+      if (g.ndim == 2) {
+        kx = (float)pos * (float)g.kmx;
+        ky = (float)freq_index(i, M) * (float)g.kmy;
+        kz = 0.0f;
+      } else {
+        const int p = (int)pos;  // < Hx * My, which fits an int
+        kx = (float)(p % g.Hx) * (float)g.kmx;
+        ky = (float)freq_index(p / g.Hx, g.My) * (float)g.kmy;
+        kz = (float)freq_index(i, M) * (float)g.kmz;
+      }
+      ddi_contract_f32(ax, ay, az, kx, ky, kz, g);
+    } else {
+      double kx, ky, kz;
+      if (g.ndim == 2) {
+        kx = (double)pos * g.kmx;
+        ky = (double)freq_index(i, M) * g.kmy;
+        kz = 0.0;
+      } else {
+        kx = (double)(pos % g.Hx) * g.kmx;
+        ky = (double)freq_index((int)(pos / g.Hx), g.My) * g.kmy;
+        kz = (double)freq_index(i, M) * g.kmz;
+      }
+      ddi_contract<R>(ax, ay, az, kx, ky, kz, g);
+    }
   }
   __syncthreads();
   fft_tile<R, M, +1>(s, NL, 1, line, t, tw);

@@ -476,7 +476,7 @@ def bench_3d_f6(S, n: int = 128, steps32: int = 200, steps64: int = 20, fp32_pea
         ws.close()
         ws = make(prec)
         t0 = time.perf_counter()
-        r = S.run_simulation_yoshida(ws, S.AdaptiveDtParams(dt_init=1e-3), t_end=1.0, save_interval=1.0,
+        r = S.run_simulation_yoshida(ws, S.AdaptiveDtParams(dt_init=1e-3), t_end=100.0, save_interval=100.0,
                                      keep_psi=False, max_accepted=k)
         secs = time.perf_counter() - t0
         acc = int(r["n_accepted"])

@@ -186,9 +186,9 @@ sbec_status sbec_run_yoshida(sbec_ws* ws, const sbec_adaptive_params* p, double 
 /* The ITP loop of find_ground_state on an existing ITP workspace (src/ground_state.jl:116-169):
  * convergence checked every check_every steps; target_Mz = NaN disables the constraint.
  * Convergence (here, in sbec_ground_state_adaptive and in batches) is the reference's
- * dE < tol && dpsi < tol, evaluated in FP64; in the FP32-bulk form the psi test uses
- * max(tol, 2^-21), the resolution of an FP32 wavefunction, since a smaller relative change of
- * max|psi| is rounding noise that never settles. */
+ * dE < tol && dpsi < tol, evaluated in FP64; in the FP32-bulk form the tests use
+ * dE < max(tol, 2^-22 |E|) and dpsi < max(tol, 2^-21), the resolution of an FP32 wavefunction
+ * and of its energy, since smaller changes are rounding noise that never settles. */
 sbec_status sbec_ground_state(sbec_ws* ws, int64_t n_steps, double tol, int64_t check_every,
                               double target_Mz, sbec_gs_result* out);
 /* _find_ground_state_adaptive (src/ground_state.jl:172-237) on an existing ITP workspace with
