@@ -627,7 +627,7 @@ class Engine final : public EngineBase {
 
   // ---------------- fused paths ----------------
   bool fused_path() const override {
-    if (s_.ddi || s_.tensor || s_.raman || s_.loss) return false;
+    if (!s_.pow2 || s_.ddi || s_.tensor || s_.raman || s_.loss) return false;
     if (!(s_.D == 1 || s_.D == 3 || s_.D == 5)) return false;
     const int nx = s_.n[0];
     if (nx < 16 || nx > 4096) return false;
@@ -1348,8 +1348,10 @@ class Engine final : public EngineBase {
       p.tab[a].lo = ptab_lo_[a];
       p.n[a] = s_.n[a];
     }
-    p.scale0 = (R)(1.0 / (double)N_);  // N_ is a power of two: exact
-    p.unbiased = (sizeof(R) == 4 && phase_itp_ == 0) ? 1 : 0;
+    p.scale0 = (R)(1.0 / (double)N_);  // exact when N_ is a power of two
+    // the unbiased FP32 form needs the exact power-of-two scale; other grids use the
+    // compensated product
+    p.unbiased = (sizeof(R) == 4 && phase_itp_ == 0 && s_.pow2) ? 1 : 0;
     return p;
   }
 
@@ -1546,9 +1548,105 @@ class Engine final : public EngineBase {
          (double)sizeof(cplx<R>) * (double)(n_in + n_out) * (double)inner * (double)outer);
   }
 
+  // ---- axes of non-power-of-two length (Bluestein, k_blue_*): per (n, direction) the chirp
+  // w_j = exp(sign i pi (j^2 mod 2n) / n) and the M-point FFT of conj(w) placed at m and M - m.
+  struct BlueTab {
+    int M = 0;
+    cplx<R>* chirp = nullptr;
+    cplx<R>* bhat = nullptr;
+  };
+
+  const BlueTab& blue_tab(int n, int sign) {
+    const int key = sign > 0 ? n : -n;
+    auto it = blue_.find(key);
+    if (it != blue_.end()) return it->second;
+    int M = 1;
+    while (M < 2 * n - 1) M *= 2;
+    const long double pi = 3.141592653589793238462643383279502884L;
+    std::vector<cplx<R>> w(n), b((size_t)M, mk<R>(0, 0));
+    for (int j = 0; j < n; ++j) {
+      const long long jj = ((long long)j * j) % (2LL * n);
+      const long double ang = (long double)sign * pi * (long double)jj / (long double)n;
+      w[j] = mk<R>((R)std::cos(ang), (R)std::sin(ang));
+      const cplx<R> cw = mk<R>((R)std::cos(ang), (R)(-std::sin(ang)));
+      b[j] = cw;
+      if (j > 0) b[(size_t)M - j] = cw;
+    }
+    BlueTab t;
+    t.M = M;
+    t.chirp = alloc<cplx<R>>(n);
+    t.bhat = alloc<cplx<R>>(M);
+    upload(t.chirp, w.data(), w.size());
+    upload(t.bhat, b.data(), b.size());
+    fft_x_n(M, t.bhat, 1, 0);  // forward transform in place
+    sync();
+    return blue_[key] = t;
+  }
+
+  // Unnormalised transform of every line of axis `axis` (sign -1 forward, +1 inverse) for an
+  // axis whose length is not a power of two.
+  void blue_axis(cplx<R>* buf, int axis, int sign) {
+    const int n = s_.n[axis];
+    int64_t inner = 1;
+    for (int a = 0; a < axis; ++a) inner *= s_.n[a];
+    const int64_t outer = nc_ / (inner * n);
+    const BlueTab& t = blue_tab(n, sign);
+    const int M = t.M;
+    const size_t need = (size_t)outer * M * inner;
+    if (need > blue_scr_n_) {
+      blue_scr_ = alloc<cplx<R>>(need);
+      blue_scr_n_ = need;
+    }
+    pb();
+    k_blue_pre<R><<<grid_for((int64_t)need), 256, 0, stream_>>>(buf, blue_scr_, n, M, inner, (int64_t)need, t.chirp);
+    done("blue", (double)sizeof(cplx<R>) * ((double)nc_ + (double)need));
+    auto line_fft = [&](int mode) {
+      if (inner == 1)
+        fft_x_n(M, blue_scr_, outer, mode);
+      else
+        fft_strided_n(M, blue_scr_, inner, inner, outer, (int64_t)M * inner, M, M, mode);
+    };
+    line_fft(0);
+    pb();
+    k_blue_mid<R><<<grid_for((int64_t)need), 256, 0, stream_>>>(blue_scr_, M, inner, (int64_t)need, t.bhat);
+    done("blue", 2.0 * (double)sizeof(cplx<R>) * (double)need);
+    line_fft(1);
+    pb();
+    k_blue_post<R><<<grid_for(nc_), 256, 0, stream_>>>(blue_scr_, buf, n, M, inner, nc_, t.chirp, (R)(1.0 / M));
+    done("blue", (double)sizeof(cplx<R>) * 2.0 * (double)nc_);
+  }
+
+  // One axis of the unnormalised transform: the line kernels for a power-of-two length,
+  // Bluestein otherwise.
+  void fft_axis(cplx<R>* buf, int axis, int sign) {
+    const int n = s_.n[axis];
+    if (n & (n - 1)) {
+      blue_axis(buf, axis, sign);
+      return;
+    }
+    const int mode = sign < 0 ? 0 : 1;
+    if (axis == 0) {
+      fft_x_n(n, buf, nc_ / n, mode);
+      return;
+    }
+    int64_t inner = 1;
+    for (int a = 0; a < axis; ++a) inner *= s_.n[a];
+    fft_strided_n(n, buf, inner, inner, nc_ / (inner * n), inner * n, n, n, mode);
+  }
+
   // Full spatial FFT of a D-component buffer: forward only (kinetic=false), or the
   // kinetic step fwd -> phase -> inv (kinetic=true).
   void fft_full(cplx<R>* buf, bool kinetic) {
+    if (!s_.pow2) {
+      // a non-power-of-two axis: forward on every axis, the kinetic phase, inverse on every axis
+      for (int a = 0; a < s_.ndim; ++a) fft_axis(buf, a, -1);
+      if (!kinetic) return;
+      pb();
+      k_kinetic_apply<R><<<grid_for(nc_), 256, 0, stream_>>>(buf, N_, nc_, phase_ref());
+      done("kinetic_phase", 2.0 * (double)sizeof(cplx<R>) * (double)nc_);
+      for (int a = s_.ndim - 1; a >= 0; --a) fft_axis(buf, a, +1);
+      return;
+    }
     const int nd = s_.ndim;
     const int nx = s_.n[0], ny = s_.n[1], nz = s_.n[2];
     const int64_t D = s_.D;
@@ -1986,6 +2084,9 @@ class Engine final : public EngineBase {
   cplx<R>* ptab_[3] = {nullptr, nullptr, nullptr};
   cplx<R>* ptab_lo_[3] = {nullptr, nullptr, nullptr};
   std::map<int, Tw<R>> tw_;
+  std::map<int, BlueTab> blue_;  // Bluestein tables by +-n
+  cplx<R>* blue_scr_ = nullptr;
+  size_t blue_scr_n_ = 0;
   double* partials_ = nullptr;
   size_t partials_n_ = 0;
   double* results_ = nullptr;

@@ -98,6 +98,63 @@ __device__ __forceinline__ float2 kinetic_rot(float2 x, const PhaseRef<float>& p
   return mk<float>(sr_add(xs.x, bx, 0x85ebca6bu), sr_add(xs.y, by, 0xc2b2ae35u));
 }
 
+// ---------------------------------------------------------------------------
+// Axes whose length n is not a power of two: Bluestein's identity
+//   X_k = w_k sum_j (x_j w_j) conj(w_{k-j}),  w_j = exp(-+ i pi j^2 / n),
+// a circular convolution of length M >= 2n - 1 (a power of two) done with the power-of-two
+// line kernels: chirp and zero-pad (k_blue_pre), forward M-point FFT, multiply by the
+// M-point FFT of the chirp (k_blue_mid), inverse M-point FFT, chirp, scale 1/M and keep the
+// first n points (k_blue_post).  The lines of an axis with element stride `inner` (the product
+// of the lower axis lengths) are laid out in the scratch as [outer][j][inner], so both the
+// grid and the scratch are read and written with inner fastest (coalesced), and the M-point
+// transforms run as strided lines of the same geometry (contiguous lines when inner = 1).
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void k_blue_pre(const cplx<R>* __restrict__ src, cplx<R>* __restrict__ scr, int n, int M, int64_t inner,
+                           int64_t total, const cplx<R>* __restrict__ chirp) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i_in = q % inner, r = q / inner;
+    const int j = (int)(r % M);
+    const int64_t i_out = r / M;
+    scr[q] = j < n ? src[i_in + (int64_t)j * inner + i_out * inner * n] * __ldg(chirp + j) : mk<R>(0, 0);
+  }
+}
+
+template <typename R>
+__global__ void k_blue_mid(cplx<R>* __restrict__ scr, int M, int64_t inner, int64_t total,
+                           const cplx<R>* __restrict__ bhat) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x)
+    scr[q] = scr[q] * __ldg(bhat + (q / inner) % M);
+}
+
+template <typename R>
+__global__ void k_blue_post(const cplx<R>* __restrict__ scr, cplx<R>* __restrict__ dst, int n, int M, int64_t inner,
+                            int64_t total, const cplx<R>* __restrict__ chirp, R inv_m) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i_in = q % inner, r = q / inner;
+    const int k = (int)(r % n);
+    const int64_t i_out = r / n;
+    const cplx<R> v = scr[(i_out * M + k) * inner + i_in] * __ldg(chirp + k);
+    dst[i_in + (int64_t)k * inner + i_out * inner * n] = inv_m * v;
+  }
+}
+
+// The kinetic phase of a grid with a non-power-of-two axis, applied between the forward and
+// inverse transforms of all axes: the product of the per-axis table entries (1/N folded
+// into the x table), one compensated product per axis in FP32.
+template <typename R>
+__global__ void k_kinetic_apply(cplx<R>* __restrict__ buf, int64_t N, int64_t total, PhaseRef<R> ph) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = q % N;
+    const int i0 = (int)(p % ph.n[0]);
+    const int64_t r = p / ph.n[0];
+    cplx<R> v = phase_mul<R>(buf[q], ph.tab[0], i0, ph.scale0, 0);
+    if (ph.ndim >= 2) v = phase_mul<R>(v, ph.tab[1], (int)(r % ph.n[1]), (R)1, 0);
+    if (ph.ndim == 3) v = phase_mul<R>(v, ph.tab[2], (int)(r / ph.n[1]), (R)1, 0);
+    buf[q] = v;
+  }
+}
+
 // A load of line data: plain (may be served by L1), or CG: through L2 only, for data
 // that other blocks of the same launch wrote (the persistent segment kernel).
 template <bool CG, typename T>

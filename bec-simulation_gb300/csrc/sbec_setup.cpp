@@ -158,10 +158,15 @@ Setup build_setup(const sbec_config& cfg) {
   for (int d = 0; d < s.ndim; ++d) {
     if (cfg.n[d] <= 0 || cfg.n[d] % 2 != 0) fail(SBEC_ERR_INVALID, "n_points must be positive even integers");
     if (!(cfg.L[d] > 0)) fail(SBEC_ERR_INVALID, "box_size must be positive");
-    if (!is_pow2(cfg.n[d]) || cfg.n[d] > 4096 || (s.ndim > 1 && cfg.n[d] > 1024))
+    // power-of-two axes run the line kernels directly; other even sizes (up to 2048) run the
+    // Bluestein transform on power-of-two lines of length >= 2n - 1
+    const bool p2 = is_pow2(cfg.n[d]);
+    if ((p2 && (cfg.n[d] > 4096 || (s.ndim > 1 && cfg.n[d] > 1024))) || (!p2 && cfg.n[d] > (d == 0 ? 2048 : 512)))
       fail(SBEC_ERR_UNSUPPORTED,
            "grid size " + std::to_string(cfg.n[d]) +
-               " unsupported: the GPU path handles power-of-two n (<= 4096 in 1-D, <= 1024 per axis in 2-D/3-D)");
+               " unsupported: the GPU path handles power-of-two n <= 4096 in 1-D and <= 1024 per axis in 2-D/3-D, "
+               "and other even n <= 2048 on the first axis, <= 512 on the others");
+    if (!p2) s.pow2 = false;
     s.n[d] = cfg.n[d];
     s.L[d] = cfg.L[d];
     s.N *= cfg.n[d];
@@ -388,6 +393,8 @@ Setup build_setup(const sbec_config& cfg) {
 
   // --- DDI (src/ddi.jl:51-82, src/ddi_padded.jl:6-49)
   s.ddi = cfg.enable_ddi != 0;
+  if (s.ddi && !s.pow2)
+    fail(SBEC_ERR_UNSUPPORTED, "the dipolar convolution on the GPU path needs power-of-two grid sizes");
   s.secular = cfg.secular_ddi != 0;
   s.padded = s.ddi && cfg.ddi_padding != 0;
   s.c_dd = std::isnan(cfg.c_dd) ? 0.0 : cfg.c_dd;

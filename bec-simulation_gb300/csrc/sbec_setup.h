@@ -24,6 +24,7 @@ struct Setup {
   int n[3] = {1, 1, 1};
   double L[3] = {1, 1, 1};
   long long N = 1;     // spatial points
+  bool pow2 = true;    // every axis a power of two (else the general path with Bluestein axes)
   int F = 0, D = 1;
   double dx[3] = {1, 1, 1};
   double dV = 1;

@@ -52,9 +52,14 @@ def test_invalid_config_rejected_before_device(libsbec):
     import spinorbec as S
 
     g = S.make_grid(S.GridConfig((24,), (8.0,)))
-    with pytest.raises(S.UnsupportedError):  # non power-of-two n (no mixed-radix kernel)
-        S.make_workspace(grid=g, atom=S.Rb87, interactions=S.InteractionParams(1.0, 0.0),
-                         sim_params=S.SimParams(1e-3, 1))
+    kw = dict(atom=S.Rb87, interactions=S.InteractionParams(1.0, 0.0), sim_params=S.SimParams(1e-3, 1))
+    with pytest.raises(S.UnsupportedError):  # the dipolar convolution needs power-of-two axes
+        S.make_workspace(grid=g, enable_ddi=True, c_dd=1.0, **kw)
+    with pytest.raises(S.UnsupportedError):  # Bluestein axes beyond 512 points (y, z)
+        S.make_workspace(grid=S.make_grid(S.GridConfig((8, 600), (8.0, 8.0))), **kw)
+    if S.device_count() == 0:  # a non-power-of-two even n is on the GPU path
+        with pytest.raises(S.DeviceError):
+            S.make_workspace(grid=g, **kw)
     g2 = S.make_grid(S.GridConfig((16,), (8.0,)))
     with pytest.raises(S.UnsupportedError):  # spin F > 6
         S.make_workspace(grid=g2, atom=S.AtomSpecies("x", 7), interactions=S.InteractionParams(1.0, 0.0),
