@@ -979,8 +979,25 @@ __device__ __forceinline__ void rotate_taylor(cplx<R> (&v)[D], R px, R py, R pz,
       cplx<R> t[D];
       nF_apply<R, D>(y, px, py, pz, st, t);
       const R f = dt / (R)k;
+      bool done_k = false;
+      if constexpr (sizeof(R) == 4) {
+        if (k == 1 && !itp) {
+          // the last addition v + (whole correction) rounded without bias: for the small
+          // angles of one step, round-to-nearest keeps a near-axis value outside the circle
+          // (the radial part of the correction is below half an ulp) and |v| grows every call
 #pragma unroll
-      for (int c = 0; c < D; ++c) y[c] = v[c] + (itp ? (-f) * t[c] : mul_mi(f * t[c]));
+          for (int c = 0; c < D; ++c) {
+            const cplx<R> corr = mul_mi(f * t[c]);
+            y[c] = mk<R>(sr_add(v[c].x, corr.x, 0x27d4eb2fu + 0x165667b1u * c),
+                         sr_add(v[c].y, corr.y, 0x9e3779b1u + 0x85ebca77u * c));
+          }
+          done_k = true;
+        }
+      }
+      if (!done_k) {
+#pragma unroll
+        for (int c = 0; c < D; ++c) y[c] = v[c] + (itp ? (-f) * t[c] : mul_mi(f * t[c]));
+      }
     }
 #pragma unroll
     for (int c = 0; c < D; ++c) v[c] = y[c];
@@ -1595,7 +1612,13 @@ __device__ __forceinline__ void tensor_lane(float2& v, const TensorArgs<float>& 
 #pragma unroll
       for (int j = 0; j < D; ++j) t += hrow[j] * yb[j];
       const float f = dtau / (float)k;
-      y = v + (a.itp ? (-f) * t : mul_mi(f * t));
+      if (k == 1 && !a.itp) {
+        // unbiased rounding of the last addition (as in rotate_taylor)
+        const float2 corr = mul_mi(f * t);
+        y = mk<float>(sr_add(v.x, corr.x, 0x27d4eb2fu + 0x165667b1u * c), sr_add(v.y, corr.y, 0x9e3779b1u + 0x85ebca77u * c));
+      } else {
+        y = v + (a.itp ? (-f) * t : mul_mi(f * t));
+      }
     }
     v = y;
   }

@@ -118,7 +118,8 @@ def run_request(req: SolveRequest) -> dict:
                             sim_params=SimParams(req.dt, req.steps, False, None, req.steps), psi_init=psi,
                             enable_ddi=req.enable_ddi, c_dd=req.c_dd, precision=req.precision, graphs=False)
     res = api.run_simulation(ws, keep_psi=False)
-    out = dict(energy=res.energies[-1], norm=res.norms[-1], converged=None, steps=req.steps)
+    out = dict(energy=res.energies[-1], norm=res.norms[-1], converged=None, steps=req.steps,
+               energy0=res.energies[0])
     ws.close()
     return out
 

@@ -388,15 +388,24 @@ def bench_serving(S, n_requests: int, fp64_probe_steps: int = 20, check_budget_s
         setup, per_step = probes[key]
         cost[r.rid] = setup + per_step * res.steps
         est64 += cost[r.rid]
-    # accuracy of served energies against the plain FP64 form (same request, same steps / tol)
+    # accuracy of served energies against the plain FP64 form (same request, same steps / tol).
+    # Ground states: the 1e-6 energy bar.  Real-time runs: the FP32 - FP64 difference of the final
+    # energy, split by whether the FP64 run itself conserves energy (drift below 1e-4 over the
+    # run); where it does not, dt is too coarse for the grid's fastest kinetic phase and the
+    # discrete dynamics is chaotic, so two roundings of it part ways.
     t0 = time.perf_counter()
-    errs = []
+    errs, dyn_ok, dyn_bad = [], [], []
     for r in sorted(reqs, key=lambda q: cost[q.rid]):
         if time.perf_counter() - t0 + cost[r.rid] > check_budget_s:
             break
-        e64 = serve.run_request(serve.SolveRequest(**{**r.__dict__, "precision": "fp64"}))["energy"]
+        o64 = serve.run_request(serve.SolveRequest(**{**r.__dict__, "precision": "fp64"}))
         e32 = out["results"][r.rid].energy
-        errs.append(abs(e32 - e64) / abs(e64))
+        rel = abs(e32 - o64["energy"]) / abs(o64["energy"])
+        if r.kind == "ground_state":
+            errs.append(rel)
+        else:
+            drift = abs(o64["energy"] - o64["energy0"]) / abs(o64["energy0"])
+            (dyn_ok if drift < 1e-4 else dyn_bad).append(rel)
     lat = sorted(x.latency for x in out["results"])
     return {"workload": f"{n_requests} requests of the seeded Poisson stream (mean 200 req/s): 1-D 256..4096, "
                         "2-D 64^2..512^2, 3-D 32^3..128^3, F in {1,2,6}, DDI for F=6, 500-5000 steps, "
@@ -409,9 +418,16 @@ def bench_serving(S, n_requests: int, fp64_probe_steps: int = 20, check_budget_s
             "fp64_one_at_a_time_solves_per_s": len(reqs) / est64,
             "fp64_estimate": f"per grid/F/kind: setup + {fp64_probe_steps}-step timed probe x steps of the served solve",
             "speedup_vs_fp64_one_at_a_time": est64 / out["wall_s"],
-            "accuracy_vs_fp64": {"checked": len(errs), "of": len(reqs), "max_energy_rel_err": max(errs) if errs else None,
-                                 "above_1e-6": sum(1 for e in errs if e > 1e-6),
-                                 "selection": f"cheapest FP64 reruns first within {check_budget_s:.0f} s"}}
+            "accuracy_vs_fp64": {
+                "selection": f"cheapest FP64 reruns first within {check_budget_s:.0f} s",
+                "ground_states": {"checked": len(errs), "of": sum(1 for r in reqs if r.kind == "ground_state"),
+                                  "max_energy_rel_err": max(errs) if errs else None,
+                                  "above_1e-6": sum(1 for e in errs if e > 1e-6)},
+                "dynamics_energy_conserving": {"checked": len(dyn_ok),
+                                               "max_energy_rel_err": max(dyn_ok) if dyn_ok else None,
+                                               "above_1e-6": sum(1 for e in dyn_ok if e > 1e-6)},
+                "dynamics_fp64_drift_above_1e-4": {"checked": len(dyn_bad),
+                                                   "max_energy_rel_err": max(dyn_bad) if dyn_bad else None}}}
 
 
 def _logged(runner):
