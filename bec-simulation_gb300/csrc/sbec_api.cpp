@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -67,6 +68,11 @@ std::mutex& tune_table_mutex() {
 std::map<std::string, int>& tune_table_map() {
   static std::map<std::string, int> t;
   return t;
+}
+
+std::atomic<bool>& tune_frozen() {
+  static std::atomic<bool> f{false};
+  return f;
 }
 }  // namespace sbec
 
@@ -1045,28 +1051,47 @@ std::unique_ptr<EngineBase> make_batch_group(const sbec_config& cfg, int n, cons
 // The find_ground_state ITP loop (src/ground_state.jl:116-169) for every solve of one group;
 // a solve leaves the active set at the check where it converges.  The NaN guard of steps
 // 1-10 (src/ground_state.jl:4-29) is evaluated once, at step 10.  out: the group's solves.
-void batch_ground_state(EngineBase& e, int64_t n_steps, double tol, int64_t check_every, sbec_gs_result* out) {
+// find_ground_state's loop (src/ground_state.jl:116-169) for every solve of one group: solve s
+// runs up to n_steps[s] steps with its convergence test every check_every[s] steps (the
+// previous psi and energy are those of its own last check).  The active solves advance
+// together in blocks that end at the next step where some solve checks or stops; a solve
+// leaves the batch when it converges or reaches its step limit.
+void batch_ground_state(EngineBase& e, const int64_t* n_steps, double tol, const int64_t* check_every,
+                        sbec_gs_result* out) {
   const int n = e.n_solves();
-  std::vector<int> active(n);
-  for (int i = 0; i < n; ++i) active[i] = i;
+  std::vector<int> active;
+  int64_t max_steps = 0;
+  for (int i = 0; i < n; ++i) {
+    active.push_back(i);
+    max_steps = std::max(max_steps, n_steps[i]);
+  }
   e.batch_set_active(active);
   std::vector<double> E_prev(n), E(n), pmax(n), dmax(n);
   e.batch_energies(E_prev.data());
   e.batch_save_prev();
-  for (int i = 0; i < n; ++i) out[i] = sbec_gs_result{0, NAN, NAN, NAN, n_steps};
+  for (int i = 0; i < n; ++i) out[i] = sbec_gs_result{0, NAN, NAN, NAN, n_steps[i]};
+  const int64_t nan_step = std::min<int64_t>(10, max_steps);
   int64_t step = 0;
-  while (step < n_steps && !active.empty()) {
-    int64_t nxt = std::min(n_steps, (step / check_every + 1) * check_every);
-    if (step < 10) nxt = std::min<int64_t>(nxt, 10);
+  while (!active.empty()) {
+    int64_t nxt = INT64_MAX;
+    for (int s : active) nxt = std::min(nxt, std::min(n_steps[s], (step / check_every[s] + 1) * check_every[s]));
+    if (step < nan_step) nxt = std::min(nxt, nan_step);
     e.batch_itp_steps(nxt - step, e.dt);
     step = nxt;
-    if (step == std::min<int64_t>(10, n_steps) && e.batch_has_nan())
+    if (step == nan_step && e.batch_has_nan())
       fail(SBEC_ERR_NUMERIC, "NaN detected in ITP within the first 10 steps. Likely potential overflow. Reduce dt.");
-    if (step % check_every == 0) {
-      e.batch_energies(E.data());
-      e.batch_max_abs(pmax.data(), dmax.data());
-      std::vector<int> keep;
-      for (int s : active) {
+    bool any_check = false, any_end = false;
+    for (int s : active) {
+      any_check = any_check || step % check_every[s] == 0;
+      any_end = any_end || step == n_steps[s];
+    }
+    if (!any_check && !any_end) continue;
+    e.batch_energies(E.data());
+    if (any_check) e.batch_max_abs(pmax.data(), dmax.data());
+    std::vector<int> keep;
+    for (int s : active) {
+      bool leave = false;
+      if (step % check_every[s] == 0) {
         const double dE = std::fabs(E[s] - E_prev[s]);
         const double dpsi = pmax[s] > 0 ? dmax[s] / pmax[s] : 0.0;
         out[s].dE = dE;
@@ -1074,23 +1099,22 @@ void batch_ground_state(EngineBase& e, int64_t n_steps, double tol, int64_t chec
         if (dE < std::max(tol, 0.5 * e.psi_resolution() * std::fabs(E[s])) &&
             dpsi < std::max(tol, e.psi_resolution())) {
           out[s].converged = 1;
-          out[s].energy = E[s];
-          out[s].steps = step;
+          leave = true;
         } else {
           E_prev[s] = E[s];
-          keep.push_back(s);
+          e.batch_save_prev_solve(s);
         }
       }
+      if (leave || step == n_steps[s]) {
+        out[s].energy = E[s];
+        out[s].steps = step;
+      } else {
+        keep.push_back(s);
+      }
+    }
+    if (keep.size() != active.size()) {
       active = keep;
       e.batch_set_active(active);
-      e.batch_save_prev();
-    }
-  }
-  if (!active.empty()) {
-    e.batch_energies(E.data());
-    for (int s : active) {
-      out[s].energy = E[s];
-      out[s].steps = step;
     }
   }
   e.sync();
@@ -1197,6 +1221,19 @@ sbec_status sbec_batch_create_grids(const sbec_config* cfg, int32_t n_solves, co
   SBEC_API_END
 }
 
+sbec_status sbec_batch_supported(const sbec_config* cfg, int32_t* supported) {
+  SBEC_API_BEGIN
+  need(cfg, "config");
+  need(supported, "supported");
+  *supported = 0;
+  const Setup s = build_setup(*cfg);  // argument errors are errors
+  const bool contact = cfg->n_c_extra == 0 && !cfg->gS_direct && !cfg->enable_ddi && !cfg->raman &&
+                       cfg->loss_gamma_dr < 1e-30 && cfg->loss_L3 < 1e-30 && std::fabs(s.c2) <= 1e-30;
+  *supported = cfg->imaginary_time && cfg->normalize_every == 1 && contact &&
+               fused_path_supported(s, cfg->precision == SBEC_FP32_BULK);
+  SBEC_API_END
+}
+
 sbec_status sbec_batch_destroy(sbec_batch* b) {
   SBEC_API_BEGIN
   delete b;
@@ -1238,6 +1275,11 @@ sbec_status sbec_batch_energies(sbec_batch* b, double* E) {
   SBEC_API_END
 }
 
+namespace {
+void batch_ground_state_all(sbec_batch* b, const int64_t* n_steps, double tol, const int64_t* check_every,
+                            sbec_gs_result* out);
+}  // namespace
+
 // The groups' ITP loops run concurrently, one host thread per group (each group has its own
 // stream, buffers and graphs); results in the caller's solve order.
 sbec_status sbec_batch_ground_state(sbec_batch* b, int64_t n_steps, double tol, int64_t check_every,
@@ -1246,11 +1288,51 @@ sbec_status sbec_batch_ground_state(sbec_batch* b, int64_t n_steps, double tol, 
   need(b, "batch");
   need(out, "out");
   if (n_steps <= 0 || check_every <= 0) fail(SBEC_ERR_INVALID, "n_steps and check_every must be positive");
+  std::vector<int64_t> ns((size_t)b->n(), n_steps), ce((size_t)b->n(), check_every);
+  batch_ground_state_all(b, ns.data(), tol, ce.data(), out);
+  SBEC_API_END
+}
+
+sbec_status sbec_batch_ground_state_each(sbec_batch* b, const int64_t* n_steps, double tol,
+                                         const int64_t* check_every, sbec_gs_result* out) {
+  SBEC_API_BEGIN
+  need(b, "batch");
+  need(n_steps, "n_steps");
+  need(check_every, "check_every");
+  need(out, "out");
+  for (int i = 0; i < b->n(); ++i)
+    if (n_steps[i] <= 0 || check_every[i] <= 0) fail(SBEC_ERR_INVALID, "n_steps and check_every must be positive");
+  batch_ground_state_all(b, n_steps, tol, check_every, out);
+  SBEC_API_END
+}
+
+sbec_status sbec_batch_set_graph_mode(sbec_batch* b, int32_t graphs) {
+  SBEC_API_BEGIN
+  need(b, "batch");
+  for (auto& g : b->groups) g->set_graphs(graphs != 0);
+  SBEC_API_END
+}
+
+namespace {
+
+// Every group of the batch (its solves' entries of the per-solve arrays); groups on their
+// own threads (and streams) when there are several.
+void batch_ground_state_all(sbec_batch* b, const int64_t* n_steps, double tol, const int64_t* check_every,
+                            sbec_gs_result* out) {
   const size_t G = b->groups.size();
   std::vector<std::vector<sbec_gs_result>> res(G);
-  for (size_t g = 0; g < G; ++g) res[g].resize(b->groups[g]->n_solves());
+  std::vector<std::vector<int64_t>> gn(G), gc(G);
+  for (size_t g = 0; g < G; ++g) {
+    res[g].resize(b->groups[g]->n_solves());
+    gn[g].resize(b->groups[g]->n_solves());
+    gc[g].resize(b->groups[g]->n_solves());
+  }
+  for (int i = 0; i < b->n(); ++i) {
+    gn[b->grp[i]][b->loc[i]] = n_steps[i];
+    gc[b->grp[i]][b->loc[i]] = check_every[i];
+  }
   if (G == 1) {
-    batch_ground_state(*b->groups[0], n_steps, tol, check_every, res[0].data());
+    batch_ground_state(*b->groups[0], gn[0].data(), tol, gc[0].data(), res[0].data());
   } else {
     int dev = 0;
     cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
@@ -1260,7 +1342,7 @@ sbec_status sbec_batch_ground_state(sbec_batch* b, int64_t n_steps, double tol, 
       th.emplace_back([&, g] {
         try {
           cuda_check(cudaSetDevice(dev), "cudaSetDevice");
-          batch_ground_state(*b->groups[g], n_steps, tol, check_every, res[g].data());
+          batch_ground_state(*b->groups[g], gn[g].data(), tol, gc[g].data(), res[g].data());
         } catch (const SbecError& e) {
           err[g] = e;
         } catch (const std::exception& e) {
@@ -1272,8 +1354,9 @@ sbec_status sbec_batch_ground_state(sbec_batch* b, int64_t n_steps, double tol, 
       if (e.status != SBEC_OK) throw e;
   }
   for (int i = 0; i < b->n(); ++i) out[i] = res[b->grp[i]][b->loc[i]];
-  SBEC_API_END
 }
+
+}  // namespace
 
 sbec_status sbec_profile_enable(sbec_ws* ws, int32_t enable) {
   SBEC_API_BEGIN
@@ -1351,6 +1434,12 @@ sbec_status sbec_tune_table_export(char* buf, int64_t cap, int64_t* len) {
     for (const auto& kv : tune_table_map()) r += kv.first + "\t" + std::to_string(kv.second) + "\n";
   }
   copy_report(r, buf, cap, len);
+  SBEC_API_END
+}
+
+sbec_status sbec_tune_freeze(int32_t frozen) {
+  SBEC_API_BEGIN
+  tune_frozen().store(frozen != 0);
   SBEC_API_END
 }
 

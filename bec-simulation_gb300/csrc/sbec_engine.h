@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -181,6 +182,7 @@ class EngineBase {
   virtual void batch_energies(double* E) = 0;                  // total_energy per solve (all solves)
   virtual void batch_max_abs(double* pmax, double* dmax) = 0;  // vs the saved previous psi (active solves)
   virtual void batch_save_prev() = 0;
+  virtual void batch_save_prev_solve(int solve) = 0;  // the same for one solve
   virtual bool batch_has_nan() = 0;
   virtual void batch_get_psi(int solve, double* host) = 0;
 
@@ -193,6 +195,13 @@ class EngineBase {
 // precisions and every workspace and batch; guarded by tune_table_mutex().
 std::mutex& tune_table_mutex();
 std::map<std::string, int>& tune_table_map();
+// sbec_tune_freeze: shapes missing from the table take the default variant (untimed)
+std::atomic<bool>& tune_frozen();
+
+// Whether a grid takes the fused row / column passes (the batch and leapfrog fast path):
+// power-of-two axes, no DDI / tensor / Raman / losses, D in {1, 3, 5}, a row-pass variant that
+// fits (threads, shared memory) for the first axis.  Host-only; defined with the FP32 engine.
+bool fused_path_supported(const Setup& s, bool fp32);
 
 std::unique_ptr<EngineBase> make_engine_f64(const Setup& s);
 std::unique_ptr<EngineBase> make_engine_f32(const Setup& s);

@@ -109,7 +109,7 @@ class Engine final : public EngineBase {
     if (const char* t = std::getenv("SBEC_TUNE")) tune_on_ = std::atoi(t) != 0;
     if (const char* f = std::getenv("SBEC_TUNE_FORCE")) tune_force_ = std::atoi(f);
     if (const char* m = std::getenv("SBEC_BATCH_MERGED")) merged_itp_ = std::atoi(m) != 0;
-    if (const char* t = std::getenv("SBEC_TENSOR_LANES")) tensor_lanes_ = std::atoi(t) != 0;
+    if (const char* t = std::getenv("SBEC_TENSOR_LANES")) tensor_mode_ = std::atoi(t);
     if (const char* g = std::getenv("SBEC_SEGMENT")) segment_on_ = std::atoi(g) != 0;
     // host-side fault injection for the tests: the segment barrier's arrival counter starts
     // beyond the block count, so no block is ever the last arriver and every wait runs out
@@ -146,6 +146,9 @@ class Engine final : public EngineBase {
     if (s_.tensor) {
       G_ = alloc<double>(s_.G.size());
       upload(G_, s_.G.data(), s_.G.size());
+      std::vector<float> g32(s_.G.begin(), s_.G.end());
+      G32_ = alloc<float>(g32.size());
+      upload(G32_, g32.data(), g32.size());
       const int np = (int)s_.pair_a.size();
       std::vector<int4> pairs(np);
       for (int q = 0; q < np; ++q) pairs[q] = make_int4(s_.pair_a[q], s_.pair_c1[q], s_.pair_c2[q], 0);
@@ -626,13 +629,7 @@ class Engine final : public EngineBase {
   double psi_resolution() const override { return sizeof(R) == 4 ? std::ldexp(1.0, -21) : 0.0; }
 
   // ---------------- fused paths ----------------
-  bool fused_path() const override {
-    if (!s_.pow2 || s_.ddi || s_.tensor || s_.raman || s_.loss) return false;
-    if (!(s_.D == 1 || s_.D == 3 || s_.D == 5)) return false;
-    const int nx = s_.n[0];
-    if (nx < 16 || nx > 4096) return false;
-    return row_variant_ok(sizeof(R) == 4, nx, s_.D, 0);
-  }
+  bool fused_path() const override { return fused_path_supported(s_, sizeof(R) == 4); }
 
   void lf_open(double dtv) override {
     update_phase(dtv, false);
@@ -1128,6 +1125,12 @@ class Engine final : public EngineBase {
                "prev copy");
   }
 
+  void batch_save_prev_solve(int solve) override {
+    const size_t off = (size_t)solve * nc_;
+    cuda_check(cudaMemcpyAsync(bprev_ + off, bpsi_ + off, sizeof(cplx<R>) * nc_, cudaMemcpyDeviceToDevice, stream_),
+               "prev copy");
+  }
+
   bool batch_has_nan() override {
     const int nb = red_blocks(nc_ * nsolve_);
     pb();
@@ -1349,9 +1352,9 @@ class Engine final : public EngineBase {
       p.n[a] = s_.n[a];
     }
     p.scale0 = (R)(1.0 / (double)N_);  // exact when N_ is a power of two
-    // the unbiased FP32 form needs the exact power-of-two scale; other grids use the
-    // compensated product
-    p.unbiased = (sizeof(R) == 4 && phase_itp_ == 0 && s_.pow2) ? 1 : 0;
+    // FP32 real time: the unbiased rotation (the line kernels of power-of-two grids, where
+    // scale0 is exact; k_kinetic_apply of other grids, which carries the rounding of x scale0)
+    p.unbiased = (sizeof(R) == 4 && phase_itp_ == 0) ? 1 : 0;
     return p;
   }
 
@@ -1426,6 +1429,11 @@ class Engine final : public EngineBase {
     if (it != tune_table().end() && std::find(cands.begin(), cands.end(), it->second) != cands.end()) {
       tune_log_.push_back(key + " -> v" + std::to_string(it->second) + " (from the process table)");
       return tuned_[key] = it->second;
+    }
+    if (tune_frozen().load()) {
+      tune_log_.push_back(key + " -> v" + std::to_string(cands[0]) + " (frozen table: default)");
+      tune_table()[key] = cands[0];
+      return tuned_[key] = cands[0];
     }
     if (capturing()) return 0;  // never reached: shapes are first met in an eager run
     if (extent > tune_buf_n_) {
@@ -1552,8 +1560,10 @@ class Engine final : public EngineBase {
   // w_j = exp(sign i pi (j^2 mod 2n) / n) and the M-point FFT of conj(w) placed at m and M - m.
   struct BlueTab {
     int M = 0;
-    cplx<R>* chirp = nullptr;
+    cplx<R>* chirp = nullptr;  // head values
+    cplx<R>* chirp_lo = nullptr;  // tails (FP32; zero in FP64)
     cplx<R>* bhat = nullptr;
+    cplx<R>* bhat_lo = nullptr;
   };
 
   const BlueTab& blue_tab(int n, int sign) {
@@ -1563,23 +1573,54 @@ class Engine final : public EngineBase {
     int M = 1;
     while (M < 2 * n - 1) M *= 2;
     const long double pi = 3.141592653589793238462643383279502884L;
-    std::vector<cplx<R>> w(n), b((size_t)M, mk<R>(0, 0));
+    using cld = std::complex<long double>;
+    std::vector<cplx<R>> w(n), wl(n), bh((size_t)M), bl((size_t)M);
+    std::vector<cld> b((size_t)M, cld(0, 0));
+    // head (rounded to R) and tail (the remainder, rounded to R; zero in FP64)
+    auto split = [](cld v, cplx<R>& hi, cplx<R>& lo) {
+      hi = mk<R>((R)v.real(), (R)v.imag());
+      lo = sizeof(R) == 4 ? mk<R>((R)(v.real() - (long double)hi.x), (R)(v.imag() - (long double)hi.y)) : mk<R>(0, 0);
+    };
     for (int j = 0; j < n; ++j) {
       const long long jj = ((long long)j * j) % (2LL * n);
       const long double ang = (long double)sign * pi * (long double)jj / (long double)n;
-      w[j] = mk<R>((R)std::cos(ang), (R)std::sin(ang));
-      const cplx<R> cw = mk<R>((R)std::cos(ang), (R)(-std::sin(ang)));
+      split(cld(std::cos(ang), std::sin(ang)), w[j], wl[j]);
+      const cld cw(std::cos(ang), -std::sin(ang));
       b[j] = cw;
       if (j > 0) b[(size_t)M - j] = cw;
     }
+    // The M-point forward transform of the chirp on the host in long double (radix 2, in
+    // place), rounded once to R: the table enters every transform of the axis, so its error
+    // must not be that of an R-precision FFT.
+    for (int i = 1, j = 0; i < M; ++i) {
+      int bit = M >> 1;
+      for (; j & bit; bit >>= 1) j ^= bit;
+      j ^= bit;
+      if (i < j) std::swap(b[(size_t)i], b[(size_t)j]);
+    }
+    for (int len = 2; len <= M; len <<= 1) {
+      const int h = len / 2;
+      for (int k = 0; k < h; ++k) {
+        const long double a = -2.0L * pi * (long double)k / (long double)len;
+        const cld tw(std::cos(a), std::sin(a));
+        for (int s0 = 0; s0 < M; s0 += len) {
+          const cld u = b[(size_t)(s0 + k)], v = b[(size_t)(s0 + k + h)] * tw;
+          b[(size_t)(s0 + k)] = u + v;
+          b[(size_t)(s0 + k + h)] = u - v;
+        }
+      }
+    }
+    for (int k = 0; k < M; ++k) split(b[(size_t)k], bh[(size_t)k], bl[(size_t)k]);
     BlueTab t;
     t.M = M;
     t.chirp = alloc<cplx<R>>(n);
+    t.chirp_lo = alloc<cplx<R>>(n);
     t.bhat = alloc<cplx<R>>(M);
+    t.bhat_lo = alloc<cplx<R>>(M);
     upload(t.chirp, w.data(), w.size());
-    upload(t.bhat, b.data(), b.size());
-    fft_x_n(M, t.bhat, 1, 0);  // forward transform in place
-    sync();
+    upload(t.chirp_lo, wl.data(), wl.size());
+    upload(t.bhat, bh.data(), bh.size());
+    upload(t.bhat_lo, bl.data(), bl.size());
     return blue_[key] = t;
   }
 
@@ -1598,7 +1639,8 @@ class Engine final : public EngineBase {
       blue_scr_n_ = need;
     }
     pb();
-    k_blue_pre<R><<<grid_for((int64_t)need), 256, 0, stream_>>>(buf, blue_scr_, n, M, inner, (int64_t)need, t.chirp);
+    k_blue_pre<R><<<grid_for((int64_t)need), 256, 0, stream_>>>(buf, blue_scr_, n, M, inner, (int64_t)need, t.chirp,
+                                                                  t.chirp_lo);
     done("blue", (double)sizeof(cplx<R>) * ((double)nc_ + (double)need));
     auto line_fft = [&](int mode) {
       if (inner == 1)
@@ -1608,11 +1650,13 @@ class Engine final : public EngineBase {
     };
     line_fft(0);
     pb();
-    k_blue_mid<R><<<grid_for((int64_t)need), 256, 0, stream_>>>(blue_scr_, M, inner, (int64_t)need, t.bhat);
+    k_blue_mid<R><<<grid_for((int64_t)need), 256, 0, stream_>>>(blue_scr_, M, inner, (int64_t)need, t.bhat,
+                                                                  t.bhat_lo);
     done("blue", 2.0 * (double)sizeof(cplx<R>) * (double)need);
     line_fft(1);
     pb();
-    k_blue_post<R><<<grid_for(nc_), 256, 0, stream_>>>(blue_scr_, buf, n, M, inner, nc_, t.chirp, (R)(1.0 / M));
+    k_blue_post<R><<<grid_for(nc_), 256, 0, stream_>>>(blue_scr_, buf, n, M, inner, nc_, t.chirp, t.chirp_lo,
+                                                         (R)(1.0 / M));
     done("blue", (double)sizeof(cplx<R>) * 2.0 * (double)nc_);
   }
 
@@ -1958,6 +2002,7 @@ class Engine final : public EngineBase {
     a.N = N_;
     a.V = V_;
     a.G = G_;
+    a.G32 = G32_;
     a.bound_coef = s_.bound_coef;
     a.itp = it ? 1 : 0;
     a.tau = (R)tau_t;
@@ -1980,7 +2025,18 @@ class Engine final : public EngineBase {
   template <int D>
   void launch_tensor_d(const TensorArgs<R>& a) {
     if constexpr (sizeof(R) == 4) {
-      if (tensor_lanes_) {
+      // default: rows of h in registers up to D = 9 (F <= 4), lane groups above (a 128^3 grid
+      // on GB300: D = 5 0.69 against 1.39 ms, D = 9 3.00 against 3.23 ms, D = 13 9.0 against
+      // 2.9 ms, where the rows kernel's 255 registers leave 7 warps per SM)
+      const int mode = tensor_mode_ >= 0 ? tensor_mode_ : (D <= 9 ? 2 : 1);
+      if (mode == 2) {
+        constexpr int NW = (D + 1) / 2;
+        pb();
+        k_tensor_rows<D, NW><<<(unsigned)((N_ + 31) / 32), 32 * NW, 0, stream_>>>(a);
+        done("tensor", (2.0 * (double)sizeof(cplx<R>) * D + (double)sizeof(R)) * (double)N_);
+        return;
+      }
+      if (mode == 1) {
         using TL = TensorLanes<D>;
         const size_t smem = TL::smem_bytes();
         auto kern = k_tensor_lanes<D>;
@@ -2130,7 +2186,10 @@ class Engine final : public EngineBase {
   // line-kernel variants in use (see sbec_lines.h); chosen by the autotuner
   int v_row_ = 0, v_str_ = 0, v_x_ = 0;
   bool merged_itp_ = false;  // SBEC_BATCH_MERGED=1: two-pass FP32 batched ITP step (predicted scale)
-  bool tensor_lanes_ = true;  // FP32 tensor step with one lane group per point (SBEC_TENSOR_LANES=0: one thread)
+  // FP32 tensor kernel (SBEC_TENSOR_LANES): 0 one thread per point, 1 a lane group per point,
+  // 2 rows of h in registers ((D + 1) / 2 warps per 32 points); -1 (default) by D
+  int tensor_mode_ = -1;
+  float* G32_ = nullptr;
   R* bcorr_ = nullptr;  // merged FP32 batched ITP: per-solve correction, prediction, ones
   R* bpred_ = nullptr;
   R* bones_ = nullptr;

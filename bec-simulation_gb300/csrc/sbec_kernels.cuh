@@ -77,24 +77,41 @@ struct PhaseRef {
 // exact powers of two) are combined as (1 + C + iS) = prod_a (1 + c_a + i s_a) in the
 // small quantities c_a, s_a (full relative precision for low k), and x is turned once:
 // x/N + (x/N)(C + iS) with the addition rounded without bias (sr_add).
+// (1 + C + iS) <- (1 + C + iS)(1 + c + is) for the table entry scale (1 + c + is).
+__device__ __forceinline__ void kin_fold(float& C, float& Sn, const Tw<float>& t, int idx, float scale, float inv) {
+  const float4 w4 = __ldg(reinterpret_cast<const float4*>(t.hi) + idx);
+  const float c = __fmul_rn(__fadd_rn(__fsub_rn(w4.x, scale), w4.z), inv);
+  const float sn = __fmul_rn(__fadd_rn(w4.y, w4.w), inv);
+  const float nC = __fadd_rn(__fadd_rn(C, c), __fmaf_rn(C, c, __fmul_rn(-Sn, sn)));
+  const float nS = __fadd_rn(__fadd_rn(Sn, sn), __fmaf_rn(Sn, c, __fmul_rn(C, sn)));
+  C = nC;
+  Sn = nS;
+}
+
 __device__ __forceinline__ float2 kinetic_rot(float2 x, const PhaseRef<float>& ph, int i0, int i1, int ilast) {
   float C = 0.0f, Sn = 0.0f;
-  auto fold = [&](const Tw<float>& t, int idx, float scale, float inv) {
-    const float4 w4 = __ldg(reinterpret_cast<const float4*>(t.hi) + idx);
-    const float c = __fmul_rn(__fadd_rn(__fsub_rn(w4.x, scale), w4.z), inv);
-    const float sn = __fmul_rn(__fadd_rn(w4.y, w4.w), inv);
-    const float nC = __fadd_rn(__fadd_rn(C, c), __fmaf_rn(C, c, __fmul_rn(-Sn, sn)));
-    const float nS = __fadd_rn(__fadd_rn(Sn, sn), __fmaf_rn(Sn, c, __fmul_rn(C, sn)));
-    C = nC;
-    Sn = nS;
-  };
   const float inv0 = 1.0f / ph.scale0;  // N: exact
-  fold(ph.tab[0], i0, ph.scale0, inv0);
-  if (ph.ndim == 3) fold(ph.tab[1], i1, 1.0f, 1.0f);
-  fold(ph.tab[ph.ndim - 1], ilast, 1.0f, 1.0f);
+  kin_fold(C, Sn, ph.tab[0], i0, ph.scale0, inv0);
+  if (ph.ndim == 3) kin_fold(C, Sn, ph.tab[1], i1, 1.0f, 1.0f);
+  kin_fold(C, Sn, ph.tab[ph.ndim - 1], ilast, 1.0f, 1.0f);
   const float2 xs = mk<float>(__fmul_rn(x.x, ph.scale0), __fmul_rn(x.y, ph.scale0));
   const float bx = __fmaf_rn(xs.x, C, __fmul_rn(-xs.y, Sn));
   const float by = __fmaf_rn(xs.y, C, __fmul_rn(xs.x, Sn));
+  return mk<float>(sr_add(xs.x, bx, 0x85ebca6bu), sr_add(xs.y, by, 0xc2b2ae35u));
+}
+
+// The same rotation for any number of axes and a scale 1/N that need not be a power of
+// two: the rounding error of x * scale0 (exact, from an fma) joins the small term, so the
+// one rounded addition left is the unbiased one.
+__device__ __forceinline__ float2 kinetic_rot_any(float2 x, const PhaseRef<float>& ph, int i0, int i1, int i2) {
+  float C = 0.0f, Sn = 0.0f;
+  kin_fold(C, Sn, ph.tab[0], i0, ph.scale0, __frcp_rn(ph.scale0));
+  if (ph.ndim >= 2) kin_fold(C, Sn, ph.tab[1], i1, 1.0f, 1.0f);
+  if (ph.ndim == 3) kin_fold(C, Sn, ph.tab[2], i2, 1.0f, 1.0f);
+  const float2 xs = mk<float>(__fmul_rn(x.x, ph.scale0), __fmul_rn(x.y, ph.scale0));
+  const float ex = __fmaf_rn(x.x, ph.scale0, -xs.x), ey = __fmaf_rn(x.y, ph.scale0, -xs.y);
+  const float bx = __fadd_rn(__fmaf_rn(xs.x, C, __fmul_rn(-xs.y, Sn)), ex);
+  const float by = __fadd_rn(__fmaf_rn(xs.y, C, __fmul_rn(xs.x, Sn)), ey);
   return mk<float>(sr_add(xs.x, bx, 0x85ebca6bu), sr_add(xs.y, by, 0xc2b2ae35u));
 }
 
@@ -109,45 +126,61 @@ __device__ __forceinline__ float2 kinetic_rot(float2 x, const PhaseRef<float>& p
 // grid and the scratch are read and written with inner fastest (coalesced), and the M-point
 // transforms run as strided lines of the same geometry (contiguous lines when inner = 1).
 // ---------------------------------------------------------------------------
+// The chirp and its spectrum are (head, tail) pairs in FP32 (cmul_comp: the factor to about
+// 2^-48): a table that enters every transform with the same rounding would otherwise change
+// the norm by the same amount at every step.
 template <typename R>
 __global__ void k_blue_pre(const cplx<R>* __restrict__ src, cplx<R>* __restrict__ scr, int n, int M, int64_t inner,
-                           int64_t total, const cplx<R>* __restrict__ chirp) {
+                           int64_t total, const cplx<R>* __restrict__ chirp, const cplx<R>* __restrict__ chirp_lo) {
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i_in = q % inner, r = q / inner;
     const int j = (int)(r % M);
     const int64_t i_out = r / M;
-    scr[q] = j < n ? src[i_in + (int64_t)j * inner + i_out * inner * n] * __ldg(chirp + j) : mk<R>(0, 0);
+    scr[q] = j < n ? cmul_comp(src[i_in + (int64_t)j * inner + i_out * inner * n], __ldg(chirp + j),
+                               __ldg(chirp_lo + j))
+                   : mk<R>(0, 0);
   }
 }
 
 template <typename R>
 __global__ void k_blue_mid(cplx<R>* __restrict__ scr, int M, int64_t inner, int64_t total,
-                           const cplx<R>* __restrict__ bhat) {
-  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x)
-    scr[q] = scr[q] * __ldg(bhat + (q / inner) % M);
+                           const cplx<R>* __restrict__ bhat, const cplx<R>* __restrict__ bhat_lo) {
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t m = (q / inner) % M;
+    scr[q] = cmul_comp(scr[q], __ldg(bhat + m), __ldg(bhat_lo + m));
+  }
 }
 
 template <typename R>
 __global__ void k_blue_post(const cplx<R>* __restrict__ scr, cplx<R>* __restrict__ dst, int n, int M, int64_t inner,
-                            int64_t total, const cplx<R>* __restrict__ chirp, R inv_m) {
+                            int64_t total, const cplx<R>* __restrict__ chirp, const cplx<R>* __restrict__ chirp_lo,
+                            R inv_m) {
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i_in = q % inner, r = q / inner;
     const int k = (int)(r % n);
     const int64_t i_out = r / n;
-    const cplx<R> v = scr[(i_out * M + k) * inner + i_in] * __ldg(chirp + k);
-    dst[i_in + (int64_t)k * inner + i_out * inner * n] = inv_m * v;
+    const cplx<R> v = cmul_comp(scr[(i_out * M + k) * inner + i_in], __ldg(chirp + k), __ldg(chirp_lo + k));
+    dst[i_in + (int64_t)k * inner + i_out * inner * n] = inv_m * v;  // 1/M: a power of two
   }
 }
 
 // The kinetic phase of a grid with a non-power-of-two axis, applied between the forward and
 // inverse transforms of all axes: the product of the per-axis table entries (1/N folded
-// into the x table), one compensated product per axis in FP32.
+// into the x table), one compensated product per axis in FP32; in FP32 real time the
+// unbiased single rotation of kinetic_rot_any.
 template <typename R>
 __global__ void k_kinetic_apply(cplx<R>* __restrict__ buf, int64_t N, int64_t total, PhaseRef<R> ph) {
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
     const int64_t p = q % N;
     const int i0 = (int)(p % ph.n[0]);
     const int64_t r = p / ph.n[0];
+    if constexpr (sizeof(R) == 4) {
+      if (ph.unbiased) {
+        buf[q] = kinetic_rot_any(buf[q], ph, i0, ph.ndim >= 2 ? (int)(r % ph.n[1]) : 0,
+                                 ph.ndim == 3 ? (int)(r / ph.n[1]) : 0);
+        continue;
+      }
+    }
     cplx<R> v = phase_mul<R>(buf[q], ph.tab[0], i0, ph.scale0, 0);
     if (ph.ndim >= 2) v = phase_mul<R>(v, ph.tab[1], (int)(r % ph.n[1]), (R)1, 0);
     if (ph.ndim == 3) v = phase_mul<R>(v, ph.tab[2], (int)(r / ph.n[1]), (R)1, 0);
@@ -1396,6 +1429,7 @@ struct TensorArgs {
   int64_t N;
   const R* V;
   const double* G;            // (4F+1) * D * D
+  const float* G32;           // the same coefficients in FP32 (FP32 form; null in FP64)
   double bound_coef;          // sum_S |g_S| (2S+1)/(2F+1)
   int n_apply;                // 1 or 2 tensor applications
   int pre_diag, post_diag;
@@ -1623,6 +1657,137 @@ __device__ __forceinline__ void tensor_lane(float2& v, const TensorArgs<float>& 
     v = y;
   }
   __syncwarp(mask);
+}
+
+// ---------------------------------------------------------------------------
+// FP32 tensor step with rows of h in registers (k_tensor_rows): a block of NW warps serves
+// 32 points, one point per lane (launched with NW = (D + 1) / 2: two rows per warp); warp q
+// builds and keeps rows i = q, q + NW, ... of its points' h in registers, and every warp holds
+// the whole spinor, so all register indices are compile-time (the warp's rows are template
+// arguments, chosen by a warp-uniform dispatch) and the G coefficients are read at
+// warp-uniform addresses (broadcast).  A Horner step multiplies the warp's rows by the vector
+// and exchanges the new entries through shared memory (double-buffered, one block barrier per
+// step).  h_ij for i > j is formed from the same coefficient G[J][j][i] and the same rounded
+// products as h_ji, so h is exactly Hermitian.  Sub-step count and series length are the
+// block's maxima (uniform trip counts around the barriers; extra terms only shorten the
+// truncation).
+// ---------------------------------------------------------------------------
+template <int D, int NW, int Q>
+__device__ __forceinline__ void tensor_rows_apply(float2 (&v)[D], const TensorArgs<float>& a, float2* ys, int lane,
+                                                  bool act, int nsub, int K, float dtau) {
+  constexpr int R = (D - Q + NW - 1) / NW;  // rows Q, Q + NW, ... < D
+  float2 h[R > 0 ? R : 1][D];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int i = Q + NW * r;
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      const int lo = i < j ? i : j, hi = i < j ? j : i;
+      float ax = 0.0f, ay = 0.0f;
+#pragma unroll
+      for (int J = hi; J <= lo + D - 1; ++J) {
+        const float g = __ldg(a.G32 + ((size_t)J * D + lo) * D + hi);
+        const float2 u = v[J - i], w = v[J - j];
+        // conj(u) w with separately rounded products: the (j, i) entry uses the same
+        // products, so it is the exact conjugate
+        const float pr = __fadd_rn(__fmul_rn(u.x, w.x), __fmul_rn(u.y, w.y));
+        const float pi = __fsub_rn(__fmul_rn(u.x, w.y), __fmul_rn(u.y, w.x));
+        ax = fmaf(g, pr, ax);
+        ay = fmaf(g, pi, ay);
+      }
+      h[r][j] = make_float2(ax, ay);
+    }
+  }
+  for (int sub = 0; sub < nsub; ++sub) {
+    float2 y[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) y[c] = v[c];
+    for (int k = K; k >= 1; --k) {
+      float2* yb = ys + (k & 1) * D * 32;
+      const float f = dtau / (float)k;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int i = Q + NW * r;
+        float2 t = make_float2(0.0f, 0.0f);
+#pragma unroll
+        for (int j = 0; j < D; ++j) t += h[r][j] * y[j];
+        float2 yn;
+        if (a.itp) {
+          yn = v[i] + (-f) * t;
+        } else if (k == 1) {
+          const float2 corr = mul_mi(f * t);  // unbiased last addition, as in rotate_taylor
+          yn = make_float2(sr_add(v[i].x, corr.x, 0x27d4eb2fu + 0x165667b1u * i),
+                           sr_add(v[i].y, corr.y, 0x9e3779b1u + 0x85ebca77u * i));
+        } else {
+          yn = v[i] + mul_mi(f * t);
+        }
+        yb[i * 32 + lane] = yn;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int c = 0; c < D; ++c) y[c] = yb[c * 32 + lane];
+    }
+#pragma unroll
+    for (int c = 0; c < D; ++c)
+      if (act) v[c] = y[c];
+    __syncthreads();  // every warp has read this sub-step's last exchange before the next one writes
+  }
+}
+
+// Runs warp q's instance (a warp-uniform branch: one template instance per warp).
+template <int D, int NW, int Q>
+__device__ __forceinline__ void tensor_rows_dispatch(int q, float2 (&v)[D], const TensorArgs<float>& a, float2* ys,
+                                                     int lane, bool act, int nsub, int K, float dtau) {
+  if constexpr (Q < NW) {
+    if (q == Q) {
+      tensor_rows_apply<D, NW, Q>(v, a, ys, lane, act, nsub, K, dtau);
+      return;
+    }
+    tensor_rows_dispatch<D, NW, Q + 1>(q, v, a, ys, lane, act, nsub, K, dtau);
+  }
+}
+
+template <int D, int NW>
+__global__ void __launch_bounds__(32 * NW) k_tensor_rows(TensorArgs<float> a) {
+  __shared__ float2 ys[2 * D * 32];
+  const int lane = threadIdx.x & 31, q = threadIdx.x >> 5;
+  const int64_t p = (int64_t)blockIdx.x * 32 + lane;
+  const bool inb = p < a.N;
+  float2 v[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) v[c] = inb ? a.psi[c * a.N + p] : make_float2(0.0f, 0.0f);
+  const float Vp = inb ? a.V[p] : 0.0f;
+  if (a.pre_diag) diag_point_t<float, D>(v, Vp, a);
+  for (int rep = 0; rep < a.n_apply; ++rep) {
+    float nl = 0.0f;
+#pragma unroll
+    for (int c = 0; c < D; ++c) nl += abs2(v[c]);
+    const bool act = inb && nl >= 1e-20f;
+    // sub-steps and series length: the block's maxima (every warp holds the same 32 points)
+    double x = act ? a.bound_coef * (double)nl * fabs((double)a.tau) : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
+    int nsub = 1;
+    if (x > 0.5) nsub = x < 0.5 * kMaxSub ? (int)ceil(x / 0.5) : kMaxSub;  // bounded for non-finite states
+    const double xs = x / nsub;
+    int K = 0;
+    {
+      double term = 1.0;
+      while (K < 40) {
+        term *= xs / (double)(K + 1);
+        if (term < a.eps) break;
+        ++K;
+      }
+      K = K + 1;
+    }
+    const float dtau = a.tau / (float)nsub;
+    tensor_rows_dispatch<D, NW, 0>(q, v, a, ys, lane, act, nsub, K, dtau);
+  }
+  if (a.post_diag) diag_point_t<float, D>(v, Vp, a);
+  if (!inb) return;
+#pragma unroll
+  for (int c = 0; c < D; ++c)
+    if (c % NW == q) a.psi[c * a.N + p] = v[c];
 }
 
 template <int D>

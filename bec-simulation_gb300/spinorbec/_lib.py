@@ -176,12 +176,17 @@ _PROTOS = {
     "sbec_tuning_report": (C.c_int, [_P, C.c_char_p, C.c_int64, C.POINTER(C.c_int64)]),
     "sbec_batch_tuning_report": (C.c_int, [_P, C.c_char_p, C.c_int64, C.POINTER(C.c_int64)]),
     "sbec_tune_table_export": (C.c_int, [C.c_char_p, C.c_int64, C.POINTER(C.c_int64)]),
+    "sbec_tune_freeze": (C.c_int, [C.c_int32]),
     "sbec_tune_table_import": (C.c_int, [C.c_char_p]),
     "sbec_batch_create": (C.c_int, [C.POINTER(sbec_config), C.c_int32, _D, _D, _D, _D, C.POINTER(_P)]),
     "sbec_batch_create_grids": (C.c_int, [C.POINTER(sbec_config), C.c_int32, C.POINTER(C.c_int32), _D, _D, _D,
                                           C.POINTER(_D), C.POINTER(_D), C.POINTER(_P)]),
     "sbec_batch_destroy": (C.c_int, [_P]),
     "sbec_batch_ground_state": (C.c_int, [_P, C.c_int64, C.c_double, C.c_int64, C.POINTER(sbec_gs_result)]),
+    "sbec_batch_ground_state_each": (C.c_int, [_P, C.POINTER(C.c_int64), C.c_double, C.POINTER(C.c_int64),
+                                               C.POINTER(sbec_gs_result)]),
+    "sbec_batch_set_graph_mode": (C.c_int, [_P, C.c_int32]),
+    "sbec_batch_supported": (C.c_int, [C.POINTER(sbec_config), C.POINTER(C.c_int32)]),
     "sbec_batch_get_psi": (C.c_int, [_P, C.c_int32, _D]),
     "sbec_batch_energies": (C.c_int, [_P, _D]),
     "sbec_measure_fma_peak": (C.c_int, [C.c_int32, _D]),

@@ -783,11 +783,26 @@ class GroundStateBatch:
         except Exception:
             pass
 
-    def ground_state(self, n_steps: int, tol: float, check_every: Optional[int] = None) -> list:
+    def ground_state(self, n_steps, tol: float, check_every=None) -> list:
+        """find_ground_state's loop for every solve.  n_steps (and check_every) is one value for
+        all solves or one per solve; check_every defaults to find_ground_state's max(1, n // 10)."""
         out = (_lib.sbec_gs_result * self.n)()
-        ce = max(1, n_steps // 10) if check_every is None else check_every
-        check(self._lib.sbec_batch_ground_state(self._h, int(n_steps), float(tol), int(ce), out))
+        if np.ndim(n_steps) == 0 and np.ndim(check_every) == 0:
+            ce = max(1, int(n_steps) // 10) if check_every is None else check_every
+            check(self._lib.sbec_batch_ground_state(self._h, int(n_steps), float(tol), int(ce), out))
+        else:
+            ns = np.broadcast_to(np.asarray(n_steps, dtype=np.int64), (self.n,)).copy()
+            if check_every is None:
+                ce = np.maximum(1, ns // 10)
+            else:
+                ce = np.broadcast_to(np.asarray(check_every, dtype=np.int64), (self.n,)).copy()
+            check(self._lib.sbec_batch_ground_state_each(self._h, ns.ctypes.data_as(C.POINTER(C.c_int64)),
+                                                         float(tol), ce.ctypes.data_as(C.POINTER(C.c_int64)), out))
         return [dict(converged=bool(r.converged), energy=r.energy, dE=r.dE, dpsi=r.dpsi, steps=r.steps) for r in out]
+
+    def set_graph_mode(self, graphs: bool) -> None:
+        """As Workspace.set_graph_mode, for every group of the batch."""
+        check(self._lib.sbec_batch_set_graph_mode(self._h, 1 if graphs else 0))
 
     def psi(self, i: int) -> np.ndarray:
         g = self.grids[int(i)]
@@ -812,6 +827,17 @@ class GroundStateBatch:
         return _report(self._lib.sbec_batch_tuning_report, self._h)
 
 
+def batch_supported(grid: Grid, F: int, precision: str = "fp32", c_lhy: float = 0.0) -> bool:
+    """Whether solves of spin F with contact couplings on `grid` can run as a GroundStateBatch
+    (sbec_batch_supported: power-of-two axes, D in {1, 3, 5}, a row pass that fits the first
+    axis).  Needs no device."""
+    cfg = _config(grid, F, ZeemanParams(), SimParams(0.005, 1, True, 1, 1), precision,
+                  InteractionParams(0.0, 0.0, c_lhy))
+    ok = C.c_int32()
+    check(load().sbec_batch_supported(C.byref(cfg), C.byref(ok)))
+    return bool(ok.value)
+
+
 def tune_table_export() -> str:
     """The autotuner's process-wide decisions (shape<TAB>variant lines), for saving."""
     lib = load()
@@ -826,6 +852,13 @@ def tune_table_import(text: str) -> None:
     """Load saved autotuner decisions: shapes found there are not timed again, so FP32 results
     are the same in every process that loads the same table."""
     check(load().sbec_tune_table_import(text.encode()))
+
+
+def tune_freeze(frozen: bool = True) -> None:
+    """frozen=True: call shapes missing from the autotuner's table take their default variant
+    instead of being timed, so no later result depends on a timing race; False: time new
+    shapes again (default)."""
+    check(load().sbec_tune_freeze(1 if frozen else 0))
 
 
 def _report(fn, handle) -> str:

@@ -16,6 +16,13 @@ Request workspaces launch their kernels eagerly (graphs off): each lives for one
 solve, and capturing and instantiating CUDA graphs in two dozen concurrent workspaces
 cost more than the replays saved (24-request stream: 8.9 solves/s eager against
 4.9-6.6 with graphs).
+
+Ground-state requests that can share kernels (merge_key: contact couplings, no DDI, same
+grid, F, dt, tol, trap and precision) are merged when the server is given a merge window:
+the requests of one key that arrive in the same window [k w, (k + 1) w) run as one
+GroundStateBatch (per-solve c0, c1 and step limit, each solve with find_ground_state's loop
+and convergence test), dispatched at the window's end.  The grouping depends only on the
+arrival times, so which requests share a batch is the same in every run.
 """
 
 from __future__ import annotations
@@ -124,17 +131,89 @@ def run_request(req: SolveRequest) -> dict:
     return out
 
 
-def pretune(requests: list) -> int:
-    """Fix the autotuner's decisions for every call shape of `requests` before any is served:
-    one two-step run per distinct (grid, F, DDI, kind, precision).  Served results then do not
-    depend on which request met a shape first; returns the number of shapes run."""
+def merge_key(req: SolveRequest) -> Optional[tuple]:
+    """The key of the requests that may run as one GroundStateBatch, or None: ground states
+    with contact couplings (F <= 2, no DDI) on a grid the batch takes (api.batch_supported),
+    with the same grid, dt, tol, trap and precision (the batch's shared terms; c0, c1 and the
+    step limit are per solve)."""
+    if req.kind != "ground_state" or req.enable_ddi or req.F > 2:
+        return None
+    if not api.batch_supported(make_grid(GridConfig(req.n_points, req.box_size)), req.F, req.precision):
+        return None
+    return (tuple(req.n_points), tuple(req.box_size), req.F, req.dt, req.tol, req.omega, req.precision)
+
+
+def run_batch(reqs: list) -> list:
+    """Run requests of one merge_key as one GroundStateBatch from the polar state (as
+    run_request); returns one result dict per request, in order."""
+    r0 = reqs[0]
+    grid = make_grid(GridConfig(r0.n_points, r0.box_size))
+    psi0 = init_psi(grid, r0.F, "polar")
+    b = api.GroundStateBatch(grid=grid, atom=AtomSpecies("req", r0.F), c0s=[r.c0 for r in reqs],
+                             c1s=[r.c1 for r in reqs], psi_inits=[psi0] * len(reqs),
+                             potential=HarmonicTrap(*([r0.omega] * len(r0.n_points))), dt=r0.dt,
+                             precision=r0.precision)
+    try:
+        b.set_graph_mode(False)
+        res = b.ground_state([r.steps for r in reqs], r0.tol)
+        dV = float(np.prod([L / n for L, n in zip(r0.box_size, r0.n_points)]))
+        outs = []
+        for i, r in enumerate(res):
+            norm = float(np.sum(np.abs(b.psi(i)) ** 2) * dV)
+            outs.append(dict(energy=r["energy"], norm=norm, converged=r["converged"], steps=r["steps"]))
+        return outs
+    finally:
+        b.close()
+
+
+def dispatch_units(requests: list, merge_window_s: float = 0.0, max_merge: int = 32,
+                   budget_bytes: float = float("inf")) -> list:
+    """Split `requests` into dispatch units [(time, [requests])], sorted by time.  Without a
+    window every request is its own unit at its arrival; with one, the requests of a
+    merge_key that arrive in the same window form units of up to max_merge requests (and at
+    most budget_bytes of summed footprint), dispatched at the window's end."""
+    order = sorted(requests, key=lambda r: r.arrival)
+    units = []
+    groups: dict = {}
+    for r in order:
+        k = merge_key(r) if merge_window_s > 0 else None
+        if k is None:
+            units.append((r.arrival, [r]))
+        else:
+            groups.setdefault((k, int(r.arrival // merge_window_s)), []).append(r)
+    for (_, w), rs in groups.items():
+        t = (w + 1) * merge_window_s
+        cur, fp = [], 0
+        for r in rs:
+            f = footprint_bytes(r)
+            if cur and (len(cur) >= max_merge or fp + f > budget_bytes):
+                units.append((t, cur))
+                cur, fp = [], 0
+            cur.append(r)
+            fp += f
+        units.append((t, cur))
+    units.sort(key=lambda u: (u[0], u[1][0].rid))
+    return units
+
+
+def pretune(requests: list, merge_window_s: float = 0.0, max_merge: int = 32) -> int:
+    """Fix the autotuner's decisions before any request is served: one two-step run per
+    distinct (grid, F, DDI, kind, precision) and per merged batch size, then the table is
+    frozen (api.tune_freeze), so shapes met later (a batch whose solves have left) take
+    their default variant untimed.  Served results then do not depend on which request met a
+    shape first; returns the number of shapes run."""
     seen = set()
-    for r in requests:
-        key = (tuple(r.n_points), r.F, r.enable_ddi, r.kind, r.precision)
+    for _, rs in dispatch_units(requests, merge_window_s, max_merge):
+        r = rs[0]
+        key = (tuple(r.n_points), r.F, r.enable_ddi, r.kind, r.precision, len(rs) if len(rs) > 1 else 0)
         if key in seen:
             continue
         seen.add(key)
-        run_request(SolveRequest(**{**r.__dict__, "steps": 2, "tol": 0.0}))
+        if len(rs) > 1:
+            run_batch([SolveRequest(**{**q.__dict__, "steps": 2, "tol": 0.0}) for q in rs])
+        else:
+            run_request(SolveRequest(**{**r.__dict__, "steps": 2, "tol": 0.0}))
+    api.tune_freeze(True)
     return len(seen)
 
 
@@ -142,10 +221,17 @@ class Server:
     """Admission by HBM budget and slots; concurrent resident workspaces."""
 
     def __init__(self, hbm_budget_bytes: float = 150e9, max_slots: int = 32,
-                 runner: Callable[[SolveRequest], dict] = run_request):
+                 runner: Callable[[SolveRequest], dict] = run_request,
+                 batch_runner: Callable[[list], list] = run_batch, merge_window_s: float = 0.0,
+                 max_merge: int = 32):
         self.budget = float(hbm_budget_bytes)
         self.max_slots = int(max_slots)
         self.runner = runner
+        self.batch_runner = batch_runner
+        self.merge_window_s = float(merge_window_s)
+        self.max_merge = int(max_merge)
+        self.merged_units = 0
+        self.merged_requests = 0
         self._used = 0.0
         self._active = 0
         self.peak_used = 0.0
@@ -176,30 +262,36 @@ class Server:
         results: list = []
         lock = threading.Lock()
 
-        def serve(req: SolveRequest):
-            fp = footprint_bytes(req)
+        def serve(reqs: list):
+            fps = [footprint_bytes(r) for r in reqs]
+            fp = sum(fps)
             if fp > self.budget:
-                raise MemoryError(f"request {req.rid} needs {fp / 1e9:.1f} GB > budget")
+                raise MemoryError(f"request {reqs[0].rid} needs {fp / 1e9:.1f} GB > budget")
             self._admit(fp)
             admitted = time.perf_counter() - t0
             try:
-                out = self.runner(req)
+                outs = [self.runner(reqs[0])] if len(reqs) == 1 else self.batch_runner(reqs)
             finally:
                 self._release(fp)
             fin = time.perf_counter() - t0
             with lock:
-                results.append(SolveResult(req.rid, req.kind, out["energy"], out["norm"], out["converged"],
-                                           out["steps"], req.arrival, admitted, fin, fp))
+                for req, out, f in zip(reqs, outs, fps):
+                    results.append(SolveResult(req.rid, req.kind, out["energy"], out["norm"], out["converged"],
+                                               out["steps"], req.arrival, admitted, fin, f))
 
-        order = sorted(requests, key=lambda r: r.arrival)
+        units = dispatch_units(requests, self.merge_window_s, self.max_merge, self.budget)
+        for _, rs in units:
+            if len(rs) > 1:
+                self.merged_units += 1
+                self.merged_requests += len(rs)
         with ThreadPoolExecutor(max_workers=self.max_slots + 4) as ex:
             futs = []
-            for req in order:
+            for t_disp, rs in units:
                 if realtime:
-                    wait = req.arrival - (time.perf_counter() - t0)
+                    wait = t_disp - (time.perf_counter() - t0)
                     if wait > 0:
                         time.sleep(wait)
-                futs.append(ex.submit(serve, req))
+                futs.append(ex.submit(serve, rs))
             for f in futs:
                 f.result()
         wall = time.perf_counter() - t0

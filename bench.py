@@ -373,11 +373,17 @@ def bench_serving(S, n_requests: int, fp64_probe_steps: int = 20, check_budget_s
     from spinorbec import serve
 
     reqs = serve.poisson_requests(n_requests, rate=200.0, seed=5)
-    n_shapes = serve.pretune(reqs)
+    window = 0.25
+    n_shapes = serve.pretune(reqs, merge_window_s=window)
     log(f"serving: autotuner fixed for {n_shapes} shapes")
-    srv = serve.Server(hbm_budget_bytes=150e9, max_slots=32, runner=_logged(serve.run_request))
-    out = srv.run(reqs, realtime=True)
-    log(f"serving: {len(reqs)} requests in {out['wall_s']:.1f} s")
+    srv = serve.Server(hbm_budget_bytes=150e9, max_slots=32, runner=_logged(serve.run_request),
+                       merge_window_s=window)
+    try:
+        out = srv.run(reqs, realtime=True)
+    finally:
+        S.tune_freeze(False)
+    log(f"serving: {len(reqs)} requests in {out['wall_s']:.1f} s ({srv.merged_requests} in {srv.merged_units} "
+        "merged batches)")
     est64 = 0.0
     probes = {}
     cost = {}
@@ -411,6 +417,10 @@ def bench_serving(S, n_requests: int, fp64_probe_steps: int = 20, check_budget_s
                         "2-D 64^2..512^2, 3-D 32^3..128^3, F in {1,2,6}, DDI for F=6, 500-5000 steps, "
                         "half ground states (tol 1e-8) half real-time runs",
             "hbm_budget_gb": 150, "max_slots": 32, "peak_concurrent": srv.peak_active,
+            "merging": {"window_s": window, "merged_units": srv.merged_units,
+                        "merged_requests": srv.merged_requests,
+                        "rule": "ground states of one grid/F/dt/tol/trap (contact couplings) arriving in the same "
+                                "window run as one GroundStateBatch, per-solve step limits"},
             "peak_admitted_gb": srv.peak_used / 1e9, "tuned_shapes_before_serving": n_shapes,
             "fp32_served_solves_per_s": out["solves_per_s"], "wall_s": out["wall_s"],
             "p50_latency_s": out["p50_latency_s"], "p99_latency_s": out["p99_latency_s"],

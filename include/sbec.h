@@ -253,9 +253,20 @@ sbec_status sbec_batch_create(const sbec_config* cfg, int32_t n_solves, const do
 sbec_status sbec_batch_create_grids(const sbec_config* cfg, int32_t n_solves, const int32_t* n, const double* L,
                                     const double* c0, const double* c1, const double* const* psi,
                                     const double* const* V, sbec_batch** out);
+/* *supported = 1 when sbec_batch_create would take cfg (contact couplings without DDI,
+ * Raman, losses or the nematic term; grids that take the fused passes: power-of-two axes,
+ * D in {1, 3, 5} and a row pass that fits the first axis), else 0.  Needs no device. */
+sbec_status sbec_batch_supported(const sbec_config* cfg, int32_t* supported);
 sbec_status sbec_batch_destroy(sbec_batch* b);
 sbec_status sbec_batch_ground_state(sbec_batch* b, int64_t n_steps, double tol, int64_t check_every,
                                     sbec_gs_result* out);
+/* The same with a step limit and check interval per solve (n_steps[i], check_every[i]): solve i
+ * follows find_ground_state(n_steps = n_steps[i]) with its convergence test every check_every[i]
+ * steps; the batch advances in blocks up to the next step where some solve checks or stops. */
+sbec_status sbec_batch_ground_state_each(sbec_batch* b, const int64_t* n_steps, double tol,
+                                         const int64_t* check_every, sbec_gs_result* out);
+/* As sbec_set_graph_mode, for every group of the batch. */
+sbec_status sbec_batch_set_graph_mode(sbec_batch* b, int32_t graphs);
 sbec_status sbec_batch_get_psi(sbec_batch* b, int32_t solve, double* psi);
 sbec_status sbec_batch_energies(sbec_batch* b, double* E);
 /* classify_phase of one solve of the batch (as sbec_classify_phase). */
@@ -301,6 +312,10 @@ sbec_status sbec_tune_table_export(char* buf, int64_t cap, int64_t* len);
  * FP32 results may differ between processes at the level of FP32 rounding.  Entries whose
  * variant is not compiled for a shape are ignored there.  No counterpart in the reference. */
 sbec_status sbec_tune_table_import(const char* text);
+/* frozen = 1: a shape missing from the table is no longer timed; it takes its default variant
+ * (recorded in the table), so results cannot depend on a timing race.  0 (default): timed on
+ * first contact.  No counterpart in the reference. */
+sbec_status sbec_tune_freeze(int32_t frozen);
 
 /* Measured FMA throughput of the current device in TFLOP/s (2 flops per FMA), FP32
  * (precision = SBEC_FP32_BULK) or FP64 (SBEC_FP64): eight register-resident FMA chains per

@@ -156,3 +156,41 @@ def test_tune_table_import_fixes_the_variant(gpu):
     assert "from the process table" in ws2.tuning_report
     assert " chosen v" not in ws2.tuning_report  # nothing was timed
     ws2.close()
+
+
+def test_batch_per_solve_limits_match_single_solves_fp64(gpu):
+    """sbec_batch_ground_state_each: every solve with its own step limit and check interval
+    (find_ground_state's max(1, n // 10)) follows the one-at-a-time find_ground_state."""
+    g = S.make_grid(S.GridConfig((32, 32), (12.0, 12.0)))
+    psi0 = S.init_psi(g, 1, "polar")
+    c0s, c1s, steps = [10.0, 12.0, 8.0], [0.5, -0.5, 0.1], [300, 470, 120]
+    b = S.GroundStateBatch(grid=g, atom=S.Rb87, c0s=c0s, c1s=c1s, psi_inits=[psi0] * 3,
+                           potential=S.HarmonicTrap(1.0, 1.0), dt=0.005, precision="fp64")
+    rb = b.ground_state(steps, 1e-9)
+    for i in range(3):
+        rs = S.find_ground_state(grid=g, atom=S.Rb87, interactions=S.InteractionParams(c0s[i], c1s[i]),
+                                 potential=S.HarmonicTrap(1.0, 1.0), dt=0.005, n_steps=steps[i], tol=1e-9,
+                                 initial_state="polar", precision="fp64")
+        assert rb[i]["steps"] == rs["steps"] and rb[i]["converged"] == rs["converged"]
+        assert abs(rb[i]["energy"] - rs["energy"]) <= 1e-12 * abs(rs["energy"])
+        assert rel_psi_err(b.psi(i), rs["workspace"].psi) < 1e-11
+        rs["workspace"].close()
+    b.close()
+
+
+def test_tune_freeze_takes_default_variants_untimed(gpu):
+    """With the table frozen, a shape met for the first time is not timed: it takes its
+    default variant, recorded in the table."""
+    g = S.make_grid(S.GridConfig((128, 32), (16.0, 8.0)))
+    S.tune_freeze(True)
+    try:
+        ws = S.make_workspace(grid=g, atom=S.Rb87, interactions=S.InteractionParams(10.0, 0.5),
+                              potential=S.HarmonicTrap(1.0, 1.0), sim_params=S.SimParams(1e-3, 20, False, None, 10),
+                              precision="fp32")
+        S.run_simulation(ws, keep_psi=False)
+        rep = ws.tuning_report
+        ws.close()
+    finally:
+        S.tune_freeze(False)
+    assert "frozen table: default" in rep
+    assert " chosen v" not in rep

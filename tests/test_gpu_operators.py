@@ -153,7 +153,7 @@ def test_tensor_channels_activation(gpu):
 
 
 def test_unsupported_and_invalid(gpu):
-    og = S.make_grid(S.GridConfig((24,), (10.0,)))
+    og = S.make_grid(S.GridConfig((2050,), (10.0,)))  # even, not a power of two, above 2048
     with pytest.raises(S.UnsupportedError):
         S.make_workspace(grid=og, atom=S.AtomSpecies("x", 1), interactions=S.InteractionParams(1.0, 0.0),
                          sim_params=S.SimParams(1e-3, 1))

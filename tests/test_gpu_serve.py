@@ -41,3 +41,32 @@ def test_served_fp32_ground_state_energy_matches_fp64(gpu):
         e32 = serve.run_request(r)["energy"]
         e64 = serve.run_request(r64)["energy"]
         assert abs(e32 - e64) / abs(e64) < 1e-6, (r.rid, e32, e64)
+
+
+def _same_key(precision):
+    return [serve.SolveRequest(10 + i, "ground_state", (64, 64), (20.0, 20.0), 1, c0, c1, st, dt=0.005,
+                               precision=precision, arrival=0.001 * i)
+            for i, (c0, c1, st) in enumerate([(10.0, -0.5, 600), (14.0, 0.4, 900), (7.0, 0.1, 450)])]
+
+
+def test_merged_ground_states_match_single_requests_fp64(gpu):
+    """Requests of one merge_key run as one batch give each request's own find_ground_state."""
+    reqs = _same_key("fp64")
+    merged = serve.run_batch(reqs)
+    for r, m in zip(reqs, merged):
+        a = serve.run_request(r)
+        assert m["steps"] == a["steps"] and m["converged"] == a["converged"]
+        assert abs(m["energy"] - a["energy"]) <= 1e-12 * abs(a["energy"])
+        assert abs(m["norm"] - a["norm"]) <= 1e-12
+
+
+def test_served_merged_fp32_deterministic_and_within_1e6_of_fp64(gpu):
+    reqs = _same_key("fp32")
+    direct = serve.run_batch(reqs)
+    srv = serve.Server(hbm_budget_bytes=4e9, max_slots=4, merge_window_s=0.05)
+    out = srv.run(reqs, realtime=True)
+    assert srv.merged_units == 1 and srv.merged_requests == 3
+    for res, d, r in zip(out["results"], direct, reqs):
+        assert res.energy == d["energy"] and res.steps == d["steps"]  # same batch, same kernels
+        e64 = serve.run_request(serve.SolveRequest(**{**r.__dict__, "precision": "fp64"}))["energy"]
+        assert abs(res.energy - e64) / abs(e64) < 1e-6, (r.rid, res.energy, e64)

@@ -85,3 +85,82 @@ def test_request_beyond_budget_is_refused():
     srv = serve.Server(hbm_budget_bytes=1e6, runner=lambda r: {})
     with pytest.raises(MemoryError):
         srv.run([req], realtime=False)
+
+
+def _gs(rid, arrival, n=(64, 64), F=1, **kw):
+    return serve.SolveRequest(rid, "ground_state", n, (20.0,) * len(n), F, 10.0 + rid, 0.1, 500 + 10 * rid,
+                              arrival=arrival, **kw)
+
+
+def test_batch_supported_follows_the_fused_passes(libsbec):
+    from spinorbec import api
+    from spinorbec.host import GridConfig, make_grid
+
+    assert api.batch_supported(make_grid(GridConfig((256, 256), (20.0, 20.0))), 1)
+    assert api.batch_supported(make_grid(GridConfig((512, 512), (20.0, 20.0))), 2)
+    assert not api.batch_supported(make_grid(GridConfig((48, 40), (12.0, 10.0))), 1)  # Bluestein axes
+    assert not api.batch_supported(make_grid(GridConfig((16, 16, 16), (8.0,) * 3)), 6)  # D = 13
+    assert not api.batch_supported(make_grid(GridConfig((4096,), (40.0,))), 1)
+
+
+def test_merge_key_admits_only_contact_ground_states(libsbec):
+    assert serve.merge_key(_gs(0, 0.0)) is not None
+    assert serve.merge_key(_gs(0, 0.0, F=2)) == serve.merge_key(_gs(1, 0.3, F=2))
+    assert serve.merge_key(_gs(0, 0.0, F=6)) is None
+    assert serve.merge_key(_gs(0, 0.0, enable_ddi=True)) is None
+    dyn = serve.SolveRequest(0, "dynamics", (64, 64), (20.0, 20.0), 1, 10.0, 0.0, 500)
+    assert serve.merge_key(dyn) is None
+    # grid, dt, tol and precision separate keys
+    assert serve.merge_key(_gs(0, 0.0)) != serve.merge_key(_gs(0, 0.0, n=(128, 128)))
+    assert serve.merge_key(_gs(0, 0.0)) != serve.merge_key(_gs(0, 0.0, dt=0.001))
+    assert serve.merge_key(_gs(0, 0.0)) != serve.merge_key(_gs(0, 0.0, tol=1e-6))
+    assert serve.merge_key(_gs(0, 0.0)) != serve.merge_key(_gs(0, 0.0, precision="fp64"))
+    # grids the batch does not take (a row pass beyond the block limits) are not merged
+    assert serve.merge_key(_gs(0, 0.0, n=(4096,))) is None
+    assert serve.merge_key(_gs(0, 0.0, n=(2048,), F=2)) is None
+    assert serve.merge_key(_gs(0, 0.0, n=(2048,))) is not None
+
+
+def test_dispatch_units_group_by_key_and_window(libsbec):
+    dyn = serve.SolveRequest(9, "dynamics", (64, 64), (20.0, 20.0), 1, 10.0, 0.0, 500, arrival=0.05)
+    reqs = [_gs(0, 0.01), _gs(1, 0.02), _gs(2, 0.03, n=(128, 128)), _gs(3, 0.12), _gs(4, 0.09), dyn]
+    assert [(t, [r.rid for r in rs]) for t, rs in serve.dispatch_units(reqs)] == \
+        [(r.arrival, [r.rid]) for r in sorted(reqs, key=lambda q: q.arrival)]
+    units = serve.dispatch_units(reqs, merge_window_s=0.1)
+    got = [(round(t, 9), [r.rid for r in rs]) for t, rs in units]
+    # window [0, 0.1): 0, 1, 4 share a key, 2 has its own grid; 3 falls in [0.1, 0.2); the
+    # dynamics request is dispatched at its arrival
+    assert got == [(0.05, [9]), (0.1, [0, 1, 4]), (0.1, [2]), (0.2, [3])]
+    # the same arrivals always give the same units
+    assert got == [(round(t, 9), [r.rid for r in rs]) for t, rs in serve.dispatch_units(reqs, merge_window_s=0.1)]
+
+
+def test_dispatch_units_respect_max_merge_and_budget(libsbec):
+    reqs = [_gs(i, 0.001 * i) for i in range(7)]
+    sizes = [len(rs) for _, rs in serve.dispatch_units(reqs, merge_window_s=1.0, max_merge=3)]
+    assert sizes == [3, 3, 1]
+    fp = serve.footprint_bytes(reqs[0])
+    sizes = [len(rs) for _, rs in serve.dispatch_units(reqs, merge_window_s=1.0, budget_bytes=2.5 * fp)]
+    assert sizes == [2, 2, 2, 1]
+
+
+def test_server_runs_merged_units_through_the_batch_runner(libsbec):
+    calls = []
+
+    def batch_runner(rs):
+        calls.append([r.rid for r in rs])
+        return [dict(energy=100.0 + r.rid, norm=1.0, converged=True, steps=r.steps) for r in rs]
+
+    active, peak, lock = [0], [0], threading.Lock()
+    reqs = [_gs(0, 0.001), _gs(1, 0.002), _gs(2, 0.003, F=6), _gs(3, 0.004)]
+    srv = serve.Server(hbm_budget_bytes=1e12, max_slots=4, runner=_fake_runner(active, lock, peak),
+                       batch_runner=batch_runner, merge_window_s=0.05)
+    out = srv.run(reqs, realtime=True)
+    assert calls == [[0, 1, 3]]
+    assert srv.merged_units == 1 and srv.merged_requests == 3
+    res = {r.rid: r for r in out["results"]}
+    assert sorted(res) == [0, 1, 2, 3]
+    for rid in (0, 1, 3):
+        assert res[rid].energy == 100.0 + rid and res[rid].admitted >= 0.05 - 1e-3
+        assert res[rid].steps == reqs[rid].steps
+    assert res[2].energy == 2.0  # the fake single runner
