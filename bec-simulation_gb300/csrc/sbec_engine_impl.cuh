@@ -2022,13 +2022,28 @@ class Engine final : public EngineBase {
   }
   void launch_potential(const PotArgs<R>& a) { SBEC_SWITCH_D(s_.D, launch_potential_d, a); }
 
+  template <int D, int RL>
+  void launch_tensor_lanes(const TensorArgs<R>& a) {
+    if constexpr (sizeof(R) == 4) {
+      using TL = TensorLanes<D, RL>;
+      const size_t smem = TL::smem_bytes();
+      auto kern = k_tensor_lanes<D, RL>;
+      static const bool once = (set_smem(kern, smem), true);
+      (void)once;
+      pb();
+      kern<<<(unsigned)((N_ + TL::PPB - 1) / TL::PPB), 256, smem, stream_>>>(a);
+      done("tensor", (2.0 * (double)sizeof(cplx<R>) * D + (double)sizeof(R)) * (double)N_);
+    }
+  }
+
   template <int D>
   void launch_tensor_d(const TensorArgs<R>& a) {
     if constexpr (sizeof(R) == 4) {
-      // default: rows of h in registers up to D = 9 (F <= 4), lane groups above (a 128^3 grid
-      // on GB300: D = 5 0.69 against 1.39 ms, D = 9 3.00 against 3.23 ms, D = 13 9.0 against
-      // 2.9 ms, where the rows kernel's 255 registers leave 7 warps per SM)
-      const int mode = tensor_mode_ >= 0 ? tensor_mode_ : (D <= 9 ? 2 : 1);
+      // default: rows of h in registers up to D = 5, lane groups with two rows per lane above
+      // (ms per call on a 128^3 grid, modes 1 / 2 / 3: D = 5 1.38 / 0.69 / 0.85, D = 7 1.58 /
+      // 1.42 / 1.20, D = 9 3.23 / 3.01 / 2.25, D = 11 3.76 / 6.34 / 3.49, D = 13 2.91 / 9.04 /
+      // 2.46; the rows kernel's registers grow with D: 255 at D = 13, 7 warps per SM)
+      const int mode = tensor_mode_ >= 0 ? tensor_mode_ : (D <= 5 ? 2 : 3);
       if (mode == 2) {
         constexpr int NW = (D + 1) / 2;
         pb();
@@ -2037,14 +2052,11 @@ class Engine final : public EngineBase {
         return;
       }
       if (mode == 1) {
-        using TL = TensorLanes<D>;
-        const size_t smem = TL::smem_bytes();
-        auto kern = k_tensor_lanes<D>;
-        static const bool once = (set_smem(kern, smem), true);
-        (void)once;
-        pb();
-        kern<<<(unsigned)((N_ + TL::PPB - 1) / TL::PPB), 256, smem, stream_>>>(a);
-        done("tensor", (2.0 * (double)sizeof(cplx<R>) * D + (double)sizeof(R)) * (double)N_);
+        launch_tensor_lanes<D, 1>(a);
+        return;
+      }
+      if (mode == 3) {
+        launch_tensor_lanes<D, 2>(a);
         return;
       }
     }
@@ -2186,8 +2198,9 @@ class Engine final : public EngineBase {
   // line-kernel variants in use (see sbec_lines.h); chosen by the autotuner
   int v_row_ = 0, v_str_ = 0, v_x_ = 0;
   bool merged_itp_ = false;  // SBEC_BATCH_MERGED=1: two-pass FP32 batched ITP step (predicted scale)
-  // FP32 tensor kernel (SBEC_TENSOR_LANES): 0 one thread per point, 1 a lane group per point,
-  // 2 rows of h in registers ((D + 1) / 2 warps per 32 points); -1 (default) by D
+  // FP32 tensor kernel (SBEC_TENSOR_LANES): 0 one thread per point, 1 a lane group per point
+  // (one row of h per lane), 2 rows of h in registers ((D + 1) / 2 warps per 32 points), 3 a
+  // lane group with two rows per lane; -1 (default) by D
   int tensor_mode_ = -1;
   float* G32_ = nullptr;
   R* bcorr_ = nullptr;  // merged FP32 batched ITP: per-solve correction, prediction, ones

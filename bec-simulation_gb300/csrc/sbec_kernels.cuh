@@ -1538,25 +1538,30 @@ __global__ void __launch_bounds__(64) k_tensor(TensorArgs<R> a) {
 }
 
 // ---------------------------------------------------------------------------
-// FP32 tensor step with one group of L lanes per point (lane c holds component c):
-// the same operator as tensor_point, laid out for occupancy.  One thread per point
-// needs the whole 13-component spinor, h and the series terms in registers (255 and
-// spills for F = 6) and keeps 8 warps per SM resident; here each lane holds one row of
-// h, the upper triangle of h is built cooperatively (entries round-robin over the
-// lanes, lower entries taken as conjugates so h stays exactly Hermitian) and each
-// Horner product broadcasts the vector through a double-buffered shared slot.  After
-// the block-wide staging of G, groups synchronise only among their own lanes.
+// FP32 tensor step with one group of L lanes per point (lane c holds components c, c + L,
+// ... — RL of them): the same operator as tensor_point, laid out for occupancy.  One thread
+// per point needs the whole 13-component spinor, h and the series terms in registers (255
+// and spills for F = 6) and keeps 8 warps per SM resident; here each lane holds RL rows of
+// h, the upper triangle of h is built cooperatively (entries round-robin over the lanes,
+// lower entries taken as conjugates so h stays exactly Hermitian) and each Horner product
+// broadcasts the vector through a double-buffered shared slot (D loads per lane and step
+// for RL rows of D complex products: RL = 2 doubles the arithmetic per shared load).
+// After the block-wide staging of G, groups synchronise only among their own lanes.
 // ---------------------------------------------------------------------------
-template <int D>
+template <int D, int RL = 1>
 struct TensorLanes {
-  static constexpr int L = D <= 8 ? 8 : 16;  // lanes per point
+  // lanes per point: one row of h per lane (8 or 16 lanes), or RL rows per lane (the power of
+  // two at or above ceil(D / RL)); lane c owns components c, c + L, ...
+  static constexpr int L = RL == 1 ? (D <= 8 ? 8 : 16)
+                                   : ((D + RL - 1) / RL <= 2 ? 2 : (D + RL - 1) / RL <= 4 ? 4 : (D + RL - 1) / RL <= 8 ? 8 : 16);
+  static constexpr int YB = L * RL;          // entries of one vector buffer (>= D)
   static constexpr int PPB = 256 / L;        // points per 256-thread block
   static constexpr int NJ = 2 * D - 1;
   static constexpr int NT = D * (D + 1) / 2;  // upper-triangle entries
   static constexpr int G_FLOATS = (NJ * D * D + 3) / 4 * 4;
   static constexpr int E_INTS = (NT + 3) / 4 * 4;
   static constexpr size_t smem_bytes() {
-    return sizeof(float) * G_FLOATS + sizeof(int) * E_INTS + sizeof(float2) * (size_t)PPB * (NT + D * D + 2 * L);
+    return sizeof(float) * G_FLOATS + sizeof(int) * E_INTS + sizeof(float2) * (size_t)PPB * (NT + D * D + 2 * YB);
   }
 };
 
@@ -1567,30 +1572,45 @@ __device__ __forceinline__ float group_sum(float x, unsigned mask) {
   return x;
 }
 
-template <int D, int L>
-__device__ __forceinline__ void diag_lane(float2& v, float Vp, const TensorArgs<float>& a, bool own, int c,
+template <int D, int L, int RL>
+__device__ __forceinline__ void diag_lane(float2 (&v)[RL], float Vp, const TensorArgs<float>& a, int c,
                                           unsigned mask) {
-  const float n = group_sum<L>(own ? abs2(v) : 0.0f, mask);
+  float s = 0.0f;
+#pragma unroll
+  for (int r = 0; r < RL; ++r)
+    if (c + L * r < D) s += abs2(v[r]);
+  const float n = group_sum<L>(s, mask);
   float Vint = a.c0 * n;
   if (a.c_lhy != 0.0f) Vint += a.c_lhy * n * sqrtf(n);
   const float veff = Vp + Vint;
-  if (!own) return;
-  if (a.itp) {
-    v = v * (expf(-veff * a.tau_d) * a.zee[c].x);
-  } else {
-    float sn, cm1;
-    sin_cosm1(veff * a.tau_d, sn, cm1);
-    v = rot_small(cmul_comp(v, a.zee[c], a.zee_lo[c]), cm1, sn);
+#pragma unroll
+  for (int r = 0; r < RL; ++r) {
+    const int comp = c + L * r;
+    if (comp >= D) continue;
+    if (a.itp) {
+      v[r] = v[r] * (expf(-veff * a.tau_d) * a.zee[comp].x);
+    } else {
+      float sn, cm1;
+      sin_cosm1(veff * a.tau_d, sn, cm1);
+      v[r] = rot_small(cmul_comp(v[r], a.zee[comp], a.zee_lo[comp]), cm1, sn);
+    }
   }
 }
 
-template <int D, int L>
-__device__ __forceinline__ void tensor_lane(float2& v, const TensorArgs<float>& a, const float* Gs, const int* Ent,
-                                            float2* Ps, float2* Hs, float2* Ys, bool own, int c, unsigned mask) {
+template <int D, int L, int RL>
+__device__ __forceinline__ void tensor_lane(float2 (&v)[RL], const TensorArgs<float>& a, const float* Gs,
+                                            const int* Ent, float2* Ps, float2* Hs, float2* Ys, int c, unsigned mask) {
   constexpr int NT = D * (D + 1) / 2;
-  const float nl = group_sum<L>(own ? abs2(v) : 0.0f, mask);
+  constexpr int YB = L * RL;
+  float s = 0.0f;
+#pragma unroll
+  for (int r = 0; r < RL; ++r)
+    if (c + L * r < D) s += abs2(v[r]);
+  const float nl = group_sum<L>(s, mask);
   if (nl < 1e-20f) return;
-  if (own) Ys[c] = v;
+#pragma unroll
+  for (int r = 0; r < RL; ++r)
+    if (c + L * r < D) Ys[c + L * r] = v[r];
   __syncwarp(mask);
   // products P[b][a] = conj(v_b) v_a (b <= a), upper-triangle storage, row b from b*D - b(b-1)/2
   for (int e = c; e < NT; e += L) {
@@ -1618,9 +1638,14 @@ __device__ __forceinline__ void tensor_lane(float2& v, const TensorArgs<float>& 
     Hs[i * D + j] = acc;
   }
   __syncwarp(mask);
-  float2 hrow[D];
+  float2 hrow[RL][D];
 #pragma unroll
-  for (int j = 0; j < D; ++j) hrow[j] = !own ? mk<float>(0.0f, 0.0f) : (j >= c ? Hs[c * D + j] : conj(Hs[j * D + c]));
+  for (int r = 0; r < RL; ++r) {
+    const int comp = c + L * r;
+#pragma unroll
+    for (int j = 0; j < D; ++j)
+      hrow[r][j] = comp >= D ? mk<float>(0.0f, 0.0f) : (j >= comp ? Hs[comp * D + j] : conj(Hs[j * D + comp]));
+  }
   const double x = a.bound_coef * (double)nl * fabs((double)a.tau);
   int nsub = 1;
   if (x > 0.5) nsub = x < 0.5 * kMaxSub ? (int)ceil(x / 0.5) : kMaxSub;  // bounded for non-finite states
@@ -1637,24 +1662,34 @@ __device__ __forceinline__ void tensor_lane(float2& v, const TensorArgs<float>& 
   }
   const float dtau = a.tau / (float)nsub;
   for (int sub = 0; sub < nsub; ++sub) {
-    float2 y = v;
-    for (int k = K; k >= 1; --k) {
-      float2* yb = Ys + (k & 1) * L;
-      if (own) yb[c] = y;
-      __syncwarp(mask);
-      float2 t = mk<float>(0.0f, 0.0f);
+    float2 y[RL];
 #pragma unroll
-      for (int j = 0; j < D; ++j) t += hrow[j] * yb[j];
+    for (int r = 0; r < RL; ++r) y[r] = v[r];
+    for (int k = K; k >= 1; --k) {
+      float2* yb = Ys + (k & 1) * YB;
+#pragma unroll
+      for (int r = 0; r < RL; ++r)
+        if (c + L * r < D) yb[c + L * r] = y[r];
+      __syncwarp(mask);
       const float f = dtau / (float)k;
-      if (k == 1 && !a.itp) {
-        // unbiased rounding of the last addition (as in rotate_taylor)
-        const float2 corr = mul_mi(f * t);
-        y = mk<float>(sr_add(v.x, corr.x, 0x27d4eb2fu + 0x165667b1u * c), sr_add(v.y, corr.y, 0x9e3779b1u + 0x85ebca77u * c));
-      } else {
-        y = v + (a.itp ? (-f) * t : mul_mi(f * t));
+#pragma unroll
+      for (int r = 0; r < RL; ++r) {
+        const int comp = c + L * r;
+        float2 t = mk<float>(0.0f, 0.0f);
+#pragma unroll
+        for (int j = 0; j < D; ++j) t += hrow[r][j] * yb[j];
+        if (k == 1 && !a.itp) {
+          // unbiased rounding of the last addition (as in rotate_taylor)
+          const float2 corr = mul_mi(f * t);
+          y[r] = mk<float>(sr_add(v[r].x, corr.x, 0x27d4eb2fu + 0x165667b1u * comp),
+                           sr_add(v[r].y, corr.y, 0x9e3779b1u + 0x85ebca77u * comp));
+        } else {
+          y[r] = v[r] + (a.itp ? (-f) * t : mul_mi(f * t));
+        }
       }
     }
-    v = y;
+#pragma unroll
+    for (int r = 0; r < RL; ++r) v[r] = y[r];
   }
   __syncwarp(mask);
 }
@@ -1790,9 +1825,9 @@ __global__ void __launch_bounds__(32 * NW) k_tensor_rows(TensorArgs<float> a) {
     if (c % NW == q) a.psi[c * a.N + p] = v[c];
 }
 
-template <int D>
+template <int D, int RL>
 __global__ void __launch_bounds__(256) k_tensor_lanes(TensorArgs<float> a) {
-  using TL = TensorLanes<D>;
+  using TL = TensorLanes<D, RL>;
   constexpr int L = TL::L;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float* Gs = reinterpret_cast<float*>(smem_raw);
@@ -1816,14 +1851,17 @@ __global__ void __launch_bounds__(256) k_tensor_lanes(TensorArgs<float> a) {
   const int64_t p = (int64_t)blockIdx.x * TL::PPB + g;
   if (p >= a.N) return;  // the whole group leaves; only group-local synchronisation follows
   const unsigned mask = ((L == 32) ? 0xffffffffu : ((1u << L) - 1u)) << ((tid & 31) / L * L);
-  const bool own = c < D;
-  float2 v = own ? a.psi[c * a.N + p] : mk<float>(0.0f, 0.0f);
+  float2 v[RL];
+#pragma unroll
+  for (int r = 0; r < RL; ++r) v[r] = c + L * r < D ? a.psi[(c + L * r) * a.N + p] : mk<float>(0.0f, 0.0f);
   const float Vp = a.V[p];
-  if (a.pre_diag) diag_lane<D, L>(v, Vp, a, own, c, mask);
+  if (a.pre_diag) diag_lane<D, L, RL>(v, Vp, a, c, mask);
   for (int r = 0; r < a.n_apply; ++r)
-    tensor_lane<D, L>(v, a, Gs, Ent, Psb + g * TL::NT, Hs + g * D * D, Ysb + g * 2 * L, own, c, mask);
-  if (a.post_diag) diag_lane<D, L>(v, Vp, a, own, c, mask);
-  if (own) a.psi[c * a.N + p] = v;
+    tensor_lane<D, L, RL>(v, a, Gs, Ent, Psb + g * TL::NT, Hs + g * D * D, Ysb + g * 2 * TL::YB, c, mask);
+  if (a.post_diag) diag_lane<D, L, RL>(v, Vp, a, c, mask);
+#pragma unroll
+  for (int r = 0; r < RL; ++r)
+    if (c + L * r < D) a.psi[(c + L * r) * a.N + p] = v[r];
 }
 
 // Spin density only (src/observables.jl:61-86).

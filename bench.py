@@ -396,11 +396,11 @@ def bench_serving(S, n_requests: int, fp64_probe_steps: int = 20, check_budget_s
         est64 += cost[r.rid]
     # accuracy of served energies against the plain FP64 form (same request, same steps / tol).
     # Ground states: the 1e-6 energy bar.  Real-time runs: the FP32 - FP64 difference of the final
-    # energy, split by whether the FP64 run itself conserves energy (drift below 1e-4 over the
-    # run); where it does not, dt is too coarse for the grid's fastest kinetic phase and the
-    # discrete dynamics is chaotic, so two roundings of it part ways.
+    # energy, split by whether the FP64 run itself conserves energy to the 1e-6 bar over the run
+    # (where it does not, the time discretisation moves the energy by more than the bar and the
+    # two roundings of the dynamics part ways), with each form's own energy drift beside it.
     t0 = time.perf_counter()
-    errs, dyn_ok, dyn_bad = [], [], []
+    errs, dyn_ok, dyn_bad, drift32, drift64 = [], [], [], [], []
     for r in sorted(reqs, key=lambda q: cost[q.rid]):
         if time.perf_counter() - t0 + cost[r.rid] > check_budget_s:
             break
@@ -411,7 +411,9 @@ def bench_serving(S, n_requests: int, fp64_probe_steps: int = 20, check_budget_s
             errs.append(rel)
         else:
             drift = abs(o64["energy"] - o64["energy0"]) / abs(o64["energy0"])
-            (dyn_ok if drift < 1e-4 else dyn_bad).append(rel)
+            drift64.append(drift)
+            drift32.append(abs(e32 - o64["energy0"]) / abs(o64["energy0"]))
+            (dyn_ok if drift < 1e-6 else dyn_bad).append(rel)
     lat = sorted(x.latency for x in out["results"])
     return {"workload": f"{n_requests} requests of the seeded Poisson stream (mean 200 req/s): 1-D 256..4096, "
                         "2-D 64^2..512^2, 3-D 32^3..128^3, F in {1,2,6}, DDI for F=6, 500-5000 steps, "
@@ -433,11 +435,16 @@ def bench_serving(S, n_requests: int, fp64_probe_steps: int = 20, check_budget_s
                 "ground_states": {"checked": len(errs), "of": sum(1 for r in reqs if r.kind == "ground_state"),
                                   "max_energy_rel_err": max(errs) if errs else None,
                                   "above_1e-6": sum(1 for e in errs if e > 1e-6)},
-                "dynamics_energy_conserving": {"checked": len(dyn_ok),
-                                               "max_energy_rel_err": max(dyn_ok) if dyn_ok else None,
-                                               "above_1e-6": sum(1 for e in dyn_ok if e > 1e-6)},
-                "dynamics_fp64_drift_above_1e-4": {"checked": len(dyn_bad),
-                                                   "max_energy_rel_err": max(dyn_bad) if dyn_bad else None}}}
+                "dynamics_fp64_conserves_to_1e-6": {"checked": len(dyn_ok),
+                                                    "max_energy_rel_err": max(dyn_ok) if dyn_ok else None,
+                                                    "above_1e-6": sum(1 for e in dyn_ok if e > 1e-6)},
+                "dynamics_fp64_drift_above_1e-6": {"checked": len(dyn_bad),
+                                                   "max_energy_rel_err": max(dyn_bad) if dyn_bad else None},
+                "dynamics_energy_drift_over_run": {
+                    "fp64_median": float(np.median(drift64)) if drift64 else None,
+                    "fp32_median": float(np.median(drift32)) if drift32 else None,
+                    "fp64_max": max(drift64) if drift64 else None, "fp32_max": max(drift32) if drift32 else None,
+                    "how": "|E(T) - E(0)| / |E(0)| of each form, E(0) of the FP64 run"}}}
 
 
 def _logged(runner):

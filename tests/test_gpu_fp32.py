@@ -49,11 +49,11 @@ def test_fp32_real_time_error_bounded(gpu, case):
 
 
 @pytest.mark.parametrize("F,lanes", [(2, "1"), (6, "1"), (6, "0"), (2, "2"), (3, "2"), (4, "2"), (5, "2"), (6, "2"),
-                                     (2, "-1"), (5, "-1")])
+                                     (2, "3"), (4, "3"), (5, "3"), (6, "3"), (2, "-1"), (5, "-1"), (6, "-1")])
 def test_fp32_tensor_step_kernels(gpu, F, lanes):
     """The FP32 general-F tensor step against the FP64 oracle, each kernel form by
     SBEC_TENSOR_LANES: 1 the lane-group kernel, 0 one thread per point, 2 rows of h in
-    registers, -1 the default choice by D."""
+    registers, 3 lane groups with two rows per lane, -1 the default choice by D."""
     import os
 
     ip = O.interaction_params_from_constraint(c_total=600.0, c1_ratio=1 / 36, F=F,
