@@ -1470,6 +1470,7 @@ __device__ __forceinline__ void tensor_point(cplx<R> (&v)[D], const TensorArgs<R
         const R gcoef = (R)__ldg(a.G + ((size_t)J * D + c) * D + cp);
         acc += gcoef * cmulc(v[J - c], v[J - cp]);
       }
+      if (c == cp) acc.y = (R)0;  // h is Hermitian: a real diagonal (not the rounding residual of conj(v) v)
       hs[hi * hstride] = acc;
       ++hi;
     }
@@ -1612,10 +1613,13 @@ __device__ __forceinline__ void tensor_lane(float2 (&v)[RL], const TensorArgs<fl
   for (int r = 0; r < RL; ++r)
     if (c + L * r < D) Ys[c + L * r] = v[r];
   __syncwarp(mask);
-  // products P[b][a] = conj(v_b) v_a (b <= a), upper-triangle storage, row b from b*D - b(b-1)/2
+  // products P[b][a] = conj(v_b) v_a (b <= a), upper-triangle storage, row b from b*D - b(b-1)/2;
+  // P[b][b] = |v_b|^2 exactly real (the fused form of conj(v) v keeps the rounding residual of
+  // x y as an imaginary part, which would make the diagonal of h complex and the step
+  // non-unitary)
   for (int e = c; e < NT; e += L) {
     const int b = Ent[e] & 0xff, aa = Ent[e] >> 8;
-    Ps[b * D - b * (b - 1) / 2 + (aa - b)] = cmulc(Ys[b], Ys[aa]);
+    Ps[b * D - b * (b - 1) / 2 + (aa - b)] = b == aa ? mk<float>(abs2(Ys[b]), 0.0f) : cmulc(Ys[b], Ys[aa]);
   }
   __syncwarp(mask);
   // h[i][j] (j >= i) = sum_{J=j}^{i+D-1} G[J][i][j] conj(v[J-i]) v[J-j] = sum G conj(P[J-j][J-i]);

@@ -181,7 +181,7 @@ def test_batch_per_solve_limits_match_single_solves_fp64(gpu):
 def test_tune_freeze_takes_default_variants_untimed(gpu):
     """With the table frozen, a shape met for the first time is not timed: it takes its
     default variant, recorded in the table."""
-    g = S.make_grid(S.GridConfig((128, 32), (16.0, 8.0)))
+    g = S.make_grid(S.GridConfig((32, 256), (8.0, 16.0)))  # a shape no other test tunes
     S.tune_freeze(True)
     try:
         ws = S.make_workspace(grid=g, atom=S.Rb87, interactions=S.InteractionParams(10.0, 0.5),
