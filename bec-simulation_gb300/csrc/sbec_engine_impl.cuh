@@ -1993,6 +1993,12 @@ class Engine final : public EngineBase {
       }
       out[c] = mk<R>((R)re, (R)im);
       out_lo[c] = mk<R>((R)(re - (double)out[c].x), (R)(im - (double)out[c].y));
+      if (sizeof(R) == 4 && !it) {
+        // the FP32 real-time diagonal step turns by e^{i arg} in small quantities
+        // (rot_small_zee): cos arg - 1 = -2 sin^2(arg / 2) without cancellation, and sin arg
+        const double s2 = std::sin(-(E[c] * tau) / 2);
+        out_lo[c] = mk<R>((R)(-2.0 * s2 * s2), (R)im);
+      }
     }
   }
 

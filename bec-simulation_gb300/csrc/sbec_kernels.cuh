@@ -656,7 +656,7 @@ struct PotArgs {
   R tau_d, tau_s, tau_ddi;
   R c0, c1, c_lhy, c2;
   cplx<R> zee[kMaxD];          // per-component Zeeman factor for diag(tau_d)
-  cplx<R> zee_lo[kMaxD];       // FP32 tails of the Zeeman factors
+  cplx<R> zee_lo[kMaxD];       // FP32 real time: (cos theta - 1, sin theta) of the factor e^{i theta}
   // Raman rotation exp(-i tau_r b(r)·F) after nem_a (raman_a) / before nem_b (raman_b)
   int raman_a, raman_b;
   R tau_r;
@@ -701,6 +701,16 @@ __device__ __forceinline__ float2 rot_small(float2 z, float cm1, float sn) {
   const float bx = __fmaf_rn(z.x, cm1, __fmul_rn(z.y, sn));
   const float by = __fmaf_rn(z.y, cm1, __fmul_rn(-z.x, sn));
   return make_float2(sr_add(z.x, bx, 0x9e3779b9u), sr_add(z.y, by, 0x7f4a7c15u));
+}
+
+// z e^{-i phi} e^{i theta} (the potential phase and a Zeeman phase) as one rotation with one
+// unbiased addition: (cm1, sn) = (cos phi - 1, sin phi), zcs = (cos theta - 1, sin theta).
+// Turning z by the Zeeman factor in a separate rounded product would drop the radial part
+// of the small rotation (below half an ulp) at every call and |z| would grow.
+__device__ __forceinline__ float2 rot_small_zee(float2 z, float cm1, float sn, float2 zcs) {
+  const float C = __fadd_rn(__fadd_rn(cm1, zcs.x), __fmaf_rn(cm1, zcs.x, __fmul_rn(sn, zcs.y)));
+  const float S = __fadd_rn(__fsub_rn(zcs.y, sn), __fmaf_rn(cm1, zcs.y, __fmul_rn(-sn, zcs.x)));
+  return rot_small(z, C, -S);
 }
 
 // u + (a A + b B) with the correction formed in full before the single addition to u
@@ -755,7 +765,7 @@ __device__ __forceinline__ void diag_apply(cplx<R> (&v)[D], R veff, R tau, int i
     float sn, cm1;
     sin_cosm1(veff * tau, sn, cm1);
 #pragma unroll
-    for (int c = 0; c < D; ++c) v[c] = rot_small(cmul_comp(v[c], zee[c], zee_lo[c]), cm1, sn);
+    for (int c = 0; c < D; ++c) v[c] = rot_small_zee(v[c], cm1, sn, zee_lo[c]);
   }
 }
 
@@ -1593,7 +1603,7 @@ __device__ __forceinline__ void diag_lane(float2 (&v)[RL], float Vp, const Tenso
     } else {
       float sn, cm1;
       sin_cosm1(veff * a.tau_d, sn, cm1);
-      v[r] = rot_small(cmul_comp(v[r], a.zee[comp], a.zee_lo[comp]), cm1, sn);
+      v[r] = rot_small_zee(v[r], cm1, sn, a.zee_lo[comp]);
     }
   }
 }
