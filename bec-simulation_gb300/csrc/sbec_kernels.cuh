@@ -1566,13 +1566,17 @@ struct TensorLanes {
   static constexpr int L = RL == 1 ? (D <= 8 ? 8 : 16)
                                    : ((D + RL - 1) / RL <= 2 ? 2 : (D + RL - 1) / RL <= 4 ? 4 : (D + RL - 1) / RL <= 8 ? 8 : 16);
   static constexpr int YB = L * RL;          // entries of one vector buffer (>= D)
+  // per-group stride of the two vector buffers: one entry of padding, so that the groups of
+  // a warp reading their own y_j in the same Horner step hit different banks (at 2 YB, a
+  // multiple of 32 words, they all hit one)
+  static constexpr int YS = 2 * YB + 1;
   static constexpr int PPB = 256 / L;        // points per 256-thread block
   static constexpr int NJ = 2 * D - 1;
   static constexpr int NT = D * (D + 1) / 2;  // upper-triangle entries
   static constexpr int G_FLOATS = (NJ * D * D + 3) / 4 * 4;
   static constexpr int E_INTS = (NT + 3) / 4 * 4;
   static constexpr size_t smem_bytes() {
-    return sizeof(float) * G_FLOATS + sizeof(int) * E_INTS + sizeof(float2) * (size_t)PPB * (NT + D * D + 2 * YB);
+    return sizeof(float) * G_FLOATS + sizeof(int) * E_INTS + sizeof(float2) * (size_t)PPB * (NT + D * D + YS);
   }
 };
 
@@ -1871,7 +1875,7 @@ __global__ void __launch_bounds__(256) k_tensor_lanes(TensorArgs<float> a) {
   const float Vp = a.V[p];
   if (a.pre_diag) diag_lane<D, L, RL>(v, Vp, a, c, mask);
   for (int r = 0; r < a.n_apply; ++r)
-    tensor_lane<D, L, RL>(v, a, Gs, Ent, Psb + g * TL::NT, Hs + g * D * D, Ysb + g * 2 * TL::YB, c, mask);
+    tensor_lane<D, L, RL>(v, a, Gs, Ent, Psb + g * TL::NT, Hs + g * D * D, Ysb + g * TL::YS, c, mask);
   if (a.post_diag) diag_lane<D, L, RL>(v, Vp, a, c, mask);
 #pragma unroll
   for (int r = 0; r < RL; ++r)

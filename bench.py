@@ -821,6 +821,10 @@ def ncu_case(args) -> None:
 
     k = args.ncu_steps
     case = args.ncu_case
+    if args.ncu_tune_table:
+        # the tuned variants of an earlier run: no autotuner trial launches in the capture
+        with open(args.ncu_tune_table) as f:
+            S.tune_table_import(f.read())
     if case in ("2d256_fp32", "2d256_fp64"):
         g = S.make_grid(S.GridConfig(N_GRID, BOX))
         ws = S.make_workspace(grid=g, atom=S.Na23, interactions=S.InteractionParams(C0, C1), zeeman=S.ZeemanParams(ZP, ZQ),
@@ -847,6 +851,9 @@ def ncu_case(args) -> None:
         S.split_step(ws, k)
     else:
         raise SystemExit(f"unknown --ncu-case {case}")
+    if args.ncu_export_table:
+        with open(args.ncu_export_table, "w") as f:
+            f.write(S.tune_table_export())
     print(f"ncu case {case}: {k} steps done")
 
 
@@ -890,6 +897,8 @@ def main():
     ap.add_argument("--ncu-case", default=None, help="short run for profiling: 2d256_fp32|2d256_fp64|batch256_fp32|3d_f6_fp32|3d_f6_fp64")
     ap.add_argument("--ncu-steps", type=int, default=4)
     ap.add_argument("--ncu-grid", type=int, default=32)
+    ap.add_argument("--ncu-tune-table", default=None, help="import this tune table first (no autotuner trials)")
+    ap.add_argument("--ncu-export-table", default=None, help="write the tune table after the run")
     ap.add_argument("--ncu-batch", type=int, default=170, help="solves in the batch256_fp32 case (the 256^2 group)")
     args = ap.parse_args()
     if args.only:
