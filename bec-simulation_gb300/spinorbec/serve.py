@@ -217,35 +217,64 @@ def pretune(requests: list, merge_window_s: float = 0.0, max_merge: int = 32) ->
     return len(seen)
 
 
+def work_estimate(req: SolveRequest) -> float:
+    """Relative cost of a request for admission order: points x components x steps, four
+    times that with the dipolar convolution (its six FFTs on the padded grid)."""
+    w = float(np.prod(req.n_points)) * (2 * req.F + 1) * req.steps
+    return 4.0 * w if req.enable_ddi else w
+
+
 class Server:
-    """Admission by HBM budget and slots; concurrent resident workspaces."""
+    """Admission by HBM budget and slots; concurrent resident workspaces.
+
+    policy "fifo" admits waiting units in the order they were dispatched; "sjf" admits the
+    waiting unit with the least estimated work (work_estimate, summed over a merged unit)
+    first, ties by dispatch order — the same solves and results, shorter queueing for short
+    requests."""
 
     def __init__(self, hbm_budget_bytes: float = 150e9, max_slots: int = 32,
                  runner: Callable[[SolveRequest], dict] = run_request,
                  batch_runner: Callable[[list], list] = run_batch, merge_window_s: float = 0.0,
-                 max_merge: int = 32):
+                 max_merge: int = 32, policy: str = "fifo"):
+        if policy not in ("fifo", "sjf"):
+            raise ValueError("policy must be 'fifo' or 'sjf'")
         self.budget = float(hbm_budget_bytes)
         self.max_slots = int(max_slots)
         self.runner = runner
         self.batch_runner = batch_runner
         self.merge_window_s = float(merge_window_s)
         self.max_merge = int(max_merge)
+        self.policy = policy
         self.merged_units = 0
         self.merged_requests = 0
         self._used = 0.0
         self._active = 0
+        self._waiting: dict = {}  # ticket -> (priority key, footprint)
+        self._tickets = 0
         self.peak_used = 0.0
         self.peak_active = 0
         self._cv = threading.Condition()
 
-    def _admit(self, fp: int) -> None:
+    def _fits(self, fp: int) -> bool:
+        return self._active < self.max_slots and (self._used + fp <= self.budget or self._active == 0)
+
+    def _admit(self, fp: int, work: float = 0.0, seq: Optional[int] = None) -> None:
         with self._cv:
-            while self._active >= self.max_slots or (self._used + fp > self.budget and self._active > 0):
+            ticket = self._tickets
+            self._tickets += 1
+            order = ticket if seq is None else seq  # dispatch order
+            key = (work, order) if self.policy == "sjf" else (0.0, order)
+            self._waiting[ticket] = (key, fp)
+            # admitted when it fits and no waiting unit ahead of it in the policy's order fits
+            while not (self._fits(fp) and
+                       all(not (k < key and self._fits(f)) for k, f in self._waiting.values())):
                 self._cv.wait()
+            del self._waiting[ticket]
             self._used += fp
             self._active += 1
             self.peak_used = max(self.peak_used, self._used)
             self.peak_active = max(self.peak_active, self._active)
+            self._cv.notify_all()
 
     def _release(self, fp: int) -> None:
         with self._cv:
@@ -262,12 +291,12 @@ class Server:
         results: list = []
         lock = threading.Lock()
 
-        def serve(reqs: list):
+        def serve(seq: int, reqs: list):
             fps = [footprint_bytes(r) for r in reqs]
             fp = sum(fps)
             if fp > self.budget:
                 raise MemoryError(f"request {reqs[0].rid} needs {fp / 1e9:.1f} GB > budget")
-            self._admit(fp)
+            self._admit(fp, sum(work_estimate(r) for r in reqs), seq)
             admitted = time.perf_counter() - t0
             try:
                 outs = [self.runner(reqs[0])] if len(reqs) == 1 else self.batch_runner(reqs)
@@ -284,14 +313,16 @@ class Server:
             if len(rs) > 1:
                 self.merged_units += 1
                 self.merged_requests += len(rs)
-        with ThreadPoolExecutor(max_workers=self.max_slots + 4) as ex:
+        # one thread per dispatched unit: every unit that has arrived waits in _admit, so the
+        # admission policy chooses among all of them
+        with ThreadPoolExecutor(max_workers=max(self.max_slots + 4, len(units))) as ex:
             futs = []
-            for t_disp, rs in units:
+            for seq, (t_disp, rs) in enumerate(units):
                 if realtime:
                     wait = t_disp - (time.perf_counter() - t0)
                     if wait > 0:
                         time.sleep(wait)
-                futs.append(ex.submit(serve, rs))
+                futs.append(ex.submit(serve, seq, rs))
             for f in futs:
                 f.result()
         wall = time.perf_counter() - t0

@@ -374,10 +374,11 @@ def bench_serving(S, n_requests: int, fp64_probe_steps: int = 20, check_budget_s
 
     reqs = serve.poisson_requests(n_requests, rate=200.0, seed=5)
     window = 0.25
+    policy = "sjf"  # shortest estimated work first among the units waiting for admission
     n_shapes = serve.pretune(reqs, merge_window_s=window)
     log(f"serving: autotuner fixed for {n_shapes} shapes")
     srv = serve.Server(hbm_budget_bytes=150e9, max_slots=32, runner=_logged(serve.run_request),
-                       merge_window_s=window)
+                       merge_window_s=window, policy=policy)
     try:
         out = srv.run(reqs, realtime=True)
     finally:
@@ -419,6 +420,8 @@ def bench_serving(S, n_requests: int, fp64_probe_steps: int = 20, check_budget_s
                         "2-D 64^2..512^2, 3-D 32^3..128^3, F in {1,2,6}, DDI for F=6, 500-5000 steps, "
                         "half ground states (tol 1e-8) half real-time runs",
             "hbm_budget_gb": 150, "max_slots": 32, "peak_concurrent": srv.peak_active,
+            "admission": f"{policy}: by HBM footprint and slots, waiting units in order of estimated work "
+                         "(points x components x steps, x4 with DDI)",
             "merging": {"window_s": window, "merged_units": srv.merged_units,
                         "merged_requests": srv.merged_requests,
                         "rule": "ground states of one grid/F/dt/tol/trap (contact couplings) arriving in the same "

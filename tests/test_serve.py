@@ -164,3 +164,41 @@ def test_server_runs_merged_units_through_the_batch_runner(libsbec):
         assert res[rid].energy == 100.0 + rid and res[rid].admitted >= 0.05 - 1e-3
         assert res[rid].steps == reqs[rid].steps
     assert res[2].energy == 2.0  # the fake single runner
+
+
+@pytest.mark.parametrize("policy", ["fifo", "sjf"])
+def test_admission_policy_order(policy):
+    """One slot: after the first request, the queued ones are admitted in arrival order
+    (fifo) or by estimated work (sjf); every request is served either way."""
+    order, lock = [], threading.Lock()
+
+    def runner(req):
+        with lock:
+            order.append(req.rid)
+        time.sleep(0.03)
+        return dict(energy=0.0, norm=1.0, converged=True, steps=req.steps)
+
+    steps = [3000, 2500, 600, 4000, 500, 1000]
+    reqs = [serve.SolveRequest(i, "dynamics", (64, 64), (20.0, 20.0), 1, 10.0, 0.0, st, arrival=0.0)
+            for i, st in enumerate(steps)]
+    srv = serve.Server(hbm_budget_bytes=1e12, max_slots=1, runner=runner, policy=policy)
+    out = srv.run(reqs, realtime=False)
+    assert sorted(r.rid for r in out["results"]) == list(range(6))
+    rest = order[1:]  # the first admission races with the other threads' arrival in the queue
+    if policy == "fifo":
+        assert rest == sorted(rest), order
+    else:
+        assert rest == sorted(rest, key=lambda i: steps[i]), order
+    assert srv.peak_active == 1
+
+
+def test_work_estimate_orders_by_size_steps_and_ddi():
+    small = serve.SolveRequest(0, "dynamics", (64, 64), (20.0, 20.0), 1, 10.0, 0.0, 500)
+    longer = serve.SolveRequest(1, "dynamics", (64, 64), (20.0, 20.0), 1, 10.0, 0.0, 5000)
+    bigger = serve.SolveRequest(2, "dynamics", (256, 256), (20.0, 20.0), 1, 10.0, 0.0, 500)
+    f6 = serve.SolveRequest(3, "dynamics", (64, 64), (20.0, 20.0), 6, 10.0, 0.0, 500)
+    f6d = serve.SolveRequest(4, "dynamics", (64, 64), (20.0, 20.0), 6, 10.0, 0.0, 500, enable_ddi=True)
+    w = serve.work_estimate
+    assert w(small) < w(longer) and w(small) < w(bigger) and w(small) < w(f6) < w(f6d)
+    with pytest.raises(ValueError):
+        serve.Server(policy="lifo")
