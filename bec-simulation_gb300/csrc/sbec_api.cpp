@@ -1151,33 +1151,34 @@ sbec_status sbec_batch_create(const sbec_config* cfg, int32_t n_solves, const do
   SBEC_API_END
 }
 
-sbec_status sbec_batch_create_grids(const sbec_config* cfg, int32_t n_solves, const int32_t* n, const double* L,
-                                    const double* c0, const double* c1, const double* const* psi,
-                                    const double* const* V, sbec_batch** out) {
-  SBEC_API_BEGIN
+namespace {
+
+// Solves grouped by grid and spin F (first appearance order): one engine per group, all solves
+// of a group sharing its potential.  F = null: every solve has cfg->F.
+sbec_batch* batch_create_grouped(const sbec_config* cfg, int32_t n_solves, const int32_t* F, const int32_t* n,
+                                 const double* L, const double* c0, const double* c1, const double* const* psi,
+                                 const double* const* V) {
   need(cfg, "config");
   need(n, "n");
   need(L, "L");
   need(c0, "c0");
   need(c1, "c1");
   need(psi, "psi");
-  need(out, "out");
-  *out = nullptr;
   if (n_solves < 1) fail(SBEC_ERR_INVALID, "n_solves must be >= 1");
   check_batch_config(cfg);
-  // group the solves by grid (first appearance order); all solves of a grid share its potential
   std::vector<sbec_config> gcfg;
   std::vector<std::vector<int>> members;
   std::vector<int> grp(n_solves), loc(n_solves);
   for (int i = 0; i < n_solves; ++i) {
     sbec_config c = *cfg;
+    if (F) c.F = F[i];
     for (int d = 0; d < 3; ++d) {
       c.n[d] = d < cfg->ndim ? n[3 * i + d] : 1;
       c.L[d] = d < cfg->ndim ? L[3 * i + d] : 1.0;
     }
     int g = -1;
     for (size_t k = 0; k < gcfg.size(); ++k) {
-      bool same = true;
+      bool same = gcfg[k].F == c.F;
       for (int d = 0; d < cfg->ndim; ++d) same = same && gcfg[k].n[d] == c.n[d] && gcfg[k].L[d] == c.L[d];
       if (same) g = (int)k;
     }
@@ -1207,7 +1208,7 @@ sbec_status sbec_batch_create_grids(const sbec_config* cfg, int32_t n_solves, co
     const auto& m = members[g];
     long long N = 1;
     for (int d = 0; d < cfg->ndim; ++d) N *= gcfg[g].n[d];
-    const size_t per = (size_t)2 * N * (2 * cfg->F + 1);
+    const size_t per = (size_t)2 * N * (2 * gcfg[g].F + 1);
     std::vector<double> gc0, gc1, gpsi(per * m.size());
     for (size_t k = 0; k < m.size(); ++k) {
       gc0.push_back(c0[m[k]]);
@@ -1217,7 +1218,29 @@ sbec_status sbec_batch_create_grids(const sbec_config* cfg, int32_t n_solves, co
     b->groups.push_back(make_batch_group(gcfg[g], (int)m.size(), gc0.data(), gc1.data(), gpsi.data(),
                                          V ? V[m[0]] : nullptr));
   }
-  *out = b.release();
+  return b.release();
+}
+
+}  // namespace
+
+sbec_status sbec_batch_create_grids(const sbec_config* cfg, int32_t n_solves, const int32_t* n, const double* L,
+                                    const double* c0, const double* c1, const double* const* psi,
+                                    const double* const* V, sbec_batch** out) {
+  SBEC_API_BEGIN
+  need(out, "out");
+  *out = nullptr;
+  *out = batch_create_grouped(cfg, n_solves, nullptr, n, L, c0, c1, psi, V);
+  SBEC_API_END
+}
+
+sbec_status sbec_batch_create_mixed(const sbec_config* cfg, int32_t n_solves, const int32_t* F, const int32_t* n,
+                                    const double* L, const double* c0, const double* c1,
+                                    const double* const* psi, const double* const* V, sbec_batch** out) {
+  SBEC_API_BEGIN
+  need(out, "out");
+  need(F, "F");
+  *out = nullptr;
+  *out = batch_create_grouped(cfg, n_solves, F, n, L, c0, c1, psi, V);
   SBEC_API_END
 }
 

@@ -181,6 +181,9 @@ _PROTOS = {
     "sbec_batch_create": (C.c_int, [C.POINTER(sbec_config), C.c_int32, _D, _D, _D, _D, C.POINTER(_P)]),
     "sbec_batch_create_grids": (C.c_int, [C.POINTER(sbec_config), C.c_int32, C.POINTER(C.c_int32), _D, _D, _D,
                                           C.POINTER(_D), C.POINTER(_D), C.POINTER(_P)]),
+    "sbec_batch_create_mixed": (C.c_int, [C.POINTER(sbec_config), C.c_int32, C.POINTER(C.c_int32),
+                                          C.POINTER(C.c_int32), _D, _D, _D, C.POINTER(_D), C.POINTER(_D),
+                                          C.POINTER(_P)]),
     "sbec_batch_destroy": (C.c_int, [_P]),
     "sbec_batch_ground_state": (C.c_int, [_P, C.c_int64, C.c_double, C.c_int64, C.POINTER(sbec_gs_result)]),
     "sbec_batch_ground_state_each": (C.c_int, [_P, C.POINTER(C.c_int64), C.c_double, C.POINTER(C.c_int64),

@@ -723,15 +723,26 @@ class GroundStateBatch:
     the batch at the check where they converge.  ``grid`` puts every solve on one grid;
     ``grids`` gives one grid per solve (sbec_batch_create_grids: solves are grouped by grid
     and the groups advance concurrently), with ``potential`` evaluated on each grid.
+    ``atoms`` (one AtomSpecies per solve, with ``grids``) mixes spins: solves are grouped by
+    grid and F (sbec_batch_create_mixed).
     """
 
-    def __init__(self, *, grid: Optional[Grid] = None, atom: AtomSpecies, c0s, c1s, psi_inits, zeeman=None,
-                 potential=None, dt: float = 0.005, c_lhy: float = 0.0, precision: str = "fp32", grids=None):
+    def __init__(self, *, grid: Optional[Grid] = None, atom: Optional[AtomSpecies] = None, c0s, c1s, psi_inits,
+                 zeeman=None, potential=None, dt: float = 0.005, c_lhy: float = 0.0, precision: str = "fp32",
+                 grids=None, atoms=None):
         lib = load()
         if (grid is None) == (grids is None):
             raise _lib.ArgumentError("give either grid (one grid for every solve) or grids (one per solve)")
-        self.F, self.D = atom.F, 2 * atom.F + 1
+        if (atom is None) == (atoms is None):
+            raise _lib.ArgumentError("give either atom (one spin for every solve) or atoms (one per solve)")
+        if atoms is not None and grids is None:
+            raise _lib.ArgumentError("atoms (one spin per solve) goes with grids (one grid per solve)")
         self.n = len(psi_inits)
+        self.atoms = [atom] * self.n if atoms is None else list(atoms)
+        if len(self.atoms) != self.n:
+            raise _lib.ArgumentError("atoms and psi_inits must have the same length")
+        atom = self.atoms[0]
+        self.F, self.D = atom.F, 2 * atom.F + 1
         if len(c0s) != self.n or len(c1s) != self.n:
             raise _lib.ArgumentError("c0s, c1s and psi_inits must have the same length")
         self.grids = [grid] * self.n if grids is None else list(grids)
@@ -767,8 +778,14 @@ class GroundStateBatch:
                 if key not in Vs:
                     Vs[key] = np.ascontiguousarray(evaluate_potential(potential, g).ravel(order="F"))
                 V_p[i] = dptr(Vs[key])
-            check(lib.sbec_batch_create_grids(C.byref(cfg), self.n, n.ctypes.data_as(C.POINTER(C.c_int32)),
-                                              dptr(L), dptr(c0), dptr(c1), psi_p, V_p, C.byref(h)))
+            if atoms is None:
+                check(lib.sbec_batch_create_grids(C.byref(cfg), self.n, n.ctypes.data_as(C.POINTER(C.c_int32)),
+                                                  dptr(L), dptr(c0), dptr(c1), psi_p, V_p, C.byref(h)))
+            else:
+                Fs = np.ascontiguousarray([a.F for a in self.atoms], dtype=np.int32)
+                check(lib.sbec_batch_create_mixed(C.byref(cfg), self.n, Fs.ctypes.data_as(C.POINTER(C.c_int32)),
+                                                  n.ctypes.data_as(C.POINTER(C.c_int32)), dptr(L), dptr(c0),
+                                                  dptr(c1), psi_p, V_p, C.byref(h)))
         self._h = h
         self._lib = lib
 
@@ -806,10 +823,11 @@ class GroundStateBatch:
 
     def psi(self, i: int) -> np.ndarray:
         g = self.grids[int(i)]
-        n = int(np.prod(g.config.n_points)) * self.D
+        D = 2 * self.atoms[int(i)].F + 1
+        n = int(np.prod(g.config.n_points)) * D
         buf = np.empty(2 * n)
         check(self._lib.sbec_batch_get_psi(self._h, int(i), dptr(buf)))
-        return from_interleaved(buf, g.config.n_points, self.D)
+        return from_interleaved(buf, g.config.n_points, D)
 
     def energies(self) -> np.ndarray:
         E = np.empty(self.n)

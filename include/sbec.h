@@ -257,6 +257,12 @@ sbec_status sbec_batch_create_grids(const sbec_config* cfg, int32_t n_solves, co
  * Raman, losses or the nematic term; grids that take the fused passes: power-of-two axes,
  * D in {1, 3, 5} and a row pass that fits the first axis), else 0.  Needs no device. */
 sbec_status sbec_batch_supported(const sbec_config* cfg, int32_t* supported);
+/* The same with a spin F per solve (F[i]; cfg->F is ignored): solves are grouped by grid and F,
+ * and psi[i] holds 2F[i]+1 components.  No counterpart in the reference, whose callers loop
+ * over the solves one at a time. */
+sbec_status sbec_batch_create_mixed(const sbec_config* cfg, int32_t n_solves, const int32_t* F, const int32_t* n,
+                                    const double* L, const double* c0, const double* c1,
+                                    const double* const* psi, const double* const* V, sbec_batch** out);
 sbec_status sbec_batch_destroy(sbec_batch* b);
 sbec_status sbec_batch_ground_state(sbec_batch* b, int64_t n_steps, double tol, int64_t check_every,
                                     sbec_gs_result* out);

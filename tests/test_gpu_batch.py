@@ -118,6 +118,46 @@ def test_batch_on_mixed_grids_matches_per_grid_batches(gpu):
         assert rel_psi_err(pm[i], ro["workspace"].psi) < PSI_TOL_FP64
 
 
+def test_batch_of_mixed_spins_matches_per_spin_batches(gpu):
+    """One batch object over spin-1 and spin-2 solves on two grids (sbec_batch_create_mixed:
+    grouped by grid and F) gives each solve the result of a batch of its own grid and F, and
+    the spin-2 results match the oracle's find_ground_state."""
+    F2 = S.AtomSpecies("87Rb-F2", 2)
+    sizes = [32, 32, 16, 32, 16]
+    Fs = [1, 2, 2, 1, 1]
+    grids_o = {n: O.make_grid(O.GridConfig((n, n), (16.0, 16.0))) for n in set(sizes)}
+    grids_s = {n: S.make_grid(S.GridConfig((n, n), (16.0, 16.0))) for n in set(sizes)}
+    states = ["polar", "ferromagnetic", "random", "random", "uniform"]
+    c1s = [-0.5, 0.3, 0.1, -0.2, 0.6]
+    psis = [O.init_psi(grids_o[n], F, st, seed=60 + i) for i, (n, F, st) in enumerate(zip(sizes, Fs, states))]
+    kw = dict(zeeman=S.ZeemanParams(0.1, 0.05), potential=S.HarmonicTrap(1.0, 1.0), dt=0.005, precision="fp64")
+    atoms = [S.Rb87 if F == 1 else F2 for F in Fs]
+    mixed = S.GroundStateBatch(grids=[grids_s[n] for n in sizes], atoms=atoms, c0s=[10.0] * 5, c1s=c1s,
+                               psi_inits=psis, **kw)
+    rm = mixed.ground_state(150, 1e-9)
+    pm = [mixed.psi(i) for i in range(5)]
+    mixed.close()
+    assert [p.shape[-1] for p in pm] == [2 * F + 1 for F in Fs]
+    for key in set(zip(sizes, Fs)):
+        idx = [i for i in range(5) if (sizes[i], Fs[i]) == key]
+        b = S.GroundStateBatch(grid=grids_s[key[0]], atom=atoms[idx[0]], c0s=[10.0] * len(idx),
+                               c1s=[c1s[i] for i in idx], psi_inits=[psis[i] for i in idx], **kw)
+        rb = b.ground_state(150, 1e-9)
+        for k, i in enumerate(idx):
+            assert rb[k] == rm[i]
+            assert np.array_equal(b.psi(k), pm[i])
+        b.close()
+    for i in (1, 2):
+        n = sizes[i]
+        ro = O.find_ground_state(grid=grids_o[n], atom=O.AtomSpecies("87Rb-F2", 2),
+                                 interactions=O.InteractionParams(10.0, c1s[i]), zeeman=O.ZeemanParams(0.1, 0.05),
+                                 V=O.harmonic_potential(grids_o[n], (1.0, 1.0)), psi_init=psis[i], dt=0.005,
+                                 n_steps=150, tol=1e-9)
+        assert rm[i]["steps"] == ro["steps"] and rm[i]["converged"] == ro["converged"]
+        assert abs(rm[i]["energy"] - ro["energy"]) <= ENERGY_TOL_FP64 * 10 * abs(ro["energy"])
+        assert rel_psi_err(pm[i], ro["workspace"].psi) < PSI_TOL_FP64
+
+
 def test_batch_spin2_fp64_against_oracle(gpu):
     """Spin-2 solves (five components, spin mixing by the Euler rotation) in one batch."""
     og = O.make_grid(O.GridConfig((32, 32), (16.0, 16.0)))
