@@ -695,6 +695,56 @@ def scan_continuation(*, param_values, make_interactions: Callable, grid, atom, 
     return results
 
 
+def find_phase_boundary(*, param_range, make_interactions: Callable, grid, atom, tol: float = 0.01,
+                        max_bisections: int = 20, batched=None, **kw) -> dict:
+    """``find_phase_boundary`` (src/phase_boundary.jl:9-60): bisection on the phase label
+    (``classify_phase`` on the device) of ``find_ground_state`` at each probe.  The two
+    endpoint solves are independent and run as one GroundStateBatch when eligible (contact
+    couplings, plain ITP loop; batched=None decides, True/False forces), with
+    find_ground_state's loop, check interval and initial state per solve; the bisection
+    probes depend on each other and run one at a time."""
+    def classify_at(val):
+        r = find_ground_state(grid=grid, atom=atom, interactions=make_interactions(val), **kw)
+        ws = r["workspace"]
+        phase = classify_phase(ws)["phase"]
+        ws.close()
+        return phase
+
+    a, b = param_range
+    ia, ib = make_interactions(a), make_interactions(b)
+    use_batch = (_batch_eligible(atom, ia, kw) and _batch_eligible(atom, ib, kw) and ia.c_lhy == ib.c_lhy
+                 if batched is None else bool(batched))
+    if use_batch:
+        dt = kw.get("dt", 0.001)
+        zeeman = ZeemanParams() if kw.get("zeeman") is None else kw["zeeman"]
+        p0 = init_psi(grid, atom.F, kw.get("initial_state", "polar"))
+        for inter in (ia, ib):
+            _validate_itp(zeeman, inter, atom.F, dt, p0, 0.0)
+        bt = GroundStateBatch(grid=grid, atom=atom, c0s=[ia.c0, ib.c0], c1s=[ia.c1, ib.c1], psi_inits=[p0, p0],
+                              zeeman=zeeman, potential=kw.get("potential"), dt=dt, c_lhy=ia.c_lhy,
+                              precision=kw.get("precision", "fp64"))
+        bt.ground_state(kw.get("n_steps", 10000), kw.get("tol", 1e-10))
+        phase_a, phase_b = bt.classify_phase(0)["phase"], bt.classify_phase(1)["phase"]
+        bt.close()
+    else:
+        phase_a, phase_b = classify_at(a), classify_at(b)
+    n_eval = 2
+    if phase_a == phase_b:
+        return dict(boundary_value=(a + b) / 2, phase_left=phase_a, phase_right=phase_b, n_evaluations=n_eval)
+    for _ in range(max_bisections):
+        if abs(b - a) < tol:
+            break
+        mid = (a + b) / 2
+        phase_mid = classify_at(mid)
+        n_eval += 1
+        if phase_mid == phase_a:
+            a = mid
+        else:
+            b = mid
+            phase_b = phase_mid
+    return dict(boundary_value=(a + b) / 2, phase_left=phase_a, phase_right=phase_b, n_evaluations=n_eval)
+
+
 def _config(grid: Grid, F: int, zeeman, sim_params: SimParams, precision: str, interactions=None) -> _lib.sbec_config:
     cfg = _lib.sbec_config()
     cfg.ndim = grid.config.ndim

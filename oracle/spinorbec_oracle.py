@@ -1966,6 +1966,34 @@ def scan_continuation(*, param_values, make_interactions: Callable, grid, atom, 
 # Host-buffer helpers (the C-ABI layout: interleaved re/im, x fastest)
 # ----------------------------------------------------------------------------
 
+
+def find_phase_boundary(*, param_range, make_interactions: Callable, grid, atom, tol: float = 0.01,
+                        max_bisections: int = 20, **kw) -> dict:
+    """``find_phase_boundary`` (src/phase_boundary.jl:9-60): bisection on the ``classify_phase``
+    label of ``find_ground_state`` at each probe; the interval keeps the left endpoint's phase
+    on its left (a midpoint of that phase moves a, any other moves b and its phase)."""
+    def classify_at(val):
+        r = find_ground_state(grid=grid, atom=atom, interactions=make_interactions(val), **kw)
+        return classify_phase(r["workspace"].psi, atom.F, grid)["phase"]
+
+    a, b = param_range
+    phase_a, phase_b = classify_at(a), classify_at(b)
+    n_eval = 2
+    if phase_a == phase_b:
+        return dict(boundary_value=(a + b) / 2, phase_left=phase_a, phase_right=phase_b, n_evaluations=n_eval)
+    for _ in range(max_bisections):
+        if abs(b - a) < tol:
+            break
+        mid = (a + b) / 2
+        phase_mid = classify_at(mid)
+        n_eval += 1
+        if phase_mid == phase_a:
+            a = mid
+        else:
+            b = mid
+            phase_b = phase_mid
+    return dict(boundary_value=(a + b) / 2, phase_left=phase_a, phase_right=phase_b, n_evaluations=n_eval)
+
 def psi_to_interleaved(psi: np.ndarray) -> np.ndarray:
     flat = np.ascontiguousarray(psi.ravel(order="F"))
     return flat.view(np.float64)

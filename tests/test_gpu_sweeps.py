@@ -6,7 +6,8 @@
   multistart fallback (:357-360), each point labelled by classify_phase (:363);
 * the adaptive-dt ground state (src/ground_state.jl:172-237) with the same dt decisions;
 * the ITP NaN guard (src/ground_state.jl:4-29, :142, :193) on a NaN planted in the host psi
-  before upload, for the fixed-dt and the adaptive loop.
+  before upload, for the fixed-dt and the adaptive loop;
+* find_phase_boundary (src/phase_boundary.jl:9-60): bisection on the device phase labels.
 """
 
 import numpy as np
@@ -75,6 +76,21 @@ def test_scan_continuation_with_multistart_fallback(gpu):
         assert a["converged"] == b["converged"]
         assert abs(a["energy"] - b["energy"]) <= ENERGY_TOL_FP64 * 10 * abs(b["energy"])
         assert rel_psi_err(a["psi"], b["psi"]) < PSI_TOL_FP64
+
+
+@pytest.mark.parametrize("batched", [None, False])
+def test_find_phase_boundary(gpu, batched):
+    """find_phase_boundary (src/phase_boundary.jl:9-60) on the device: the same probes, phases,
+    evaluation count and boundary as the oracle; the endpoint solves as one batch (default) or
+    one at a time."""
+    og = O.make_grid(O.GridConfig((32,), (16.0,)))
+    hg = S.make_grid(S.GridConfig((32,), (16.0,)))
+    kw = dict(tol=0.05, max_bisections=10, dt=0.01, n_steps=600, initial_state="uniform")
+    ro = O.find_phase_boundary(param_range=(-0.7, 0.4), make_interactions=lambda v: O.InteractionParams(10.0, v),
+                               grid=og, atom=O.Rb87, V=O.harmonic_potential(og, (1.0,)), **kw)
+    rg = S.find_phase_boundary(param_range=(-0.7, 0.4), make_interactions=lambda v: S.InteractionParams(10.0, v),
+                               grid=hg, atom=S.Rb87, potential=S.HarmonicTrap(1.0), batched=batched, **kw)
+    assert rg == ro
 
 
 def test_adaptive_ground_state(gpu):

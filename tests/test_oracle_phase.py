@@ -1,8 +1,9 @@
 """Pins of the oracle's phase diagnostics and ground-state sweeps to the reference's own tests:
 ``classify_phase`` (test/test_diagnostics.jl:250-280), ``pair_amplitude_spectrum``
-(test/test_observables.jl:80-125), ``scan_continuation`` (test/test_continuation.jl) and the
-adaptive-dt ground state (test/test_adaptive_dt.jl:6-24), plus the step-1 NaN guard of
-``_find_ground_state_adaptive`` (src/ground_state.jl:193)."""
+(test/test_observables.jl:80-125), ``scan_continuation`` (test/test_continuation.jl),
+``find_phase_boundary`` (test/test_phase_boundary.jl) and the adaptive-dt ground state
+(test/test_adaptive_dt.jl:6-24), plus the step-1 NaN guard of ``_find_ground_state_adaptive``
+(src/ground_state.jl:193)."""
 
 import math
 
@@ -112,3 +113,42 @@ def test_adaptive_ground_state_nan_guard_at_step_1():  # src/ground_state.jl:193
     with pytest.raises(ValueError, match="NaN detected in ITP at step 1"):
         O.find_ground_state(grid=g, atom=O.Rb87, interactions=O.InteractionParams(10.0, -0.5), psi_init=psi,
                             dt=0.005, n_steps=200, tol=1e-8, adaptive_dt=True)
+
+
+# ---- find_phase_boundary (src/phase_boundary.jl:9-60), ported from test/test_phase_boundary.jl
+
+def _pb_kw():
+    return dict(grid=O.make_grid(O.GridConfig((16,), (10.0,))), atom=O.Rb87, dt=0.01, n_steps=500,
+                make_interactions=lambda v: O.InteractionParams(10.0, v))
+
+
+def test_phase_boundary_returns_valid_result():
+    r = O.find_phase_boundary(param_range=(-10.0, 10.0), tol=1.0, max_bisections=5, **_pb_kw())
+    assert set(r) == {"boundary_value", "phase_left", "phase_right", "n_evaluations"}
+    assert r["n_evaluations"] >= 2
+    assert -10.0 <= r["boundary_value"] <= 10.0
+
+
+def test_phase_boundary_same_phase_returns_midpoint():
+    r = O.find_phase_boundary(param_range=(-10.0, -5.0), tol=0.1, max_bisections=3, **_pb_kw())
+    assert r["n_evaluations"] == 2
+    assert r["phase_left"] == r["phase_right"]
+    assert r["boundary_value"] == -7.5
+
+
+def test_phase_boundary_bisection_narrows_interval():
+    r1 = O.find_phase_boundary(param_range=(-20.0, 20.0), tol=5.0, max_bisections=3, **_pb_kw())
+    r2 = O.find_phase_boundary(param_range=(-20.0, 20.0), tol=2.0, max_bisections=10, **_pb_kw())
+    assert r2["n_evaluations"] >= r1["n_evaluations"]
+
+
+def test_phase_boundary_bisects_a_ferromagnetic_edge():
+    """From the 'uniform' start the spin-mixing step selects the phase: ferromagnetic for c1 < 0,
+    another phase for c1 > 0; the bisection keeps the ferromagnetic left end and closes on 0."""
+    g = O.make_grid(O.GridConfig((32,), (16.0,)))
+    r = O.find_phase_boundary(param_range=(-0.7, 0.4), make_interactions=lambda v: O.InteractionParams(10.0, v),
+                              grid=g, atom=O.Rb87, tol=0.05, max_bisections=10, V=O.harmonic_potential(g, (1.0,)),
+                              dt=0.01, n_steps=600, initial_state="uniform")
+    assert r["phase_left"] == "ferromagnetic" and r["phase_right"] != "ferromagnetic"
+    assert r["n_evaluations"] == 2 + 5  # 1.1 halved five times is below 0.05
+    assert -0.2 < r["boundary_value"] < 0.2
