@@ -985,6 +985,79 @@ sbec_status sbec_energy_breakdown(sbec_ws* ws, sbec_energy_terms* out) {
   SBEC_API_END
 }
 
+// estimate_splitting_error (src/diagnostics.jl:214-251): one split step of dt against two of
+// dt/2 (kinetic phase and potential steps at dt/2) from the same state; returns
+// max|psi_1 - psi_2| / max|psi|.  psi, t and step are restored (the saved psi stays on the
+// device, slot A).
+sbec_status sbec_estimate_splitting_error(sbec_ws* ws, double* err) {
+  SBEC_API_BEGIN
+  need(err, "err");
+  EngineBase& e = E(ws);
+  const double t0 = e.t, dt = e.dt, kdt = ws->kin_dt;
+  const long long s0 = e.step;
+  const bool kit = ws->kin_itp;
+  e.copy_slot(kSlotA, kPsi);
+  split_steps(ws, 1);
+  e.copy_slot(kSlotB, kPsi);
+  e.copy_slot(kPsi, kSlotA);
+  e.t = t0;
+  e.step = s0;
+  e.dt = dt / 2;
+  ws->kin_dt = dt / 2;
+  ws->kin_itp = e.itp;
+  try {
+    split_steps(ws, 2);
+  } catch (...) {
+    e.dt = dt;
+    ws->kin_dt = kdt;
+    ws->kin_itp = kit;
+    throw;
+  }
+  e.dt = dt;
+  ws->kin_dt = kdt;
+  ws->kin_itp = kit;
+  double p1, d1, p0, d0;
+  e.max_abs(kPsi, kSlotB, &p1, &d1);  // max |psi_half - psi_full|
+  e.max_abs(kSlotA, kSlotA, &p0, &d0);  // max |psi| of the saved state
+  e.copy_slot(kPsi, kSlotA);
+  e.t = t0;
+  e.step = s0;
+  *err = d1 / p0;
+  SBEC_API_END
+}
+
+// validate_conservation's measurement (src/diagnostics.jl:259-293): the relative drifts of the
+// norm, the energy and Mz over n split steps (Mz relative to max(|Mz0|, 1e-10)); psi, t and step
+// are restored.  The tolerance test stays with the caller.
+sbec_status sbec_conservation_drift(sbec_ws* ws, int64_t n_steps, double* norm_drift, double* energy_drift,
+                                    double* mag_drift) {
+  SBEC_API_BEGIN
+  need(norm_drift, "norm_drift");
+  need(energy_drift, "energy_drift");
+  need(mag_drift, "mag_drift");
+  if (n_steps < 0) fail(SBEC_ERR_INVALID, "n_steps must be non-negative");
+  EngineBase& e = E(ws);
+  const double t0 = e.t;
+  const long long s0 = e.step;
+  e.copy_slot(kSlotA, kPsi);
+  double N0, M0, N1, M1;
+  norm_and_mz(e, &N0, &M0);
+  zee(ws);
+  const double E0 = total_energy(e);
+  split_steps(ws, n_steps);
+  norm_and_mz(e, &N1, &M1);
+  zee(ws);
+  const double E1 = total_energy(e);
+  e.copy_slot(kPsi, kSlotA);
+  e.t = t0;
+  e.step = s0;
+  zee(ws);
+  *norm_drift = std::fabs(N1 - N0) / std::max(N0, 1e-30);
+  *energy_drift = std::fabs(E1 - E0) / std::max(std::fabs(E0), 1e-30);
+  *mag_drift = std::fabs(M1 - M0) / std::max(std::fabs(M0), 1e-10);
+  SBEC_API_END
+}
+
 sbec_status sbec_total_norm(sbec_ws* ws, double* norm) {
   SBEC_API_BEGIN
   need(norm, "norm");

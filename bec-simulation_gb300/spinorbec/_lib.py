@@ -177,6 +177,8 @@ _PROTOS = {
     "sbec_batch_tuning_report": (C.c_int, [_P, C.c_char_p, C.c_int64, C.POINTER(C.c_int64)]),
     "sbec_tune_table_export": (C.c_int, [C.c_char_p, C.c_int64, C.POINTER(C.c_int64)]),
     "sbec_tune_freeze": (C.c_int, [C.c_int32]),
+    "sbec_estimate_splitting_error": (C.c_int, [_P, _D]),
+    "sbec_conservation_drift": (C.c_int, [_P, C.c_int64, _D, _D, _D]),
     "sbec_tune_table_import": (C.c_int, [C.c_char_p]),
     "sbec_batch_create": (C.c_int, [C.POINTER(sbec_config), C.c_int32, _D, _D, _D, _D, C.POINTER(_P)]),
     "sbec_batch_create_grids": (C.c_int, [C.POINTER(sbec_config), C.c_int32, C.POINTER(C.c_int32), _D, _D, _D,

@@ -695,6 +695,26 @@ def scan_continuation(*, param_values, make_interactions: Callable, grid, atom, 
     return results
 
 
+def estimate_splitting_error(ws: Workspace) -> float:
+    """``estimate_splitting_error`` (src/diagnostics.jl:214-251): one split step of dt against
+    two of dt/2 from the current state (restored afterwards, the saved copy on the device);
+    max|psi_1 - psi_2| / max|psi|."""
+    err = C.c_double()
+    check(ws._lib.sbec_estimate_splitting_error(ws.handle, C.byref(err)))
+    return err.value
+
+
+def validate_conservation(ws: Workspace, *, n_steps: int = 100, tol_norm: float = 1e-12, tol_energy: float = 1e-3,
+                          tol_magnetization: float = 1e-6) -> dict:
+    """``validate_conservation`` (src/diagnostics.jl:259-293): the drifts of N, E and Mz over
+    n_steps split steps on the device (the state restored), passed when all are below their
+    tolerances."""
+    nd, ed, md = C.c_double(), C.c_double(), C.c_double()
+    check(ws._lib.sbec_conservation_drift(ws.handle, int(n_steps), C.byref(nd), C.byref(ed), C.byref(md)))
+    return dict(passed=nd.value < tol_norm and ed.value < tol_energy and md.value < tol_magnetization,
+                norm_drift=nd.value, energy_drift=ed.value, magnetization_drift=md.value)
+
+
 def find_phase_boundary(*, param_range, make_interactions: Callable, grid, atom, tol: float = 0.01,
                         max_bisections: int = 20, batched=None, **kw) -> dict:
     """``find_phase_boundary`` (src/phase_boundary.jl:9-60): bisection on the phase label

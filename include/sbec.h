@@ -204,6 +204,13 @@ sbec_status sbec_ground_state_adaptive(sbec_ws* ws, int64_t n_steps, double tol,
 sbec_status sbec_total_energy(sbec_ws* ws, double* E);
 sbec_status sbec_energy_breakdown(sbec_ws* ws, sbec_energy_terms* out);
 /* total_norm, magnetization (src/observables.jl:13-31). */
+/* estimate_splitting_error (src/diagnostics.jl:214-251): max|psi_dt - psi_{2 x dt/2}| / max|psi|
+ * from the current state, which is restored. */
+sbec_status sbec_estimate_splitting_error(sbec_ws* ws, double* err);
+/* validate_conservation's drifts (src/diagnostics.jl:259-293) over n_steps split steps: |dN|/N,
+ * |dE|/|E|, |dMz|/max(|Mz|, 1e-10); the state is restored. */
+sbec_status sbec_conservation_drift(sbec_ws* ws, int64_t n_steps, double* norm_drift, double* energy_drift,
+                                    double* mag_drift);
 sbec_status sbec_total_norm(sbec_ws* ws, double* norm);
 sbec_status sbec_magnetization(sbec_ws* ws, double* Mz);
 /* Spin density (Fx, Fy, Fz) on the grid (src/observables.jl:61-86); 3*n_total doubles. */

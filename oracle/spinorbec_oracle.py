@@ -1967,6 +1967,49 @@ def scan_continuation(*, param_values, make_interactions: Callable, grid, atom, 
 # ----------------------------------------------------------------------------
 
 
+
+def estimate_splitting_error(ws: Workspace) -> float:
+    """``estimate_splitting_error`` (src/diagnostics.jl:214-251): one split step of dt against
+    two of dt/2 (kinetic phase prepared for dt/2) from the same state, max|psi_1 - psi_2| /
+    max|psi|; psi, t and step restored."""
+    psi_save, t_save, step_save = ws.psi.copy(), ws.t, ws.step
+    kin_save, sp = ws.kinetic_phase, ws.sim_params
+    psi_norm = float(np.abs(psi_save).max())
+    split_step(ws)
+    psi_full = ws.psi.copy()
+    ws.psi[...] = psi_save
+    ws.t, ws.step = t_save, step_save
+    dt_half = sp.dt / 2
+    ws.kinetic_phase = prepare_kinetic_phase(ws.grid, dt_half, sp.imaginary_time)
+    ws.sim_params = SimParams(dt_half, sp.n_steps, sp.imaginary_time, sp.normalize_every, sp.save_every)
+    try:
+        split_step(ws)
+        split_step(ws)
+        psi_half = ws.psi.copy()
+    finally:
+        ws.kinetic_phase, ws.sim_params = kin_save, sp
+    ws.psi[...] = psi_save
+    ws.t, ws.step = t_save, step_save
+    return float(np.abs(psi_full - psi_half).max()) / psi_norm
+
+
+def validate_conservation(ws: Workspace, *, n_steps: int = 100, tol_norm: float = 1e-12, tol_energy: float = 1e-3,
+                          tol_magnetization: float = 1e-6) -> dict:
+    """``validate_conservation`` (src/diagnostics.jl:259-293): drifts of N, E and Mz over
+    n_steps split steps (the state restored), passed when all are below their tolerances."""
+    psi_save, t_save, step_save = ws.psi.copy(), ws.t, ws.step
+    N0, E0, M0 = total_norm(ws.psi, ws.grid), total_energy(ws), magnetization(ws.psi, ws.grid, ws.F)
+    for _ in range(n_steps):
+        split_step(ws)
+    N1, E1, M1 = total_norm(ws.psi, ws.grid), total_energy(ws), magnetization(ws.psi, ws.grid, ws.F)
+    ws.psi[...] = psi_save
+    ws.t, ws.step = t_save, step_save
+    nd = abs(N1 - N0) / max(N0, 1e-30)
+    ed = abs(E1 - E0) / max(abs(E0), 1e-30)
+    md = abs(M1 - M0) / max(abs(M0), 1e-10)
+    return dict(passed=nd < tol_norm and ed < tol_energy and md < tol_magnetization, norm_drift=nd,
+                energy_drift=ed, magnetization_drift=md)
+
 def find_phase_boundary(*, param_range, make_interactions: Callable, grid, atom, tol: float = 0.01,
                         max_bisections: int = 20, **kw) -> dict:
     """``find_phase_boundary`` (src/phase_boundary.jl:9-60): bisection on the ``classify_phase``
