@@ -111,6 +111,7 @@ class Engine final : public EngineBase {
     if (const char* m = std::getenv("SBEC_BATCH_MERGED")) merged_itp_ = std::atoi(m) != 0;
     if (const char* t = std::getenv("SBEC_TENSOR_LANES")) tensor_mode_ = std::atoi(t);
     if (const char* g = std::getenv("SBEC_SEGMENT")) segment_on_ = std::atoi(g) != 0;
+    if (const char* g = std::getenv("SBEC_ITP_STEPS")) use_itp_steps_ = std::atoi(g) != 0;
     // host-side fault injection for the tests: the segment barrier's arrival counter starts
     // beyond the block count, so no block is ever the last arriver and every wait runs out
     if (const char* f = std::getenv("SBEC_FAULT_SEGMENT_STALL")) segment_stall_ = std::atoi(f) != 0;
@@ -749,6 +750,20 @@ class Engine final : public EngineBase {
     if (n <= 0) return;
     const int flags = (kin_itp ? 1 : 0) | (it ? 2 : 0) | (normalize ? 4 : 0);
     bool pending = false;
+    if (s_.ndim == 1 && it && normalize && s_.n[0] >= 32 && s_.n[0] <= kItpStepsMaxLine && use_itp_steps_) {
+      // one launch for all n steps (k_row_itp_steps): the 1-D solve is one row-pass block
+      RowArgs<R> a = row_args(false);
+      a.p1 = pot_full(dtv / 2, it);
+      a.p2 = pot_full(dtv / 2, it);
+      a.flags |= RP_POT1 | RP_KIN_X | RP_POT2 | RP_NORM;
+      const LineCtx<R> c = line_ctx();
+      const Tw<R> tw = twiddle(s_.n[0]);
+      pb();
+      row_itp_steps<R>(c, tw, s_.n[0], s_.D, a, n, 0, results_ + 40);
+      done("row_pass", (double)n * (2.0 * (double)sizeof(cplx<R>) * nc_ + (double)sizeof(R) * N_));
+      pending = true;
+      n = 0;
+    }
     for (long long done_steps = 0; done_steps < n;) {
       const long long m = std::min(kGraphChunk, n - done_steps);
       const GraphKey key{2, m, dtv, kin_dt, zeeman_p, zeeman_q, flags | (pending ? 8 : 0)};
@@ -2208,6 +2223,8 @@ class Engine final : public EngineBase {
   // (one row of h per lane), 2 rows of h in registers ((D + 1) / 2 warps per 32 points), 3 a
   // lane group with two rows per lane; -1 (default) by D
   int tensor_mode_ = -1;
+  // 1-D fused ITP steps in one launch (k_row_itp_steps); SBEC_ITP_STEPS=0: one launch per step
+  bool use_itp_steps_ = true;
   float* G32_ = nullptr;
   R* bcorr_ = nullptr;  // merged FP32 batched ITP: per-solve correction, prediction, ones
   R* bpred_ = nullptr;

@@ -1327,6 +1327,28 @@ k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
   row_pass_block<R, N, D, RPB, P, PP, false>(a, st, ph, tw, (int)blockIdx.x, smem_raw, true);
 }
 
+// n fused ITP split steps of a 1-D solve (one row-pass block holds its whole line of all
+// components) in one launch: each iteration is the row pass of fused_steps_body (V/2, kinetic,
+// V/2, norm partial), the block's partial is the solve's norm (what the one-block finish of
+// the separate launches writes), and the next iteration scales by it.  The state is
+// bit-identical to the launch-per-step sequence; the last step's renormalisation is left
+// pending in norm_out, as there.
+template <typename R, int N, int D, int RPB, int P = 0, bool PP = false>
+__global__ void __launch_bounds__(row_threads<R, N, D, RPB, P>())
+k_row_itp_steps(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw, long long n_steps, int first_pending,
+                double* norm_out) {
+  pdl_wait();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int base = a.flags;
+  for (long long step = 0; step < n_steps; ++step) {
+    a.flags = base | ((step > 0 || first_pending) ? RP_SCALE : 0);
+    row_pass_block<R, N, D, RPB, P, PP, false>(a, st, ph, tw, 0, smem_raw, false);
+    __syncthreads();  // psi stores and the partial are visible to the whole block
+    if (threadIdx.x == 0) norm_out[0] = a.partials[0];
+    __syncthreads();
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Persistent leapfrog segment (src/simulation.jl:49-94, the merged steps between save
 // points) for 2-D grids: one cooperative launch runs n steps, each the kinetic column

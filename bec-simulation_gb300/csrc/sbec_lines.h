@@ -43,6 +43,13 @@ struct LineKernels {
   static void row(const LineCtx<R>& c, const Tw<R>& tw, int n, int D, const RowArgs<R>& a, int blocks);
 };
 
+// n fused ITP split steps of a 1-D solve in one launch (k_row_itp_steps, plan variant 0;
+// sbec_itp_steps.cu): lines of 32-1024 points, D in {1, 3, 5}.
+constexpr int kItpStepsMaxLine = 1024;
+template <typename R>
+void row_itp_steps(const LineCtx<R>& c, const Tw<R>& tw, int n, int D, const RowArgs<R>& a, long long n_steps,
+                   int first_pending, double* norm_out);
+
 // Persistent 2-D leapfrog segments (sbec_segment_f32.cu, kernel k_lf_segment): FP32,
 // square grids of 64-512 points per side, D in {1, 3}.  One cooperative launch runs
 // n_steps merged leapfrog steps of the default plan.
