@@ -25,7 +25,8 @@ LIB = LIB_DIR / "libsbec.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["sbec_engine_f64.cu", "sbec_engine_f32.cu", "sbec_lines_f64.cu", "sbec_lines_f32_v0.cu",
               "sbec_lines_f32_v1.cu", "sbec_lines_f32_v2.cu", "sbec_lines_f32_v3.cu", "sbec_lines_f32_v4.cu",
-              "sbec_lines_f32_v5.cu", "sbec_lines_f32_v6.cu", "sbec_lines_f32_v7.cu", "sbec_segment_f32.cu",
+              "sbec_lines_f32_v5.cu", "sbec_lines_f32_v6.cu", "sbec_lines_f32_v7.cu", "sbec_rows_f32_v12.cu",
+              "sbec_rows_f32_v13.cu", "sbec_rows_f32_v14.cu", "sbec_rows_f32_v15.cu", "sbec_segment_f32.cu",
               "sbec_noalloc.cu", "sbec_peaks.cu", "sbec_itp_steps_f32.cu", "sbec_itp_steps_f64.cu"]
 CPP_SOURCES = ["sbec_setup.cpp", "sbec_api.cpp"]
 

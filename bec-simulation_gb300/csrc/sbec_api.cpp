@@ -1101,10 +1101,11 @@ namespace {
 void check_batch_config(const sbec_config* cfg) {
   if (!cfg->imaginary_time || cfg->normalize_every != 1)
     fail(SBEC_ERR_INVALID, "batched ground states need imaginary_time=1 and normalize_every=1");
-  if (cfg->n_c_extra != 0 || cfg->gS_direct || cfg->enable_ddi || cfg->raman ||
-      !(cfg->loss_gamma_dr < 1e-30 && cfg->loss_L3 < 1e-30))
+  if (cfg->gS_direct || cfg->enable_ddi || cfg->raman || !(cfg->loss_gamma_dr < 1e-30 && cfg->loss_L3 < 1e-30))
     fail(SBEC_ERR_UNSUPPORTED,
-         "batched ground states support contact c0/c1 (+LHY) couplings without DDI, Raman or losses");
+         "batched ground states support contact c0/c1 (+LHY, nematic c2) couplings without DDI, Raman or losses");
+  // c_extra may carry the nematic c2 (shared by every solve); couplings that switch on the
+  // tensor step (an even c_k, k >= 4) are refused by the group's engine (no fused path)
 }
 
 std::unique_ptr<EngineBase> make_batch_group(const sbec_config& cfg, int n, const double* c0, const double* c1,
@@ -1323,8 +1324,8 @@ sbec_status sbec_batch_supported(const sbec_config* cfg, int32_t* supported) {
   need(supported, "supported");
   *supported = 0;
   const Setup s = build_setup(*cfg);  // argument errors are errors
-  const bool contact = cfg->n_c_extra == 0 && !cfg->gS_direct && !cfg->enable_ddi && !cfg->raman &&
-                       cfg->loss_gamma_dr < 1e-30 && cfg->loss_L3 < 1e-30 && std::fabs(s.c2) <= 1e-30;
+  const bool contact = !s.tensor && !cfg->gS_direct && !cfg->enable_ddi && !cfg->raman &&
+                       cfg->loss_gamma_dr < 1e-30 && cfg->loss_L3 < 1e-30;
   *supported = cfg->imaginary_time && cfg->normalize_every == 1 && contact &&
                fused_path_supported(s, cfg->precision == SBEC_FP32_BULK);
   SBEC_API_END

@@ -917,7 +917,6 @@ class Engine final : public EngineBase {
 
   void batch_init(int n, const double* c0, const double* c1, const double* psi_all) override {
     if (!fused_path()) fail(SBEC_ERR_UNSUPPORTED, "batched solves need the fused path (no DDI / tensor, D in {1,3,5})");
-    if (nematic()) fail(SBEC_ERR_UNSUPPORTED, "batched solves do not take the nematic (c2) step");
     if (n < 1) fail(SBEC_ERR_INVALID, "n_solves must be >= 1");
     nsolve_ = n;
     const size_t tot = (size_t)n * nc_;
@@ -1092,6 +1091,7 @@ class Engine final : public EngineBase {
     k_seg_finish<1><<<(na + 127) / 128, 128, 0, stream_>>>(partials_, bpe, na, active_, 0, bres_, 16);
     done("reduce_finish", 8.0 * bpe * na);
     SBEC_SWITCH_D(s_.D, launch_batch_energy_local_d, bpe, na);
+    if (nematic()) SBEC_SWITCH_D(s_.D, launch_batch_pair_energy_d, bpe, na);
     std::vector<double> h((size_t)nsolve_ * 16);
     cuda_check(cudaMemcpyAsync(h.data(), bres_, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, stream_), "fetch");
     sync();
@@ -1112,6 +1112,7 @@ class Engine final : public EngineBase {
       double e = 0.5 * (r[0] * dV / N) + r[o] * dV + ez + 0.5 * (double)c0h[b] * r[o + 1] * dV +
                  0.5 * (double)c1h[b] * r[o + 2] * dV;
       if (s_.c_lhy != 0.0) e += (2.0 / 5.0) * s_.c_lhy * r[o + 3] * dV;
+      if (nematic()) e += 0.5 * s_.c2 * r[o + 4] * dV;  // _nematic_energy (src/energy.jl:106-109)
       E[b] = e;
     }
   }
@@ -1412,25 +1413,65 @@ class Engine final : public EngineBase {
     return st != cudaStreamCaptureStatusNone;
   }
 
-  std::vector<int> line_candidates(int n, bool row) const {
+  // Candidates of a call shape: row passes (row), strided lines (reg, not row: tile and
+  // register forms) or x lines (tile forms).
+  std::vector<int> line_candidates(int n, bool row, bool reg) const {
     std::vector<int> c;
-    for (int v = 0; v < kLineVariants; ++v) {
-      if (line_variant(sizeof(R) == 4, n, v) != v) continue;
+    for (int v = 0; v < (reg ? kRowVariants : kLineVariants); ++v) {
+      if (line_variant(sizeof(R) == 4, n, v) != v || !row_variant_compiled(v)) continue;
       if (row && !row_variant_ok(sizeof(R) == 4, n, s_.D, v)) continue;
+      if (!row && v >= kLineVariants && n > 1024) continue;  // register strided lines up to 1024 points
       c.push_back(v);
     }
     return c;
   }
 
+  // Runs strided-line variant v (tile forms 0-7, register forms 12-15).
+  void strided_variant_launch(int v, const LineCtx<R>& c, const Tw<R>& tw, int n, cplx<R>* data, int64_t S,
+                              int64_t inner, int64_t outer, int64_t outer_stride, int n_in, int n_out, int mode,
+                              const int* om, int op) {
+    if constexpr (sizeof(R) == 4) {
+      switch (line_variant(true, n, v)) {
+        case 12: RegKernels<R, 12>::fft_strided(c, tw, n, data, S, inner, outer, outer_stride, n_in, n_out, mode, om, op); return;
+        case 13: RegKernels<R, 13>::fft_strided(c, tw, n, data, S, inner, outer, outer_stride, n_in, n_out, mode, om, op); return;
+        case 14: RegKernels<R, 14>::fft_strided(c, tw, n, data, S, inner, outer, outer_stride, n_in, n_out, mode, om, op); return;
+        case 15: RegKernels<R, 15>::fft_strided(c, tw, n, data, S, inner, outer, outer_stride, n_in, n_out, mode, om, op); return;
+        default: break;
+      }
+    }
+    with_variant(n, v, [&](auto vv) {
+      LineKernels<R, decltype(vv)::value>::fft_strided(c, tw, n, data, S, inner, outer, outer_stride, n_in, n_out,
+                                                       mode, om, op);
+    });
+  }
+
+  // Runs row-pass variant v (tile forms 0-7 through LineKernels, register forms 12-15).
+  void row_variant_launch(int v, const LineCtx<R>& c, const Tw<R>& tw, int nx, int D, const RowArgs<R>& a, int nb) {
+    if constexpr (sizeof(R) == 4) {
+      switch (line_variant(true, nx, v)) {
+        case 12: RegKernels<R, 12>::row(c, tw, nx, D, a, nb); return;
+        case 13: RegKernels<R, 13>::row(c, tw, nx, D, a, nb); return;
+        case 14: RegKernels<R, 14>::row(c, tw, nx, D, a, nb); return;
+        case 15: RegKernels<R, 15>::row(c, tw, nx, D, a, nb); return;
+        default: break;
+      }
+    }
+    with_variant(nx, v, [&](auto vv) { LineKernels<R, decltype(vv)::value>::row(c, tw, nx, D, a, nb); });
+  }
+
   // Variant for a call shape: forced, cached, or measured now.  launch(v, buf)
   // runs variant v on buf, a copy of the `extent` elements at src.
   template <typename Launch>
-  int line_tune(const std::string& shape, int n, bool row, const cplx<R>* src, size_t extent, Launch&& launch) {
-    const std::vector<int> cands = line_candidates(n, row);
+  int line_tune(const std::string& shape, int n, bool row, const cplx<R>* src, size_t extent, Launch&& launch,
+                bool reg = false) {
+    reg = reg || row;
+    const std::vector<int> cands = line_candidates(n, row, reg);
     if (cands.empty()) return 0;
     if (tune_force_ >= 0) {
+      // a forced register form (12-15) runs the x-line kernels of its plan and tile scale
+      const int f = reg ? tune_force_ : (tune_force_ & (kLineVariants - 1));
       for (int v : cands)
-        if (v == tune_force_) return v;
+        if (v == f) return v;
       return 0;
     }
     if (!tune_on_ || cands.size() == 1) return cands[0];
@@ -1519,7 +1560,7 @@ class Engine final : public EngineBase {
                          const int bps = (int)((a.n_rows + rpb - 1) / rpb);
                          b.blocks_per_solve = bps;
                          const int nb = b.active ? bps * b.n_slots : bps;
-                         with_variant(nx, v, [&](auto vv) { LineKernels<R, decltype(vv)::value>::row(c, tw, nx, D, b, nb); });
+                         row_variant_launch(v, c, tw, nx, D, b, nb);
                        });
   }
 
@@ -1556,17 +1597,11 @@ class Engine final : public EngineBase {
                                  std::to_string(n_in) + "/" + std::to_string(n_out) + " mode=" + std::to_string(mode) +
                                  (om ? " batched" : ""),
                              n, false, data, extent, [&](int v, cplx<R>* buf) {
-                               with_variant(n, v, [&](auto vv) {
-                                 LineKernels<R, decltype(vv)::value>::fft_strided(c, tw, n, buf, S, inner, outer,
-                                                                                  outer_stride, n_in, n_out, mode, om,
-                                                                                  op);
-                               });
-                             });
-    pb();
-    with_variant(n, vs, [&](auto v) {
-      LineKernels<R, decltype(v)::value>::fft_strided(c, tw, n, data, S, inner, outer, outer_stride, n_in, n_out,
+                               strided_variant_launch(v, c, tw, n, buf, S, inner, outer, outer_stride, n_in, n_out,
                                                       mode, om, op);
-    });
+                             }, true);
+    pb();
+    strided_variant_launch(vs, c, tw, n, data, S, inner, outer, outer_stride, n_in, n_out, mode, om, op);
     done(mode == 2 ? "fft_last_kinetic" : "fft_strided",
          (double)sizeof(cplx<R>) * (double)(n_in + n_out) * (double)inner * (double)outer);
   }
@@ -1788,6 +1823,17 @@ class Engine final : public EngineBase {
                                nz, 0);
   }
 
+  // per-solve sum |A00|^2 -> bres_[16 b + 1 + D + 4]
+  template <int D>
+  void launch_batch_pair_energy_d(int bpe, int na) {
+    pb();
+    k_batch_pair_energy<R, D><<<dim3(bpe, na), kRedThreads, 0, stream_>>>(bpsi_, N_, nc_, active_, partials_);
+    done("reduce", sizeof(cplx<R>) * D * (double)N_ * na);
+    pb();
+    k_seg_finish<1><<<(na + 127) / 128, 128, 0, stream_>>>(partials_, bpe, na, active_, 0, bres_ + 1 + D + 4, 16);
+    done("reduce_finish", 8.0 * bpe * na);
+  }
+
   template <int D>
   void launch_batch_energy_local_d(int bpe, int na) {
     pb();
@@ -1837,7 +1883,7 @@ class Engine final : public EngineBase {
     const Tw<R> tw = twiddle(nx);
     const int D = s_.D;
     pb();
-    with_variant(nx, v_row_, [&](auto v) { LineKernels<R, decltype(v)::value>::row(c, tw, nx, D, a, nb); });
+    row_variant_launch(v_row_, c, tw, nx, D, a, nb);
     done("row_pass", 2.0 * (double)sizeof(cplx<R>) * nc_ + (double)sizeof(R) * N_ * ((a.flags & RP_POT1) ? 1 : 0));
     return nb;
   }
@@ -2241,7 +2287,7 @@ class Engine final : public EngineBase {
   double* snap_psi_[2] = {nullptr, nullptr};
   cudaEvent_t snap_ev_[2] = {nullptr, nullptr};
   bool tune_on_ = true;       // SBEC_TUNE=0: variant 0 everywhere
-  int tune_force_ = -1;       // SBEC_TUNE_FORCE=v: variant v wherever it is compiled
+  int tune_force_ = -1;       // SBEC_TUNE_FORCE=v: variant v wherever it is compiled (line kernels: v & 7)
   bool row_tuned_ = false;
   std::map<std::string, int> tuned_;  // this engine's strided / x decisions by call shape
   std::vector<std::string> tune_log_;

@@ -100,10 +100,10 @@ __device__ __forceinline__ void dft(cplx<R>* v) {
   }
 }
 
-// Twiddle, butterfly and store of one Stockham stage for the values v a thread loaded.
+// Twiddles and butterflies of one Stockham stage on the values v a thread loaded
+// (butterfly b holds v[b*RAD .. b*RAD+RAD-1], read at j + r*N/RAD, j = t + b*TPL).
 template <typename R, int N, int E, int RAD, int SIGN>
-__device__ __forceinline__ void fft_stage_store(cplx<R>* s, int SI, int SL, int l, int t, int Ns, const Tw<R>& tw,
-                                                cplx<R> (&v)[E]) {
+__device__ __forceinline__ void fft_stage_math(int t, int Ns, const Tw<R>& tw, cplx<R> (&v)[E]) {
   constexpr int TPL = N / E;
   constexpr int NBT = E / RAD;
 #pragma unroll
@@ -116,6 +116,20 @@ __device__ __forceinline__ void fft_stage_store(cplx<R>* s, int SI, int SL, int 
       for (int r = 1; r < RAD; ++r) v[b * RAD + r] = tw_mul<R>(v[b * RAD + r], tw, r * step, SIGN > 0);
     }
     dft<R, RAD, SIGN>(&v[b * RAD]);
+  }
+}
+
+// Twiddle, butterfly and store of one Stockham stage for the values v a thread loaded.
+template <typename R, int N, int E, int RAD, int SIGN>
+__device__ __forceinline__ void fft_stage_store(cplx<R>* s, int SI, int SL, int l, int t, int Ns, const Tw<R>& tw,
+                                                cplx<R> (&v)[E]) {
+  constexpr int TPL = N / E;
+  constexpr int NBT = E / RAD;
+  fft_stage_math<R, N, E, RAD, SIGN>(t, Ns, tw, v);
+#pragma unroll
+  for (int b = 0; b < NBT; ++b) {
+    const int j = t + b * TPL;
+    const int jm = j & (Ns - 1);
     const int base = (j - jm) * RAD + jm;
 #pragma unroll
     for (int r = 0; r < RAD; ++r) s[(base + r * Ns) * SI + l * SL] = v[b * RAD + r];
@@ -186,6 +200,109 @@ __device__ __forceinline__ void run_stages(cplx<R>* s, int SI, int SL, int l, in
   if constexpr (sizeof...(REST) > 0) run_stages<R, N, E, SIGN, REST...>(s, SI, SL, l, t, Ns * RAD, tw, act);
 }
 
+// ---- register-resident transforms (the D lines of one row per thread)
+//
+// Thread t of a line keeps the values at positions x = t + k*TPL (k < E, TPL = N/E) in u[k].
+// Butterfly b of a radix-RAD Stockham stage reads positions j + r*N/RAD with j = t + b*TPL,
+// i.e. slot k = b + r*(E/RAD) of u; the first stage (Ns = 1) can therefore take its inputs
+// straight from u, and the last stage (Ns = N/RAD, where (j mod Ns) = j) writes its outputs
+// to those same positions.  A transform thus starts from and ends in registers, with shared
+// memory used only between its stages (one barrier per inner stage in the ping-pong form).
+// Same twiddles, butterflies and order of operations as the tile transforms above, so the
+// results are bit-identical to them.
+template <int E, int RAD>
+__host__ __device__ constexpr int reg_slot(int e) {
+  return e / RAD + (e % RAD) * (E / RAD);
+}
+
+// First stage: registers -> dst (lines l0 .. l0+D-1 of the tile, element i of line l at
+// i*SI + l*SL, as in the tile transforms).
+template <typename R, int N, int E, int RAD, int SIGN, int D>
+__device__ __forceinline__ void reg_stage_first(const cplx<R> (&u)[D][E], cplx<R>* dst, int SI, int SL, int l0,
+                                                int t, const Tw<R>& tw) {
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    cplx<R> v[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = u[c][reg_slot<E, RAD>(e)];
+    fft_stage_store<R, N, E, RAD, SIGN>(dst, SI, SL, l0 + c, t, 1, tw, v);
+  }
+}
+
+template <typename R, int N, int E, int RAD>
+__device__ __forceinline__ void reg_stage_load(const cplx<R>* src, int SI, int SL, int l, int t, cplx<R> (&v)[E]) {
+  constexpr int TPL = N / E;
+  constexpr int NBT = E / RAD;
+  constexpr int STRIDE = N / RAD;
+#pragma unroll
+  for (int b = 0; b < NBT; ++b) {
+#pragma unroll
+    for (int r = 0; r < RAD; ++r) v[b * RAD + r] = src[(t + b * TPL + r * STRIDE) * SI + l * SL];
+  }
+}
+
+// Stages after the first: inner stages through shared memory, the last one into registers.
+// On entry cur holds the previous stage's output and every thread has passed the barrier
+// after its stores; oth is free (ping-pong form).
+template <typename R, int N, int E, int SIGN, bool PP, int D, int RAD, int... REST>
+__device__ __forceinline__ void reg_stages(cplx<R> (&u)[D][E], cplx<R>*& cur, cplx<R>*& oth, int SI, int SL, int l0,
+                                           int t, int Ns, const Tw<R>& tw) {
+  if constexpr (sizeof...(REST) == 0) {
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      cplx<R> v[E];
+      reg_stage_load<R, N, E, RAD>(cur, SI, SL, l0 + c, t, v);
+      fft_stage_math<R, N, E, RAD, SIGN>(t, Ns, tw, v);
+#pragma unroll
+      for (int e = 0; e < E; ++e) u[c][reg_slot<E, RAD>(e)] = v[e];
+    }
+  } else {
+    if constexpr (PP) {
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+        cplx<R> v[E];
+        reg_stage_load<R, N, E, RAD>(cur, SI, SL, l0 + c, t, v);
+        fft_stage_store<R, N, E, RAD, SIGN>(oth, SI, SL, l0 + c, t, Ns, tw, v);
+      }
+      __syncthreads();
+      cplx<R>* x = cur;
+      cur = oth;
+      oth = x;
+    } else {
+      cplx<R> v[D][E];
+#pragma unroll
+      for (int c = 0; c < D; ++c) reg_stage_load<R, N, E, RAD>(cur, SI, SL, l0 + c, t, v[c]);
+      __syncthreads();
+#pragma unroll
+      for (int c = 0; c < D; ++c) fft_stage_store<R, N, E, RAD, SIGN>(cur, SI, SL, l0 + c, t, Ns, tw, v[c]);
+      __syncthreads();
+    }
+    reg_stages<R, N, E, SIGN, PP, D, REST...>(u, cur, oth, SI, SL, l0, t, Ns * RAD, tw);
+  }
+}
+
+// A whole transform of the D lines held in u.  The first stage writes into oth (ping-pong
+// form): cur may still be read by the last stage of a transform before.  The in-place
+// form has one buffer and waits for those reads first.  On return the last stage has
+// read cur and oth is free again.
+template <typename R, int N, int E, int SIGN, bool PP, int D, int RAD0, int... REST>
+__device__ __forceinline__ void reg_fft_run(cplx<R> (&u)[D][E], cplx<R>*& cur, cplx<R>*& oth, int SI, int SL, int l0,
+                                            int t, const Tw<R>& tw) {
+  static_assert(sizeof...(REST) >= 1, "register transforms need at least two stages");
+  if constexpr (PP) {
+    reg_stage_first<R, N, E, RAD0, SIGN, D>(u, oth, SI, SL, l0, t, tw);
+    __syncthreads();
+    cplx<R>* x = cur;
+    cur = oth;
+    oth = x;
+  } else {
+    __syncthreads();
+    reg_stage_first<R, N, E, RAD0, SIGN, D>(u, cur, SI, SL, l0, t, tw);
+    __syncthreads();
+  }
+  reg_stages<R, N, E, SIGN, PP, D, REST...>(u, cur, oth, SI, SL, l0, t, RAD0, tw);
+}
+
 // Radix plans per line length: E = largest radix; stages run in the listed order.
 // FP64 (FP64-throughput bound) uses radix-16 stages, which need the fewest
 // twiddle multiplies; FP32 (latency / bandwidth bound) uses radix-4/8 stages so
@@ -204,6 +321,12 @@ template <int N> struct FftPlan32;
     static __device__ __forceinline__ cplx<R>* run_pp(cplx<R>* a, cplx<R>* b, int SI, int SL,   \
                                                       int l, int t, const Tw<R>& tw, bool act) { \
       return run_stages_pp<R, NN, EE, SIGN, __VA_ARGS__>(a, b, SI, SL, l, t, 1, tw, act);        \
+    }                                                                                            \
+    template <typename R, int SIGN, bool PP, int D>                                              \
+    static __device__ __forceinline__ void run_reg(cplx<R> (&u)[D][EE], cplx<R>*& cur,          \
+                                                   cplx<R>*& oth, int SI, int SL, int l0, int t, \
+                                                   const Tw<R>& tw) {                            \
+      reg_fft_run<R, NN, EE, SIGN, PP, D, __VA_ARGS__>(u, cur, oth, SI, SL, l0, t, tw);         \
     }                                                                                            \
   };
 SBEC_PLAN(FftPlan, 2, 2, 2)

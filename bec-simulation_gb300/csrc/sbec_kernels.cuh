@@ -315,6 +315,79 @@ k_fft_strided(cplx<R>* __restrict__ data, int64_t S, int64_t inner, int64_t oute
                                            (int64_t)blockIdx.x * W, o, smem_raw, true);
 }
 
+// Register-resident form of k_fft_strided (same modes, pruning, arithmetic and results): thread
+// (w, t) of a tile of W lines holds elements i = t + k*TPL (k < E) of line w in registers, loads
+// them from and stores them to global memory directly (the same coalescing as the tile
+// loads: W consecutive elements per row), and in mode 2 multiplies the kinetic phase on the
+// registers between the forward and the inverse transform; shared memory (element (i, w) at
+// i*W + w) carries only the transforms' inner stages.
+template <typename R, int N, int W, int P, bool PP>
+__global__ void __launch_bounds__(W*(N / PlanOf<R, N, P>::E))
+k_fft_strided_reg(cplx<R>* __restrict__ data, int64_t S, int64_t inner, int64_t outer_stride, int n_in, int n_out,
+                  int mode, PhaseRef<R> ph, Tw<R> tw, const int* __restrict__ omap, int oper) {
+  constexpr int E = PlanOf<R, N, P>::E;
+  constexpr int TPL = N / E;
+  pdl_wait();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx<R>* cur = reinterpret_cast<cplx<R>*>(smem_raw);
+  cplx<R>* oth = cur + W * N;
+  const int64_t o = omap ? (int64_t)omap[blockIdx.y / oper] * oper + blockIdx.y % oper : (int64_t)blockIdx.y;
+  const int64_t i0 = (int64_t)blockIdx.x * W;
+  const int tid = threadIdx.x;
+  const int w = tid % W, t = tid / W;
+  const bool live = i0 + w < inner;
+  cplx<R>* g = data + o * outer_stride + i0;
+  cplx<R> u[1][E];
+#pragma unroll
+  for (int k = 0; k < E; ++k) {
+    const int i = t + k * TPL;
+    u[0][k] = (live && i < n_in) ? g[(int64_t)i * S + w] : mk<R>(0, 0);
+  }
+  if (mode == 1) {
+    PlanOf<R, N, P>::template run_reg<R, +1, PP, 1>(u, cur, oth, W, 1, w, t, tw);
+  } else {
+    PlanOf<R, N, P>::template run_reg<R, -1, PP, 1>(u, cur, oth, W, 1, w, t, tw);
+    if (mode == 2) {
+      // lower-axis coordinates and factors of the kinetic phase for this line
+      int64_t pos = i0 + w;
+      cplx<R> f = mk<R>(1, 0);
+      int idx0 = 0, idx1 = 0;
+      if (ph.ndim >= 2) {
+        idx0 = (int)(pos % ph.n[0]);
+        pos /= ph.n[0];
+        f = f * __ldg(ph.tab[0].hi + idx0);
+      }
+      if (ph.ndim == 3) {
+        idx1 = (int)(pos % ph.n[1]);
+        f = f * __ldg(ph.tab[1].hi + idx1);
+      }
+      const Tw<R> last = ph.tab[ph.ndim - 1];
+#pragma unroll
+      for (int k = 0; k < E; ++k) {
+        const int i = t + k * TPL;
+        if constexpr (sizeof(R) == 8) {
+          u[0][k] = u[0][k] * (f * __ldg(last.hi + i));
+        } else if (ph.unbiased) {
+          u[0][k] = kinetic_rot(u[0][k], ph, idx0, idx1, i);
+        } else {
+          cplx<R> v = phase_mul<R>(u[0][k], ph.tab[0], idx0, ph.scale0, 0);
+          if (ph.ndim == 3) v = phase_mul<R>(v, ph.tab[1], idx1, (R)1, 0);
+          u[0][k] = phase_mul<R>(v, last, i, (R)1, 0);
+        }
+      }
+      PlanOf<R, N, P>::template run_reg<R, +1, PP, 1>(u, cur, oth, W, 1, w, t, tw);
+    }
+  }
+  pdl_trigger();
+  if (live) {
+#pragma unroll
+    for (int k = 0; k < E; ++k) {
+      const int i = t + k * TPL;
+      if (i < n_out) g[(int64_t)i * S + w] = u[0][k];
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Dipolar convolution (src/ddi.jl:108-136, src/ddi_padded.jl:55-85).
 // Real spin-density fields live on the simulation grid (nx, ny, nz); the
@@ -1325,6 +1398,141 @@ k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
   pdl_wait();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   row_pass_block<R, N, D, RPB, P, PP, false>(a, st, ph, tw, (int)blockIdx.x, smem_raw, true);
+}
+
+// Register-resident form of the fused row pass: the operators, flags and arithmetic of
+// row_pass_block, with thread t of tile row rr holding positions x = t + k*TPL (k < E) of
+// all D components of its row in registers.  Every x transform starts from and ends in
+// registers (the first and last Stockham stages read and write exactly those positions,
+// reg_fft_run), so psi is loaded from and stored to global memory directly (consecutive
+// threads, consecutive x), the potential stages and the kinetic phase run on registers
+// between the transforms, and shared memory carries only the transforms' inner stages:
+// per pass half the shared-memory traffic and block barriers of the tile form, and no
+// thread idles during a transform.  The states are bit-identical to the tile form of the
+// same plan; the norm partials (RP_NORM, RP_MID) are summed in another order.
+// u[c][k] <- u[c][k+1], u[c][E-1] <- u[c][0]: after E calls u is back in its order.
+template <typename R, int D, int E>
+__device__ __forceinline__ void rotate_slots(cplx<R> (&u)[D][E]) {
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    const cplx<R> f = u[c][0];
+#pragma unroll
+    for (int k = 0; k + 1 < E; ++k) u[c][k] = u[c][k + 1];
+    u[c][E - 1] = f;
+  }
+}
+
+template <typename R, int N, int D, int RPB, int P, bool PP>
+__global__ void __launch_bounds__(RPB*(N / PlanOf<R, N, P>::E))
+k_row_pass_reg(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
+  constexpr int E = PlanOf<R, N, P>::E;
+  constexpr int TPL = N / E;
+  pdl_wait();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double red[32];
+  cplx<R>* cur = reinterpret_cast<cplx<R>*>(smem_raw);
+  cplx<R>* oth = cur + D * RPB * N;  // second tile of the ping-pong stages (PP)
+  const int tid = threadIdx.x;
+  const int rr = tid / TPL, t = tid % TPL;
+  const int blk = (int)blockIdx.x;
+  const int slot = a.active ? (int)(blk / a.blocks_per_solve) : 0;
+  const int lblk = a.active ? (int)(blk % a.blocks_per_solve) : blk;
+  const int b = a.active ? a.active[slot] : 0;
+  cplx<R>* psi = a.psi + (int64_t)b * a.solve_stride;
+  const R c0 = a.c0s ? a.c0s[b] : a.p1.c0;
+  const R c1 = a.c1s ? a.c1s[b] : a.p1.c1;
+  const int64_t row = (int64_t)lblk * RPB + rr;
+  const bool live = row < a.n_rows;
+  R scale = (R)1;
+  if (a.flags & RP_SCALE) scale = (R)(1.0 / sqrt(a.norm_total[b] * a.dV));
+  if (a.flags & RP_CORR) scale = a.corr[b];
+  const bool scaled = (a.flags & (RP_SCALE | RP_CORR)) != 0;
+  cplx<R> u[D][E];
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+#pragma unroll
+    for (int k = 0; k < E; ++k) {
+      cplx<R> v = mk<R>(0, 0);
+      if (live) v = psi[c * a.N + row * N + t + k * TPL];
+      if (scaled) v = v * scale;
+      u[c][k] = v;
+    }
+  }
+  const int l0 = rr * D;
+  if (a.flags & RP_INV_X) PlanOf<R, N, P>::template run_reg<R, +1, PP, D>(u, cur, oth, 1, N, l0, t, tw);
+  // The pointwise stages take the thread's E points one after another through slot 0 of u
+  // (rotate_slots): a runtime loop keeps one copy of the stage's code, where unrolling
+  // over the points would inline the potential stage E times per flag.
+  double acc = 0.0;
+  if (a.flags & RP_POT1) {
+    const R pred = (a.flags & RP_MID) ? a.pred[b] : (R)1;
+#pragma unroll 1
+    for (int k = 0; k < E; ++k) {
+      if (live) {
+        cplx<R> v[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) v[c] = u[c][0];
+        const R Vp = a.p1.V[row * N + t + k * TPL];
+        pot_stage<R, D>(v, Vp, a.p1, st, c0, c1);
+        if (a.flags & RP_MID) {
+#pragma unroll
+          for (int c = 0; c < D; ++c) {
+            acc += (double)v[c].x * v[c].x + (double)v[c].y * v[c].y;
+            v[c] = v[c] * pred;
+          }
+          pot_stage<R, D>(v, Vp, a.p2, st, c0, c1);
+        }
+#pragma unroll
+        for (int c = 0; c < D; ++c) u[c][0] = v[c];
+      }
+      rotate_slots<R, D, E>(u);
+    }
+  }
+  if (a.flags & (RP_FWD_X | RP_KIN_X)) PlanOf<R, N, P>::template run_reg<R, -1, PP, D>(u, cur, oth, 1, N, l0, t, tw);
+  if (a.flags & RP_KIN_X) {
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+#pragma unroll
+      for (int k = 0; k < E; ++k) u[c][k] = phase_mul<R>(u[c][k], ph.tab[0], t + k * TPL, ph.scale0, ph.unbiased);
+    }
+    PlanOf<R, N, P>::template run_reg<R, +1, PP, D>(u, cur, oth, 1, N, l0, t, tw);
+  }
+  if (a.flags & (RP_POT2 | RP_NORM)) {
+#pragma unroll 1
+    for (int k = 0; k < E; ++k) {
+      if (live) {
+        if (a.flags & RP_POT2) {
+          cplx<R> v[D];
+#pragma unroll
+          for (int c = 0; c < D; ++c) v[c] = u[c][0];
+          pot_stage<R, D>(v, a.p2.V[row * N + t + k * TPL], a.p2, st, c0, c1);
+#pragma unroll
+          for (int c = 0; c < D; ++c) u[c][0] = v[c];
+        }
+#pragma unroll
+        for (int c = 0; c < D; ++c) acc += (double)u[c][0].x * u[c][0].x + (double)u[c][0].y * u[c][0].y;
+      }
+      rotate_slots<R, D, E>(u);
+    }
+  }
+  pdl_trigger();
+  if (live) {
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+#pragma unroll
+      for (int k = 0; k < E; ++k) psi[c * a.N + row * N + t + k * TPL] = u[c][k];
+    }
+  }
+  if (a.flags & (RP_NORM | RP_MID)) {
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((tid & 31) == 0) red[tid >> 5] = acc;
+    __syncthreads();
+    if (tid == 0) {
+      double x = 0.0;
+      for (int w = 0; w < (int)((blockDim.x + 31) >> 5); ++w) x += red[w];
+      a.partials[blk] = x;
+    }
+  }
 }
 
 // n fused ITP split steps of a 1-D solve (one row-pass block holds its whole line of all
@@ -2373,6 +2581,30 @@ __global__ void __launch_bounds__(kRedThreads) k_batch_energy_local(const cplx<R
     acc[D + 3] += n * n * sqrt(n);
   }
   block_reduce_store_2d<D + 4>(acc, partials, false);
+}
+
+// Per-solve sum over points of |A00|^2 (the nematic energy, as k_pair_energy) for solve
+// active[blockIdx.y].
+template <typename R, int D>
+__global__ void __launch_bounds__(kRedThreads) k_batch_pair_energy(const cplx<R>* __restrict__ psi, int64_t N,
+                                                                   int64_t solve_stride,
+                                                                   const int* __restrict__ active,
+                                                                   double* partials) {
+  double acc[1] = {0.0};
+  const cplx<R>* base = psi + (int64_t)active[blockIdx.y] * solve_stride;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < N; p += (int64_t)gridDim.x * blockDim.x) {
+    double ar = 0.0, ai = 0.0;
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      const cplx<R> x = base[c * N + p], y = base[(D - 1 - c) * N + p];
+      const double pr = (double)x.x * y.x - (double)x.y * y.y;
+      const double pi = (double)x.x * y.y + (double)x.y * y.x;
+      ar += (c & 1) ? -pr : pr;
+      ai += (c & 1) ? -pi : pi;
+    }
+    acc[0] += (ar * ar + ai * ai) / (double)D;
+  }
+  block_reduce_store_2d<1>(acc, partials, false);
 }
 
 // Per-solve kinetic sum over a compact (slot-ordered) transformed scratch buffer.

@@ -14,6 +14,13 @@
 // FP32 lines of kMinTunedLine points or more have all eight variants, each compiled
 // in its own translation unit (sbec_lines_f32_v<V>.cu); FP64 and shorter lines
 // have variant 0 only.
+//
+// The fused row pass and the strided lines have four more variants, 8 + V for ping-pong V
+// (12-15): the register-resident forms (k_row_pass_reg, k_fft_strided_reg;
+// sbec_rows_f32_v<V>.cu), in which a thread keeps its positions of a line (of all D lines
+// of its row, in the row pass) in registers between the transforms.  Row tiles are rows of
+// TPL threads (a thread covers all D components of its positions), ~64 threads at tile
+// scale 0 and twice that at scale 1; strided tiles are those of variant V - 8.
 #pragma once
 
 #include <algorithm>
@@ -24,7 +31,13 @@
 namespace sbec {
 
 constexpr int kLineVariants = 8;
+constexpr int kRowVariants = 16;  // row passes and strided lines: 0-7 tile form, 12-15 register form
 constexpr int kMinTunedLine = 32;
+
+// A row-pass / strided variant is compiled: the tile forms, and the register forms with
+// ping-pong stages.
+inline bool row_variant_compiled(int V) { return V < 8 || (V >= 12 && V < kRowVariants); }
+inline bool row_variant_reg(int V) { return V >= 8; }
 
 template <typename R>
 struct LineCtx {
@@ -41,6 +54,15 @@ struct LineKernels {
                           int64_t outer, int64_t outer_stride, int n_in, int n_out, int mode, const int* omap,
                           int oper);
   static void row(const LineCtx<R>& c, const Tw<R>& tw, int n, int D, const RowArgs<R>& a, int blocks);
+};
+
+// Register-resident row passes and strided lines (V = 12..15).
+template <typename R, int V>
+struct RegKernels {
+  static void row(const LineCtx<R>& c, const Tw<R>& tw, int n, int D, const RowArgs<R>& a, int blocks);
+  static void fft_strided(const LineCtx<R>& c, const Tw<R>& tw, int n, cplx<R>* data, int64_t S, int64_t inner,
+                          int64_t outer, int64_t outer_stride, int n_in, int n_out, int mode, const int* omap,
+                          int oper);
 };
 
 // n fused ITP split steps of a 1-D solve in one launch (k_row_itp_steps, plan variant 0;
@@ -65,7 +87,7 @@ inline int line_tpl(bool fp32, int n, int V) { return std::max(1, n / plan_radix
 
 inline int row_rpb_host(bool fp32, int n, int D, int V) {
   V = line_variant(fp32, n, V);
-  int r = 64 / (D * line_tpl(fp32, n, V));
+  int r = row_variant_reg(V) ? 64 / line_tpl(fp32, n, V) : 64 / (D * line_tpl(fp32, n, V));
   if (r < 1) r = 1;
   return r << ((V >> 1) & 1);
 }
@@ -73,6 +95,7 @@ inline int row_rpb_host(bool fp32, int n, int D, int V) {
 inline int row_threads_host(bool fp32, int n, int D, int V) {
   V = line_variant(fp32, n, V);
   const int rpb = row_rpb_host(fp32, n, D, V);
+  if (row_variant_reg(V)) return rpb * line_tpl(fp32, n, V);
   const int fft = D * rpb * line_tpl(fp32, n, V);
   const int pts = std::min(rpb * n, 1024);
   return (std::max(fft, pts) + 31) / 32 * 32;

@@ -181,4 +181,100 @@ void LineKernels<R, V>::row(const LineCtx<R>& c, const Tw<R>& tw, int n, int D, 
 
 #undef SBEC_LINE_CASES
 
+// ---- register-resident row passes and strided lines (V = 12..15: plan V & 1, tile scale
+// (V >> 1) & 1, ping-pong)
+template <typename R, int N, int V>
+constexpr int row_rpb_reg_v() {
+  constexpr int tpl = N / PlanOf<R, N, (V & 1)>::E;
+  constexpr int r = 64 / tpl;
+  return (r < 1 ? 1 : r) << ((V >> 1) & 1);
+}
+
+template <typename R, int V>
+struct RegImpl {
+  static constexpr int P = V & 1;
+  static_assert(V >= 12 && V < 16, "register forms are variants 12-15");
+
+  template <int NN>
+  static void fft_strided(const LineCtx<R>& c, const Tw<R>& tw, cplx<R>* data, int64_t S, int64_t inner,
+                          int64_t outer, int64_t outer_stride, int n_in, int n_out, int mode, const int* omap,
+                          int oper) {
+    constexpr int W = strided_w_v<R, NN, (V & 7)>();
+    constexpr int TPL = NN / PlanOf<R, NN, P>::E;
+    constexpr long TILE = (long)sizeof(cplx<R>) * W * NN;
+    constexpr bool PP = 2 * TILE <= 200 * 1024;
+    const size_t smem = PP ? 2 * TILE : TILE;
+    auto kern = k_fft_strided_reg<R, NN, W, P, PP>;
+    static const bool once = (line_set_smem(kern, smem), true);
+    (void)once;
+    dim3 grid((unsigned)((inner + W - 1) / W), (unsigned)outer);
+    line_launch(c, kern, grid, dim3(W * TPL), smem, data, S, inner, outer_stride, n_in, n_out, mode, c.ph, tw, omap,
+                oper);
+  }
+
+  template <int NN, int D>
+  static void row(const LineCtx<R>& c, const Tw<R>& tw, const RowArgs<R>& a, int blocks) {
+    constexpr int RPB = row_rpb_reg_v<R, NN, V>();
+    constexpr int NT = RPB * (NN / PlanOf<R, NN, P>::E);
+    constexpr long TILE = (long)sizeof(cplx<R>) * D * RPB * NN;
+    if constexpr (NT > 1024 || 2 * TILE > 200 * 1024) {
+      fail(SBEC_ERR_UNSUPPORTED, "row pass tile too large for this line length");
+    } else {
+      const size_t smem = 2 * TILE;
+      auto kern = k_row_pass_reg<R, NN, D, RPB, P, true>;
+      static const bool once = (line_set_smem(kern, smem), true);
+      (void)once;
+      line_launch(c, kern, dim3((unsigned)blocks), dim3(NT), smem, a, c.st, c.ph, tw);
+    }
+  }
+
+  template <int NN>
+  static void row_n(const LineCtx<R>& c, const Tw<R>& tw, int D, const RowArgs<R>& a, int blocks) {
+    switch (D) {
+      case 1: row<NN, 1>(c, tw, a, blocks); break;
+      case 3: row<NN, 3>(c, tw, a, blocks); break;
+      case 5: row<NN, 5>(c, tw, a, blocks); break;
+      default: fail(SBEC_ERR_UNSUPPORTED, "fused path needs D in {1,3,5}");
+    }
+  }
+};
+
+template <typename R, int V>
+void RegKernels<R, V>::fft_strided(const LineCtx<R>& c, const Tw<R>& tw, int n, cplx<R>* data, int64_t S,
+                                   int64_t inner, int64_t outer, int64_t outer_stride, int n_in, int n_out, int mode,
+                                   const int* omap, int oper) {
+  switch (n) {
+#define SBEC_REG_STRIDED(NN)                                                                                  \
+  case NN:                                                                                                    \
+    RegImpl<R, V>::template fft_strided<NN>(c, tw, data, S, inner, outer, outer_stride, n_in, n_out, mode, omap, \
+                                            oper);                                                            \
+    return;
+    SBEC_REG_STRIDED(32)
+    SBEC_REG_STRIDED(64)
+    SBEC_REG_STRIDED(128)
+    SBEC_REG_STRIDED(256)
+    SBEC_REG_STRIDED(512)
+    SBEC_REG_STRIDED(1024)
+#undef SBEC_REG_STRIDED
+    default: fail(SBEC_ERR_UNSUPPORTED, "unsupported strided FFT length " + std::to_string(n) + " for line variant " +
+                                            std::to_string(V));
+  }
+}
+
+template <typename R, int V>
+void RegKernels<R, V>::row(const LineCtx<R>& c, const Tw<R>& tw, int n, int D, const RowArgs<R>& a, int blocks) {
+  switch (n) {
+    case 32: RegImpl<R, V>::template row_n<32>(c, tw, D, a, blocks); return;
+    case 64: RegImpl<R, V>::template row_n<64>(c, tw, D, a, blocks); return;
+    case 128: RegImpl<R, V>::template row_n<128>(c, tw, D, a, blocks); return;
+    case 256: RegImpl<R, V>::template row_n<256>(c, tw, D, a, blocks); return;
+    case 512: RegImpl<R, V>::template row_n<512>(c, tw, D, a, blocks); return;
+    case 1024: RegImpl<R, V>::template row_n<1024>(c, tw, D, a, blocks); return;
+    case 2048: RegImpl<R, V>::template row_n<2048>(c, tw, D, a, blocks); return;
+    case 4096: RegImpl<R, V>::template row_n<4096>(c, tw, D, a, blocks); return;
+    default: fail(SBEC_ERR_UNSUPPORTED, "unsupported row length " + std::to_string(n) + " for row variant " +
+                                            std::to_string(V));
+  }
+}
+
 }  // namespace sbec

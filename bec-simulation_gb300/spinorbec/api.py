@@ -599,11 +599,20 @@ def _find_ground_state_adaptive(grid, atom, interactions, zeeman, potential, dt,
                 final_dt=final_dt.value)
 
 
+def _nematic_c2(interactions: InteractionParams):
+    """The nematic c2 of contact couplings (c_extra[0]), or None when c_extra holds a higher
+    coupling (c3 and up: the tensor path or terms the batch does not take)."""
+    extra = [float(v) for v in interactions.c_extra]
+    if any(abs(v) > 1e-30 for v in extra[1:]):
+        return None
+    return extra[0] if extra else 0.0
+
+
 def _batch_eligible(atom: AtomSpecies, interactions: InteractionParams, kw: dict) -> bool:
     """Whether every start of a multistart search can run as one GroundStateBatch: the batch
-    takes contact couplings (c0, c1, c_lhy) with a static Zeeman term and the plain
-    find_ground_state loop (no DDI, adaptive dt or magnetisation constraint)."""
-    if atom.F > 2 or any(abs(float(v)) > 1e-30 for v in interactions.c_extra):
+    takes contact couplings (c0, c1, c_lhy and the nematic c2) with a static Zeeman term and
+    the plain find_ground_state loop (no DDI, adaptive dt or magnetisation constraint)."""
+    if atom.F > 2 or _nematic_c2(interactions) is None:
         return False
     if kw.get("enable_ddi") or kw.get("adaptive_dt") or kw.get("target_magnetization") is not None:
         return False
@@ -638,7 +647,7 @@ def find_ground_state_multistart(*, initial_states=("polar", "ferromagnetic", "u
         b = GroundStateBatch(grid=grid, atom=atom, c0s=[interactions.c0] * len(starts),
                              c1s=[interactions.c1] * len(starts), psi_inits=[p for _, _, p in starts],
                              zeeman=zeeman, potential=kw.get("potential"), dt=dt, c_lhy=interactions.c_lhy,
-                             precision=kw.get("precision", "fp64"))
+                             c2=_nematic_c2(interactions), precision=kw.get("precision", "fp64"))
         n_steps = kw.get("n_steps", 10000)
         res = b.ground_state(n_steps, kw.get("tol", 1e-10))
         results = []
@@ -733,7 +742,7 @@ def find_phase_boundary(*, param_range, make_interactions: Callable, grid, atom,
     a, b = param_range
     ia, ib = make_interactions(a), make_interactions(b)
     use_batch = (_batch_eligible(atom, ia, kw) and _batch_eligible(atom, ib, kw) and ia.c_lhy == ib.c_lhy
-                 if batched is None else bool(batched))
+                 and _nematic_c2(ia) == _nematic_c2(ib) if batched is None else bool(batched))
     if use_batch:
         dt = kw.get("dt", 0.001)
         zeeman = ZeemanParams() if kw.get("zeeman") is None else kw["zeeman"]
@@ -742,7 +751,7 @@ def find_phase_boundary(*, param_range, make_interactions: Callable, grid, atom,
             _validate_itp(zeeman, inter, atom.F, dt, p0, 0.0)
         bt = GroundStateBatch(grid=grid, atom=atom, c0s=[ia.c0, ib.c0], c1s=[ia.c1, ib.c1], psi_inits=[p0, p0],
                               zeeman=zeeman, potential=kw.get("potential"), dt=dt, c_lhy=ia.c_lhy,
-                              precision=kw.get("precision", "fp64"))
+                              c2=_nematic_c2(ia) or 0.0, precision=kw.get("precision", "fp64"))
         bt.ground_state(kw.get("n_steps", 10000), kw.get("tol", 1e-10))
         phase_a, phase_b = bt.classify_phase(0)["phase"], bt.classify_phase(1)["phase"]
         bt.close()
@@ -774,6 +783,12 @@ def _config(grid: Grid, F: int, zeeman, sim_params: SimParams, precision: str, i
     cfg.F = F
     if interactions is not None:
         cfg.c0, cfg.c1, cfg.c_lhy = interactions.c0, interactions.c1, interactions.c_lhy
+        ce = tuple(interactions.c_extra)
+        if len(ce) > _lib.SBEC_MAX_C_EXTRA:
+            raise _lib.ArgumentError("too many c_extra entries")
+        cfg.n_c_extra = len(ce)
+        for i, v in enumerate(ce):
+            cfg.c_extra[i] = float(v)
     z = zeeman(0.0) if callable(zeeman) else zeeman
     cfg.zeeman_p, cfg.zeeman_q = z.p, z.q
     cfg.dt = sim_params.dt
@@ -794,12 +809,13 @@ class GroundStateBatch:
     ``grids`` gives one grid per solve (sbec_batch_create_grids: solves are grouped by grid
     and the groups advance concurrently), with ``potential`` evaluated on each grid.
     ``atoms`` (one AtomSpecies per solve, with ``grids``) mixes spins: solves are grouped by
-    grid and F (sbec_batch_create_mixed).
+    grid and F (sbec_batch_create_mixed).  ``c_lhy`` and the nematic ``c2`` (the reference's
+    c_extra[0], src/nematic.jl:34-51) are shared by every solve.
     """
 
     def __init__(self, *, grid: Optional[Grid] = None, atom: Optional[AtomSpecies] = None, c0s, c1s, psi_inits,
-                 zeeman=None, potential=None, dt: float = 0.005, c_lhy: float = 0.0, precision: str = "fp32",
-                 grids=None, atoms=None):
+                 zeeman=None, potential=None, dt: float = 0.005, c_lhy: float = 0.0, c2: float = 0.0,
+                 precision: str = "fp32", grids=None, atoms=None):
         lib = load()
         if (grid is None) == (grids is None):
             raise _lib.ArgumentError("give either grid (one grid for every solve) or grids (one per solve)")
@@ -821,7 +837,7 @@ class GroundStateBatch:
         self.grid = grid if grid is not None else self.grids[0]
         zeeman = ZeemanParams() if zeeman is None else zeeman
         cfg = _config(self.grid, atom.F, zeeman, SimParams(dt, 1, True, 1, 1), precision,
-                      InteractionParams(0.0, 0.0, c_lhy))
+                      InteractionParams(0.0, 0.0, c_lhy, (float(c2),) if abs(float(c2)) > 1e-30 else ()))
         c0 = np.ascontiguousarray(c0s, dtype=np.float64)
         c1 = np.ascontiguousarray(c1s, dtype=np.float64)
         h = C.c_void_p()
@@ -915,12 +931,12 @@ class GroundStateBatch:
         return _report(self._lib.sbec_batch_tuning_report, self._h)
 
 
-def batch_supported(grid: Grid, F: int, precision: str = "fp32", c_lhy: float = 0.0) -> bool:
-    """Whether solves of spin F with contact couplings on `grid` can run as a GroundStateBatch
-    (sbec_batch_supported: power-of-two axes, D in {1, 3, 5}, a row pass that fits the first
-    axis).  Needs no device."""
+def batch_supported(grid: Grid, F: int, precision: str = "fp32", c_lhy: float = 0.0, c2: float = 0.0) -> bool:
+    """Whether solves of spin F with contact couplings (and the nematic c2) on `grid` can run as
+    a GroundStateBatch (sbec_batch_supported: power-of-two axes, D in {1, 3, 5}, a row pass that
+    fits the first axis).  Needs no device."""
     cfg = _config(grid, F, ZeemanParams(), SimParams(0.005, 1, True, 1, 1), precision,
-                  InteractionParams(0.0, 0.0, c_lhy))
+                  InteractionParams(0.0, 0.0, c_lhy, (float(c2),) if abs(float(c2)) > 1e-30 else ()))
     ok = C.c_int32()
     check(load().sbec_batch_supported(C.byref(cfg), C.byref(ok)))
     return bool(ok.value)
@@ -961,13 +977,18 @@ def find_ground_states_batched(*, grid: Grid, atom: AtomSpecies, interactions: l
                                potential=None, dt: float = 0.005, n_steps: int = 10000, tol: float = 1e-10,
                                precision: str = "fp32") -> list:
     """``find_ground_state`` for many (interactions, psi0) pairs at once; one result per pair.
-    The batch takes per-solve c0 and c1 and a shared c_lhy; couplings in c_extra (the
-    nematic c2 or the tensor path) are not on the batched path."""
-    if any(abs(float(v)) > 1e-30 for ip in interactions for v in ip.c_extra):
-        raise _lib.UnsupportedError("batched solves take c0, c1 and c_lhy only; c_extra needs find_ground_state")
+    The batch takes per-solve c0 and c1 and a shared c_lhy and nematic c2; higher couplings in
+    c_extra (the tensor path) are not on the batched path."""
+    c2s = {_nematic_c2(ip) for ip in interactions}
+    if None in c2s:
+        raise _lib.UnsupportedError("batched solves take c0, c1, c_lhy and c2 only; higher c_extra needs "
+                                    "find_ground_state")
+    if len(c2s) > 1:
+        raise _lib.UnsupportedError("the solves of a batch share one nematic c2")
     b = GroundStateBatch(grid=grid, atom=atom, c0s=[ip.c0 for ip in interactions], c1s=[ip.c1 for ip in interactions],
                          psi_inits=psi_inits, zeeman=zeeman, potential=potential, dt=dt,
-                         c_lhy=interactions[0].c_lhy if interactions else 0.0, precision=precision)
+                         c_lhy=interactions[0].c_lhy if interactions else 0.0, c2=c2s.pop() if c2s else 0.0,
+                         precision=precision)
     res = b.ground_state(n_steps, tol)
     for i, r in enumerate(res):
         r["psi"] = b.psi(i)

@@ -247,7 +247,9 @@ sbec_status sbec_classify_phase(sbec_ws* ws, sbec_phase_info* out);
  * solves; a batch steps all solves that share grid, F, V, dt and Zeeman in the same
  * kernels (per-solve c0, c1 and psi), each with the find_ground_state convergence
  * test of src/ground_state.jl:138-159.  cfg: imaginary_time=1, normalize_every=1,
- * contact couplings only (no c_extra/DDI); cfg->c0/c1 are ignored.
+ * contact couplings: per-solve c0/c1 (cfg->c0/c1 are ignored), a shared c_lhy and a shared
+ * nematic c2 (cfg->c_extra[0], src/nematic.jl:34-51); no DDI, Raman, losses or couplings
+ * that switch on the tensor step.
  * psi: n_solves consecutive host psi buffers (reference layout). */
 typedef struct sbec_batch sbec_batch;
 sbec_status sbec_batch_create(const sbec_config* cfg, int32_t n_solves, const double* c0, const double* c1,
@@ -260,9 +262,10 @@ sbec_status sbec_batch_create(const sbec_config* cfg, int32_t n_solves, const do
 sbec_status sbec_batch_create_grids(const sbec_config* cfg, int32_t n_solves, const int32_t* n, const double* L,
                                     const double* c0, const double* c1, const double* const* psi,
                                     const double* const* V, sbec_batch** out);
-/* *supported = 1 when sbec_batch_create would take cfg (contact couplings without DDI,
- * Raman, losses or the nematic term; grids that take the fused passes: power-of-two axes,
- * D in {1, 3, 5} and a row pass that fits the first axis), else 0.  Needs no device. */
+/* *supported = 1 when sbec_batch_create would take cfg (contact couplings, the nematic c2
+ * included, without DDI, Raman, losses or the tensor step; grids that take the fused passes:
+ * power-of-two axes, D in {1, 3, 5} and a row pass that fits the first axis), else 0.  Needs
+ * no device. */
 sbec_status sbec_batch_supported(const sbec_config* cfg, int32_t* supported);
 /* The same with a spin F per solve (F[i]; cfg->F is ignored): solves are grouped by grid and F,
  * and psi[i] holds 2F[i]+1 components.  No counterpart in the reference, whose callers loop

@@ -177,6 +177,52 @@ def test_batch_spin2_fp64_against_oracle(gpu):
     b.close()
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_batch_spin2_nematic_against_oracle(gpu, precision):
+    """Spin-2 solves with the nematic (singlet-pair) c2 shared by the batch: the pair step in
+    both potential stages of the fused passes and the pair energy in the convergence test."""
+    og = O.make_grid(O.GridConfig((32, 32), (16.0, 16.0)))
+    hg = S.make_grid(S.GridConfig((32, 32), (16.0, 16.0)))
+    states = ["polar", "ferromagnetic", "random", "uniform"]
+    c1s = [0.5, -0.5, 0.2, -0.1]
+    c2 = -0.4
+    psis = [O.init_psi(og, 2, st, seed=80 + i) for i, st in enumerate(states)]
+    n_steps = 200 if precision == "fp64" else 800
+    b = S.GroundStateBatch(grid=hg, atom=S.AtomSpecies("f2", 2), c0s=[10.0] * 4, c1s=c1s, psi_inits=psis,
+                           potential=S.HarmonicTrap(1.0, 1.0), dt=0.005, c2=c2, precision=precision)
+    res = b.ground_state(n_steps, 1e-9)
+    for i, (p0, c1, r) in enumerate(zip(psis, c1s, res)):
+        ro = O.find_ground_state(grid=og, atom=O.AtomSpecies("f2", 2),
+                                 interactions=O.InteractionParams(10.0, c1, 0.0, (c2,)),
+                                 V=O.harmonic_potential(og, (1.0, 1.0)), psi_init=p0, dt=0.005, n_steps=n_steps,
+                                 tol=1e-9)
+        if precision == "fp64":
+            assert r["steps"] == ro["steps"] and r["converged"] == ro["converged"]
+            assert abs(r["energy"] - ro["energy"]) <= ENERGY_TOL_FP64 * 10 * abs(ro["energy"])
+            assert rel_psi_err(b.psi(i), ro["workspace"].psi) < PSI_TOL_FP64
+        else:
+            # FP32 bulk: the energy bar of the batched form against the FP64 oracle
+            assert abs(r["energy"] - ro["energy"]) / abs(ro["energy"]) < 1e-6
+    b.close()
+
+
+def test_multistart_spin2_nematic_runs_batched(gpu):
+    """find_ground_state_multistart takes the batch for spin-2 contact couplings with c2 and
+    gives the one-at-a-time results."""
+    hg = S.make_grid(S.GridConfig((32, 32), (16.0, 16.0)))
+    kw = dict(grid=hg, atom=S.AtomSpecies("f2", 2), interactions=S.InteractionParams(10.0, 0.3, 0.0, (0.5,)),
+              potential=S.HarmonicTrap(1.0, 1.0), dt=0.005, n_steps=300, tol=1e-9, n_random=2, precision="fp64")
+    rb = S.find_ground_state_multistart(batched=None, **kw)
+    rs = S.find_ground_state_multistart(batched=False, **kw)
+    assert rb["initial_state"] == rs["initial_state"]
+    for a, c in zip(rb["all_results"], rs["all_results"]):
+        assert a["steps"] == c["steps"] and a["converged"] == c["converged"]
+        assert abs(a["energy"] - c["energy"]) <= 1e-11 * abs(c["energy"])
+    rb["workspace"].close()
+    for a in rs["all_results"]:
+        a["workspace"].close()
+
+
 def test_tune_table_import_fixes_the_variant(gpu):
     """A shape found in an imported tune table is not timed again: the workspace reports the
     table's variant, and an exported table loads back unchanged."""

@@ -71,10 +71,19 @@ def test_fp32_nematic_against_oracle(gpu, F, c2):
     ws_g.close()
 
 
-def test_batch_with_nematic_is_unsupported(gpu):
+def test_batch_nematic_needs_one_shared_c2(gpu):
+    """The batch takes the nematic c2 as one value for every solve; per-solve c2 values and
+    couplings that switch on the tensor step stay on find_ground_state."""
     g = S.make_grid(S.GridConfig((32, 32), (16.0, 16.0)))
-    psis = [S.init_psi(g, 1, "polar") for _ in range(2)]
+    psis = [S.init_psi(g, 2, "polar") for _ in range(2)]
+    f2 = S.AtomSpecies("f2", 2)
     with pytest.raises(S.UnsupportedError):
-        S.find_ground_states_batched(grid=g, atom=S.Rb87, interactions=[S.InteractionParams(10.0, 0.5, 0.0, (5.0,))] * 2,
+        S.find_ground_states_batched(grid=g, atom=f2, interactions=[S.InteractionParams(10.0, 0.5, 0.0, (5.0,)),
+                                                                    S.InteractionParams(10.0, 0.5, 0.0, (4.0,))],
+                                     psi_inits=psis, potential=S.HarmonicTrap(1.0, 1.0), dt=0.005, n_steps=10,
+                                     tol=1e-12, precision="fp32")
+    with pytest.raises(S.UnsupportedError):
+        S.find_ground_states_batched(grid=g, atom=f2, interactions=[S.InteractionParams(10.0, 0.5, 0.0,
+                                                                                        (0.5, 0.0, 0.3))] * 2,
                                      psi_inits=psis, potential=S.HarmonicTrap(1.0, 1.0), dt=0.005, n_steps=10,
                                      tol=1e-12, precision="fp32")

@@ -6,7 +6,9 @@ created) and checked against the FP64 oracle on the fused row/column path, the
 batched ground state and the unfused x-line path (3-D with DDI).  With tuning on,
 the decisions are reported and two workspaces of one shape give identical
 results.  The ping-pong stage form (variants 4-7) does the arithmetic of the in-place
-form (variants 0-3) in the same order, so the two give bit-identical states."""
+form (variants 0-3) in the same order, so the two give bit-identical states; so does the
+register-resident row pass (variants 12-15) against the tile form of the same plan and
+tile scale (variants 4-7)."""
 
 import os
 
@@ -19,7 +21,7 @@ from parity_util import make_pair, rel_psi_err
 
 pytestmark = pytest.mark.gpu
 
-VARIANTS = list(range(8))
+VARIANTS = list(range(8)) + [12, 13, 14, 15]
 
 
 class _env:
@@ -104,6 +106,37 @@ def test_ping_pong_stages_bit_identical(gpu, v):
         psis.append(ws_g.psi.copy())
         ws_g.close()
     assert np.array_equal(psis[0], psis[1])
+
+
+@pytest.mark.parametrize("v", [4, 5, 6, 7])
+@pytest.mark.parametrize("shape", [((128, 64), (20.0, 20.0), 1), ((256,), (20.0,), 1), ((64, 32), (16.0, 8.0), 2)])
+def test_register_row_pass_bit_identical(gpu, v, shape):
+    n, L, F = shape
+    psis = []
+    for form in (v, v + 8):
+        with _env(SBEC_TUNE_FORCE=form):
+            ws_g = make_pair(n, L, F, c0=10.0, c1=0.5, omega=(1.0,) * len(n), zeeman=(0.0, 0.1), dt=1e-3,
+                             precision="fp32", state="random", seed=5)[1]
+        S.split_step(ws_g, 30)
+        assert f"row variant {form} (forced)" in ws_g.tuning_report
+        psis.append(ws_g.psi.copy())
+        ws_g.close()
+    assert np.array_equal(psis[0], psis[1])
+
+
+@pytest.mark.parametrize("v", [4, 5, 6, 7])
+def test_register_row_pass_itp_matches_tile_form(gpu, v):
+    # imaginary time: the renormalisation sums (FP64) are added in another order, so the
+    # states agree to the last bits rather than bit for bit
+    psis = []
+    for form in (v, v + 8):
+        with _env(SBEC_TUNE_FORCE=form):
+            ws_g = make_pair((64, 64), (20.0, 20.0), 1, c0=10.0, c1=-0.5, omega=(1.0, 1.0), dt=5e-3,
+                             itp=True, precision="fp32", state="random", seed=7)[1]
+        S.split_step(ws_g, 40)
+        psis.append(ws_g.psi.copy())
+        ws_g.close()
+    assert rel_psi_err(psis[1], psis[0]) < 1e-6
 
 
 def test_tuning_reports_and_is_shared(gpu):

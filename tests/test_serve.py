@@ -101,6 +101,8 @@ def test_batch_supported_follows_the_fused_passes(libsbec):
     assert not api.batch_supported(make_grid(GridConfig((48, 40), (12.0, 10.0))), 1)  # Bluestein axes
     assert not api.batch_supported(make_grid(GridConfig((16, 16, 16), (8.0,) * 3)), 6)  # D = 13
     assert not api.batch_supported(make_grid(GridConfig((4096,), (40.0,))), 1)
+    # the nematic c2 rides on the fused passes
+    assert api.batch_supported(make_grid(GridConfig((64, 64), (20.0, 20.0))), 2, c2=0.4)
 
 
 def test_merge_key_admits_only_contact_ground_states(libsbec):
