@@ -7,8 +7,8 @@ batched ground state and the unfused x-line path (3-D with DDI).  With tuning on
 the decisions are reported and two workspaces of one shape give identical
 results.  The ping-pong stage form (variants 4-7) does the arithmetic of the in-place
 form (variants 0-3) in the same order, so the two give bit-identical states; so does the
-register-resident row pass (variants 12-15) against the tile form of the same plan and
-tile scale (variants 4-7)."""
+register-resident row pass and strided lines (variants 12-15) against the tile forms of
+the same plan and tile scale (variants 4-7)."""
 
 import os
 
@@ -109,7 +109,8 @@ def test_ping_pong_stages_bit_identical(gpu, v):
 
 
 @pytest.mark.parametrize("v", [4, 5, 6, 7])
-@pytest.mark.parametrize("shape", [((128, 64), (20.0, 20.0), 1), ((256,), (20.0,), 1), ((64, 32), (16.0, 8.0), 2)])
+@pytest.mark.parametrize("shape", [((128, 64), (20.0, 20.0), 1), ((256,), (20.0,), 1), ((64, 32), (16.0, 8.0), 2),
+                                   ((32, 64, 32), (16.0, 16.0, 16.0), 1)])
 def test_register_row_pass_bit_identical(gpu, v, shape):
     n, L, F = shape
     psis = []
