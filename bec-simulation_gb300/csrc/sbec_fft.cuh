@@ -215,43 +215,73 @@ __host__ __device__ constexpr int reg_slot(int e) {
   return e / RAD + (e % RAD) * (E / RAD);
 }
 
-// First stage: registers -> dst (lines l0 .. l0+D-1 of the tile, element i of line l at
-// i*SI + l*SL, as in the tile transforms).
-template <typename R, int N, int E, int RAD, int SIGN, int D>
-__device__ __forceinline__ void reg_stage_first(const cplx<R> (&u)[D][E], cplx<R>* dst, int SI, int SL, int l0,
-                                                int t, const Tw<R>& tw) {
+// Shared-memory index of element i of line l for the register-resident transforms.  Rows
+// (RegRowIx): line after line, one complex of padding after every 16, which takes the 4-way
+// bank conflicts out of the radix-4/8 Stockham stores (j*RAD + r, a stride of RAD elements
+// across a half-warp) at 1/16 more shared memory.  Strided tiles (RegColIx): element (i, w)
+// at i*W + w, as the tile form (consecutive threads are consecutive lines there).
+struct RegRowIx {
+  int line;  // N + N/16
+  __device__ __forceinline__ int operator()(int i, int l) const { return l * line + i + (i >> 4); }
+};
+struct RegColIx {
+  int W;
+  __device__ __forceinline__ int operator()(int i, int l) const { return i * W + l; }
+};
+
+// Stores of one stage after fft_stage_math (the autosorted positions of fft_stage_store).
+template <typename R, int N, int E, int RAD, typename Ix>
+__device__ __forceinline__ void reg_stage_store(cplx<R>* dst, const Ix& ix, int l, int t, int Ns,
+                                                const cplx<R> (&v)[E]) {
+  constexpr int TPL = N / E;
+  constexpr int NBT = E / RAD;
+#pragma unroll
+  for (int b = 0; b < NBT; ++b) {
+    const int j = t + b * TPL;
+    const int jm = j & (Ns - 1);
+    const int base = (j - jm) * RAD + jm;
+#pragma unroll
+    for (int r = 0; r < RAD; ++r) dst[ix(base + r * Ns, l)] = v[b * RAD + r];
+  }
+}
+
+// First stage: registers -> dst (lines l0 .. l0+D-1 of the tile).
+template <typename R, int N, int E, int RAD, int SIGN, int D, typename Ix>
+__device__ __forceinline__ void reg_stage_first(const cplx<R> (&u)[D][E], cplx<R>* dst, const Ix& ix, int l0, int t,
+                                                const Tw<R>& tw) {
 #pragma unroll
   for (int c = 0; c < D; ++c) {
     cplx<R> v[E];
 #pragma unroll
     for (int e = 0; e < E; ++e) v[e] = u[c][reg_slot<E, RAD>(e)];
-    fft_stage_store<R, N, E, RAD, SIGN>(dst, SI, SL, l0 + c, t, 1, tw, v);
+    fft_stage_math<R, N, E, RAD, SIGN>(t, 1, tw, v);
+    reg_stage_store<R, N, E, RAD>(dst, ix, l0 + c, t, 1, v);
   }
 }
 
-template <typename R, int N, int E, int RAD>
-__device__ __forceinline__ void reg_stage_load(const cplx<R>* src, int SI, int SL, int l, int t, cplx<R> (&v)[E]) {
+template <typename R, int N, int E, int RAD, typename Ix>
+__device__ __forceinline__ void reg_stage_load(const cplx<R>* src, const Ix& ix, int l, int t, cplx<R> (&v)[E]) {
   constexpr int TPL = N / E;
   constexpr int NBT = E / RAD;
   constexpr int STRIDE = N / RAD;
 #pragma unroll
   for (int b = 0; b < NBT; ++b) {
 #pragma unroll
-    for (int r = 0; r < RAD; ++r) v[b * RAD + r] = src[(t + b * TPL + r * STRIDE) * SI + l * SL];
+    for (int r = 0; r < RAD; ++r) v[b * RAD + r] = src[ix(t + b * TPL + r * STRIDE, l)];
   }
 }
 
 // Stages after the first: inner stages through shared memory, the last one into registers.
 // On entry cur holds the previous stage's output and every thread has passed the barrier
 // after its stores; oth is free (ping-pong form).
-template <typename R, int N, int E, int SIGN, bool PP, int D, int RAD, int... REST>
-__device__ __forceinline__ void reg_stages(cplx<R> (&u)[D][E], cplx<R>*& cur, cplx<R>*& oth, int SI, int SL, int l0,
+template <typename R, int N, int E, int SIGN, bool PP, int D, typename Ix, int RAD, int... REST>
+__device__ __forceinline__ void reg_stages(cplx<R> (&u)[D][E], cplx<R>*& cur, cplx<R>*& oth, const Ix& ix, int l0,
                                            int t, int Ns, const Tw<R>& tw) {
   if constexpr (sizeof...(REST) == 0) {
 #pragma unroll
     for (int c = 0; c < D; ++c) {
       cplx<R> v[E];
-      reg_stage_load<R, N, E, RAD>(cur, SI, SL, l0 + c, t, v);
+      reg_stage_load<R, N, E, RAD>(cur, ix, l0 + c, t, v);
       fft_stage_math<R, N, E, RAD, SIGN>(t, Ns, tw, v);
 #pragma unroll
       for (int e = 0; e < E; ++e) u[c][reg_slot<E, RAD>(e)] = v[e];
@@ -261,8 +291,9 @@ __device__ __forceinline__ void reg_stages(cplx<R> (&u)[D][E], cplx<R>*& cur, cp
 #pragma unroll
       for (int c = 0; c < D; ++c) {
         cplx<R> v[E];
-        reg_stage_load<R, N, E, RAD>(cur, SI, SL, l0 + c, t, v);
-        fft_stage_store<R, N, E, RAD, SIGN>(oth, SI, SL, l0 + c, t, Ns, tw, v);
+        reg_stage_load<R, N, E, RAD>(cur, ix, l0 + c, t, v);
+        fft_stage_math<R, N, E, RAD, SIGN>(t, Ns, tw, v);
+        reg_stage_store<R, N, E, RAD>(oth, ix, l0 + c, t, Ns, v);
       }
       __syncthreads();
       cplx<R>* x = cur;
@@ -271,13 +302,16 @@ __device__ __forceinline__ void reg_stages(cplx<R> (&u)[D][E], cplx<R>*& cur, cp
     } else {
       cplx<R> v[D][E];
 #pragma unroll
-      for (int c = 0; c < D; ++c) reg_stage_load<R, N, E, RAD>(cur, SI, SL, l0 + c, t, v[c]);
+      for (int c = 0; c < D; ++c) reg_stage_load<R, N, E, RAD>(cur, ix, l0 + c, t, v[c]);
       __syncthreads();
 #pragma unroll
-      for (int c = 0; c < D; ++c) fft_stage_store<R, N, E, RAD, SIGN>(cur, SI, SL, l0 + c, t, Ns, tw, v[c]);
+      for (int c = 0; c < D; ++c) {
+        fft_stage_math<R, N, E, RAD, SIGN>(t, Ns, tw, v[c]);
+        reg_stage_store<R, N, E, RAD>(cur, ix, l0 + c, t, Ns, v[c]);
+      }
       __syncthreads();
     }
-    reg_stages<R, N, E, SIGN, PP, D, REST...>(u, cur, oth, SI, SL, l0, t, Ns * RAD, tw);
+    reg_stages<R, N, E, SIGN, PP, D, Ix, REST...>(u, cur, oth, ix, l0, t, Ns * RAD, tw);
   }
 }
 
@@ -285,22 +319,22 @@ __device__ __forceinline__ void reg_stages(cplx<R> (&u)[D][E], cplx<R>*& cur, cp
 // form): cur may still be read by the last stage of a transform before.  The in-place
 // form has one buffer and waits for those reads first.  On return the last stage has
 // read cur and oth is free again.
-template <typename R, int N, int E, int SIGN, bool PP, int D, int RAD0, int... REST>
-__device__ __forceinline__ void reg_fft_run(cplx<R> (&u)[D][E], cplx<R>*& cur, cplx<R>*& oth, int SI, int SL, int l0,
+template <typename R, int N, int E, int SIGN, bool PP, int D, typename Ix, int RAD0, int... REST>
+__device__ __forceinline__ void reg_fft_run(cplx<R> (&u)[D][E], cplx<R>*& cur, cplx<R>*& oth, const Ix& ix, int l0,
                                             int t, const Tw<R>& tw) {
   static_assert(sizeof...(REST) >= 1, "register transforms need at least two stages");
   if constexpr (PP) {
-    reg_stage_first<R, N, E, RAD0, SIGN, D>(u, oth, SI, SL, l0, t, tw);
+    reg_stage_first<R, N, E, RAD0, SIGN, D>(u, oth, ix, l0, t, tw);
     __syncthreads();
     cplx<R>* x = cur;
     cur = oth;
     oth = x;
   } else {
     __syncthreads();
-    reg_stage_first<R, N, E, RAD0, SIGN, D>(u, cur, SI, SL, l0, t, tw);
+    reg_stage_first<R, N, E, RAD0, SIGN, D>(u, cur, ix, l0, t, tw);
     __syncthreads();
   }
-  reg_stages<R, N, E, SIGN, PP, D, REST...>(u, cur, oth, SI, SL, l0, t, RAD0, tw);
+  reg_stages<R, N, E, SIGN, PP, D, Ix, REST...>(u, cur, oth, ix, l0, t, RAD0, tw);
 }
 
 // Radix plans per line length: E = largest radix; stages run in the listed order.
@@ -322,11 +356,11 @@ template <int N> struct FftPlan32;
                                                       int l, int t, const Tw<R>& tw, bool act) { \
       return run_stages_pp<R, NN, EE, SIGN, __VA_ARGS__>(a, b, SI, SL, l, t, 1, tw, act);        \
     }                                                                                            \
-    template <typename R, int SIGN, bool PP, int D>                                              \
+    template <typename R, int SIGN, bool PP, int D, typename Ix>                                 \
     static __device__ __forceinline__ void run_reg(cplx<R> (&u)[D][EE], cplx<R>*& cur,          \
-                                                   cplx<R>*& oth, int SI, int SL, int l0, int t, \
+                                                   cplx<R>*& oth, const Ix& ix, int l0, int t,   \
                                                    const Tw<R>& tw) {                            \
-      reg_fft_run<R, NN, EE, SIGN, PP, D, __VA_ARGS__>(u, cur, oth, SI, SL, l0, t, tw);         \
+      reg_fft_run<R, NN, EE, SIGN, PP, D, Ix, __VA_ARGS__>(u, cur, oth, ix, l0, t, tw);         \
     }                                                                                            \
   };
 SBEC_PLAN(FftPlan, 2, 2, 2)

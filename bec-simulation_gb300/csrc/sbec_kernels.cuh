@@ -331,6 +331,7 @@ k_fft_strided_reg(cplx<R>* __restrict__ data, int64_t S, int64_t inner, int64_t 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<R>* cur = reinterpret_cast<cplx<R>*>(smem_raw);
   cplx<R>* oth = cur + W * N;
+  const RegColIx ix{W};
   const int64_t o = omap ? (int64_t)omap[blockIdx.y / oper] * oper + blockIdx.y % oper : (int64_t)blockIdx.y;
   const int64_t i0 = (int64_t)blockIdx.x * W;
   const int tid = threadIdx.x;
@@ -344,9 +345,9 @@ k_fft_strided_reg(cplx<R>* __restrict__ data, int64_t S, int64_t inner, int64_t 
     u[0][k] = (live && i < n_in) ? g[(int64_t)i * S + w] : mk<R>(0, 0);
   }
   if (mode == 1) {
-    PlanOf<R, N, P>::template run_reg<R, +1, PP, 1>(u, cur, oth, W, 1, w, t, tw);
+    PlanOf<R, N, P>::template run_reg<R, +1, PP, 1>(u, cur, oth, ix, w, t, tw);
   } else {
-    PlanOf<R, N, P>::template run_reg<R, -1, PP, 1>(u, cur, oth, W, 1, w, t, tw);
+    PlanOf<R, N, P>::template run_reg<R, -1, PP, 1>(u, cur, oth, ix, w, t, tw);
     if (mode == 2) {
       // lower-axis coordinates and factors of the kinetic phase for this line
       int64_t pos = i0 + w;
@@ -375,7 +376,7 @@ k_fft_strided_reg(cplx<R>* __restrict__ data, int64_t S, int64_t inner, int64_t 
           u[0][k] = phase_mul<R>(v, last, i, (R)1, 0);
         }
       }
-      PlanOf<R, N, P>::template run_reg<R, +1, PP, 1>(u, cur, oth, W, 1, w, t, tw);
+      PlanOf<R, N, P>::template run_reg<R, +1, PP, 1>(u, cur, oth, ix, w, t, tw);
     }
   }
   pdl_trigger();
@@ -1431,7 +1432,8 @@ k_row_pass_reg(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double red[32];
   cplx<R>* cur = reinterpret_cast<cplx<R>*>(smem_raw);
-  cplx<R>* oth = cur + D * RPB * N;  // second tile of the ping-pong stages (PP)
+  cplx<R>* oth = cur + D * RPB * (N + N / 16);  // second tile of the ping-pong stages (PP)
+  const RegRowIx ix{N + N / 16};
   const int tid = threadIdx.x;
   const int rr = tid / TPL, t = tid % TPL;
   const int blk = (int)blockIdx.x;
@@ -1458,8 +1460,14 @@ k_row_pass_reg(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
       u[c][k] = v;
     }
   }
+  // the potential at the thread's positions, loaded here so that the loads overlap the
+  // inverse transform (rotated with u through the potential stage)
+  R vp[E];
+  const bool pot1 = (a.flags & RP_POT1) != 0;
+#pragma unroll
+  for (int k = 0; k < E; ++k) vp[k] = (pot1 && live) ? a.p1.V[row * N + t + k * TPL] : (R)0;
   const int l0 = rr * D;
-  if (a.flags & RP_INV_X) PlanOf<R, N, P>::template run_reg<R, +1, PP, D>(u, cur, oth, 1, N, l0, t, tw);
+  if (a.flags & RP_INV_X) PlanOf<R, N, P>::template run_reg<R, +1, PP, D>(u, cur, oth, ix, l0, t, tw);
   // The pointwise stages take the thread's E points one after another through slot 0 of u
   // (rotate_slots): a runtime loop keeps one copy of the stage's code, where unrolling
   // over the points would inline the potential stage E times per flag.
@@ -1472,7 +1480,7 @@ k_row_pass_reg(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
         cplx<R> v[D];
 #pragma unroll
         for (int c = 0; c < D; ++c) v[c] = u[c][0];
-        const R Vp = a.p1.V[row * N + t + k * TPL];
+        const R Vp = vp[0];
         pot_stage<R, D>(v, Vp, a.p1, st, c0, c1);
         if (a.flags & RP_MID) {
 #pragma unroll
@@ -1486,16 +1494,22 @@ k_row_pass_reg(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
         for (int c = 0; c < D; ++c) u[c][0] = v[c];
       }
       rotate_slots<R, D, E>(u);
+      {
+        const R f = vp[0];
+#pragma unroll
+        for (int q = 0; q + 1 < E; ++q) vp[q] = vp[q + 1];
+        vp[E - 1] = f;
+      }
     }
   }
-  if (a.flags & (RP_FWD_X | RP_KIN_X)) PlanOf<R, N, P>::template run_reg<R, -1, PP, D>(u, cur, oth, 1, N, l0, t, tw);
+  if (a.flags & (RP_FWD_X | RP_KIN_X)) PlanOf<R, N, P>::template run_reg<R, -1, PP, D>(u, cur, oth, ix, l0, t, tw);
   if (a.flags & RP_KIN_X) {
 #pragma unroll
     for (int c = 0; c < D; ++c) {
 #pragma unroll
       for (int k = 0; k < E; ++k) u[c][k] = phase_mul<R>(u[c][k], ph.tab[0], t + k * TPL, ph.scale0, ph.unbiased);
     }
-    PlanOf<R, N, P>::template run_reg<R, +1, PP, D>(u, cur, oth, 1, N, l0, t, tw);
+    PlanOf<R, N, P>::template run_reg<R, +1, PP, D>(u, cur, oth, ix, l0, t, tw);
   }
   if (a.flags & (RP_POT2 | RP_NORM)) {
 #pragma unroll 1

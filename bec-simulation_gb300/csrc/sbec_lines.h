@@ -103,7 +103,8 @@ inline int row_threads_host(bool fp32, int n, int D, int V) {
 
 inline size_t row_smem_host(bool fp32, int n, int D, int V) {
   const int pp = (line_variant(fp32, n, V) >> 2) & 1;
-  return (size_t)(fp32 ? 8 : 16) * D * row_rpb_host(fp32, n, D, V) * n << pp;
+  const int line = row_variant_reg(line_variant(fp32, n, V)) ? n + n / 16 : n;  // register rows: padded lines
+  return (size_t)(fp32 ? 8 : 16) * D * row_rpb_host(fp32, n, D, V) * line << pp;
 }
 
 // A row-pass variant can run: at most 1024 threads and 200 KB of shared memory.

@@ -216,7 +216,7 @@ struct RegImpl {
   static void row(const LineCtx<R>& c, const Tw<R>& tw, const RowArgs<R>& a, int blocks) {
     constexpr int RPB = row_rpb_reg_v<R, NN, V>();
     constexpr int NT = RPB * (NN / PlanOf<R, NN, P>::E);
-    constexpr long TILE = (long)sizeof(cplx<R>) * D * RPB * NN;
+    constexpr long TILE = (long)sizeof(cplx<R>) * D * RPB * (NN + NN / 16);  // padded lines (RegRowIx)
     if constexpr (NT > 1024 || 2 * TILE > 200 * 1024) {
       fail(SBEC_ERR_UNSUPPORTED, "row pass tile too large for this line length");
     } else {
