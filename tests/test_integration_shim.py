@@ -21,6 +21,8 @@ JL_TO_C = {
     "Ptr{Float64}": {"double*"},
     "Ref{Float64}": {"double*"},
     "Ref{Int64}": {"int64_t*"},
+    "Ref{Int32}": {"int32_t*"},
+    "Ptr{SbecGsResult}": {"sbec_gs_result*"},
     "Ref{Ptr{Cvoid}}": {"sbec_ws**", "sbec_batch**", "void**"},
     "Ref{SbecConfig}": {"sbec_config*"},
     "Ref{SbecGsResult}": {"sbec_gs_result*"},

@@ -204,3 +204,20 @@ def test_work_estimate_orders_by_size_steps_and_ddi():
     assert w(small) < w(longer) and w(small) < w(bigger) and w(small) < w(f6) < w(f6d)
     with pytest.raises(ValueError):
         serve.Server(policy="lifo")
+
+
+def test_batch_eligibility_takes_a_nematic_c2():
+    """find_ground_state_multistart / find_phase_boundary route spin-1/2 contact couplings,
+    the nematic c2 included, through a batch; higher c_extra entries and DDI keep the
+    one-at-a-time loop."""
+    from spinorbec import api
+    from spinorbec.host import AtomSpecies, InteractionParams
+
+    f2 = AtomSpecies("f2", 2)
+    assert api._nematic_c2(InteractionParams(10.0, 0.5)) == 0.0
+    assert api._nematic_c2(InteractionParams(10.0, 0.5, 0.0, (0.4,))) == 0.4
+    assert api._nematic_c2(InteractionParams(10.0, 0.5, 0.0, (0.4, 0.0, 0.2))) is None
+    assert api._batch_eligible(f2, InteractionParams(10.0, 0.5, 0.0, (0.4,)), {})
+    assert not api._batch_eligible(f2, InteractionParams(10.0, 0.5, 0.0, (0.4, 0.0, 0.2)), {})
+    assert not api._batch_eligible(f2, InteractionParams(10.0, 0.5, 0.0, (0.4,)), {"enable_ddi": True})
+    assert not api._batch_eligible(AtomSpecies("f3", 3), InteractionParams(10.0, 0.5), {})
