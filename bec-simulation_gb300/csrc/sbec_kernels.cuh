@@ -1251,6 +1251,29 @@ enum RowFlags {
   RP_MID = 256    // after POT1: norm partial, multiply by pred[solve], POT2 (p2) — before FWD_X
 };
 
+// acc += |psi|^2 of one point (all D components), for the renormalisation sums of a row
+// pass.  FP64: added to acc component by component in FP64.  FP32: the point's sum is formed
+// in FP32 by FMAs (relative error a few units of 2^-24, without bias) and added once; the
+// sums over points stay FP64.  Per element that is two FP32 FMAs instead of two conversions
+// and three FP64 operations — on a part whose FP64 rate is 1/64 of FP32 the FP64 form made the
+// closing ITP row pass FP64-bound.  The resulting scale is rounded to FP32 anyway (it
+// multiplies FP32 data), which dominates the difference.
+template <typename R, int D>
+__device__ __forceinline__ void add_point_norm2(double& acc, const cplx<R> (&v)[D]) {
+  if constexpr (sizeof(R) == 4) {
+    float n = 0.0f;
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      n = fmaf(v[c].x, v[c].x, n);
+      n = fmaf(v[c].y, v[c].y, n);
+    }
+    acc += (double)n;
+  } else {
+#pragma unroll
+    for (int c = 0; c < D; ++c) acc += (double)v[c].x * v[c].x + (double)v[c].y * v[c].y;
+  }
+}
+
 template <typename R>
 struct RowArgs {
   cplx<R>* psi;
@@ -1340,11 +1363,9 @@ __device__ __forceinline__ void row_pass_block(const RowArgs<R>& a, const SpinTa
       const R Vp = a.p1.V[(row0 + r) * N + x];
       pot_stage<R, D>(v, Vp, a.p1, st, c0, c1);
       if (a.flags & RP_MID) {
+        add_point_norm2<R, D>(acc, v);
 #pragma unroll
-        for (int c = 0; c < D; ++c) {
-          acc += (double)v[c].x * v[c].x + (double)v[c].y * v[c].y;
-          v[c] = v[c] * pred;
-        }
+        for (int c = 0; c < D; ++c) v[c] = v[c] * pred;
         pot_stage<R, D>(v, Vp, a.p2, st, c0, c1);
       }
 #pragma unroll
@@ -1370,8 +1391,7 @@ __device__ __forceinline__ void row_pass_block(const RowArgs<R>& a, const SpinTa
 #pragma unroll
         for (int c = 0; c < D; ++c) s[(c * RPB + r) * N + x] = v[c];
       }
-#pragma unroll
-      for (int c = 0; c < D; ++c) acc += (double)v[c].x * v[c].x + (double)v[c].y * v[c].y;
+      add_point_norm2<R, D>(acc, v);
     }
     __syncthreads();
   }
@@ -1483,11 +1503,9 @@ k_row_pass_reg(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
         const R Vp = vp[0];
         pot_stage<R, D>(v, Vp, a.p1, st, c0, c1);
         if (a.flags & RP_MID) {
+          add_point_norm2<R, D>(acc, v);
 #pragma unroll
-          for (int c = 0; c < D; ++c) {
-            acc += (double)v[c].x * v[c].x + (double)v[c].y * v[c].y;
-            v[c] = v[c] * pred;
-          }
+          for (int c = 0; c < D; ++c) v[c] = v[c] * pred;
           pot_stage<R, D>(v, Vp, a.p2, st, c0, c1);
         }
 #pragma unroll
@@ -1523,8 +1541,12 @@ k_row_pass_reg(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
 #pragma unroll
           for (int c = 0; c < D; ++c) u[c][0] = v[c];
         }
+        {
+          cplx<R> v[D];
 #pragma unroll
-        for (int c = 0; c < D; ++c) acc += (double)u[c][0].x * u[c][0].x + (double)u[c][0].y * u[c][0].y;
+          for (int c = 0; c < D; ++c) v[c] = u[c][0];
+          add_point_norm2<R, D>(acc, v);
+        }
       }
       rotate_slots<R, D, E>(u);
     }
