@@ -114,3 +114,61 @@ def test_spin6_ddi_norm_and_magnetization_1d():  # test/test_physics_level3.jl:1
         if step % 50 == 0:
             assert abs(O.total_norm(ws.psi, g) - n0) / n0 < 1e-6
             assert abs(O.magnetization(ws.psi, g, 6) - m0) < 1e-4
+
+
+def _tf_density(V, g, dV):
+    """thomas_fermi_density(V, g, dV; N_target=1) (src/thomas_fermi.jl:5-45): n = max(0, (mu - V)/g)
+    with mu found by bisection so that sum(n) dV = 1."""
+    def norm(mu):
+        return float(np.sum(np.maximum(mu - V, 0.0)) / g * dV)
+    lo, hi = float(V.min()), float(V.min() + 2.0 * (V.max() - V.min()))
+    while norm(hi) < 1.0 and hi < V.max() * 100:
+        hi *= 2.0
+    for _ in range(200):
+        mid = 0.5 * (lo + hi)
+        nm = norm(mid)
+        if abs(nm - 1.0) < 1e-12:
+            lo = hi = mid
+            break
+        if nm < 1.0:
+            lo = mid
+        else:
+            hi = mid
+    mu = 0.5 * (lo + hi)
+    return np.maximum(mu - V, 0.0) / g, mu
+
+
+def test_thomas_fermi_1d():  # test/test_physics_level2.jl:6-47
+    c0 = 200.0
+    g = O.make_grid(O.GridConfig((256,), (20.0,)))
+    r = O.find_ground_state(grid=g, atom=O.AtomSpecies("t", 1), interactions=O.InteractionParams(c0, 0.0),
+                            V=O.harmonic_potential(g, (1.0,)), dt=0.005, n_steps=10000, tol=1e-10,
+                            initial_state="polar")
+    assert r["converged"]
+    dV = O.cell_volume(g)
+    x = g.x[0]
+    n_num = np.abs(r["workspace"].psi[:, 1]) ** 2
+    mu = (3 * c0 / (4 * math.sqrt(2))) ** (2 / 3)
+    n_tf = np.maximum(0.0, (mu - x ** 2 / 2) / c0)
+    n_tf /= n_tf.sum() * dV
+    assert np.sum(np.abs(n_num - n_tf)) * dV < 0.05
+    peak = n_num.max()
+    R_num = max(abs(x[i]) for i in range(len(x)) if n_num[i] > 0.01 * peak)
+    assert abs(R_num - math.sqrt(2 * mu)) / math.sqrt(2 * mu) < 0.1
+
+
+def test_thomas_fermi_2d():  # test/test_physics_level2.jl:49-83
+    c0 = 200.0
+    g = O.make_grid(O.GridConfig((64, 64), (15.0, 15.0)))
+    V = O.harmonic_potential(g, (1.0, 1.0))
+    r = O.find_ground_state(grid=g, atom=O.AtomSpecies("t", 1), interactions=O.InteractionParams(c0, 0.0), V=V,
+                            dt=0.005, n_steps=10000, tol=1e-10, initial_state="polar")
+    assert r["converged"]
+    dV = O.cell_volume(g)
+    n_num = np.abs(r["workspace"].psi[..., 1]) ** 2
+    n_tf, mu = _tf_density(V, c0, dV)
+    assert np.sum(np.abs(n_num - n_tf)) * dV < 0.10
+    peak = n_num.max()
+    X, Y = np.meshgrid(g.x[0], g.x[1], indexing="ij")
+    R_num = float(np.sqrt(X ** 2 + Y ** 2)[n_num > 0.01 * peak].max())
+    assert abs(R_num - math.sqrt(2 * mu)) / math.sqrt(2 * mu) < 0.15
