@@ -1421,16 +1421,6 @@ k_row_pass(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
   row_pass_block<R, N, D, RPB, P, PP, false>(a, st, ph, tw, (int)blockIdx.x, smem_raw, true);
 }
 
-// Register-resident form of the fused row pass: the operators, flags and arithmetic of
-// row_pass_block, with thread t of tile row rr holding positions x = t + k*TPL (k < E) of
-// all D components of its row in registers.  Every x transform starts from and ends in
-// registers (the first and last Stockham stages read and write exactly those positions,
-// reg_fft_run), so psi is loaded from and stored to global memory directly (consecutive
-// threads, consecutive x), the potential stages and the kinetic phase run on registers
-// between the transforms, and shared memory carries only the transforms' inner stages:
-// per pass half the shared-memory traffic and block barriers of the tile form, and no
-// thread idles during a transform.  The states are bit-identical to the tile form of the
-// same plan; the norm partials (RP_NORM, RP_MID) are summed in another order.
 // u[c][k] <- u[c][k+1], u[c][E-1] <- u[c][0]: after E calls u is back in its order.
 template <typename R, int D, int E>
 __device__ __forceinline__ void rotate_slots(cplx<R> (&u)[D][E]) {
@@ -1443,6 +1433,17 @@ __device__ __forceinline__ void rotate_slots(cplx<R> (&u)[D][E]) {
   }
 }
 
+// Register-resident form of the fused row pass: the operators, flags and arithmetic of
+// row_pass_block, with thread t of tile row rr holding positions x = t + k*TPL (k < E) of
+// all D components of its row in registers.  Every x transform starts from and ends in
+// registers (the first and last Stockham stages read and write exactly those positions,
+// reg_fft_run), so psi is loaded from and stored to global memory directly (consecutive
+// threads, consecutive x), the potential stages and the kinetic phase run on registers
+// between the transforms, and shared memory carries only the transforms' inner stages
+// (lines padded by one complex after every 16, RegRowIx): per pass half the shared-memory
+// traffic and block barriers of the tile form, and no thread idles during a transform.
+// The states are bit-identical to the tile form of the same plan; the norm partials
+// (RP_NORM, RP_MID) are summed in another order.
 template <typename R, int N, int D, int RPB, int P, bool PP>
 __global__ void __launch_bounds__(RPB*(N / PlanOf<R, N, P>::E))
 k_row_pass_reg(RowArgs<R> a, SpinTabs<R> st, PhaseRef<R> ph, Tw<R> tw) {
