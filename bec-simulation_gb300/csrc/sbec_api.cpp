@@ -1098,14 +1098,25 @@ sbec_status sbec_classify_phase(sbec_ws* ws, sbec_phase_info* out) {
 // ---- batches of independent ITP solves (find_ground_state per solve, one schedule)
 namespace {
 
-void check_batch_config(const sbec_config* cfg) {
+// Options a batch takes (the same for every group of a batch).
+void check_batch_options(const sbec_config* cfg) {
   if (!cfg->imaginary_time || cfg->normalize_every != 1)
     fail(SBEC_ERR_INVALID, "batched ground states need imaginary_time=1 and normalize_every=1");
   if (cfg->gS_direct || cfg->enable_ddi || cfg->raman || !(cfg->loss_gamma_dr < 1e-30 && cfg->loss_L3 < 1e-30))
     fail(SBEC_ERR_UNSUPPORTED,
          "batched ground states support contact c0/c1 (+LHY, nematic c2) couplings without DDI, Raman or losses");
-  // c_extra may carry the nematic c2 (shared by every solve); couplings that switch on the
-  // tensor step (an even c_k, k >= 4) are refused by the group's engine (no fused path)
+}
+
+// One group's grid and spin: argument errors, then the fused passes the batch runs on (no
+// tensor step — c_extra may carry the nematic c2, shared by every solve, but not an even c_k
+// with k >= 4 — D in {1, 3, 5}, power-of-two axes), all before any device work (the same test
+// as sbec_batch_supported).
+void check_batch_group(const sbec_config* cfg) {
+  const Setup s = build_setup(*cfg);
+  if (!fused_path_supported(s, cfg->precision == SBEC_FP32_BULK))
+    fail(SBEC_ERR_UNSUPPORTED,
+         "batched ground states need the fused passes: no tensor step, D in {1, 3, 5}, power-of-two axes "
+         "and a row pass that fits the first axis");
 }
 
 std::unique_ptr<EngineBase> make_batch_group(const sbec_config& cfg, int n, const double* c0, const double* c1,
@@ -1212,8 +1223,8 @@ sbec_status sbec_batch_create(const sbec_config* cfg, int32_t n_solves, const do
   need(psi, "psi");
   need(out, "out");
   *out = nullptr;
-  check_batch_config(cfg);
-  build_setup(*cfg);  // argument errors before the device check
+  check_batch_options(cfg);  // argument and support errors before the device check
+  check_batch_group(cfg);
   if (sbec_device_count() < 1) fail(SBEC_ERR_DEVICE, "no CUDA device available (the GPU path has no CPU fallback)");
   auto b = std::make_unique<sbec_batch>();
   b->groups.push_back(make_batch_group(*cfg, n_solves, c0, c1, psi, V));
@@ -1239,7 +1250,7 @@ sbec_batch* batch_create_grouped(const sbec_config* cfg, int32_t n_solves, const
   need(c1, "c1");
   need(psi, "psi");
   if (n_solves < 1) fail(SBEC_ERR_INVALID, "n_solves must be >= 1");
-  check_batch_config(cfg);
+  check_batch_options(cfg);
   std::vector<sbec_config> gcfg;
   std::vector<std::vector<int>> members;
   std::vector<int> grp(n_solves), loc(n_solves);
@@ -1257,7 +1268,7 @@ sbec_batch* batch_create_grouped(const sbec_config* cfg, int32_t n_solves, const
       if (same) g = (int)k;
     }
     if (g < 0) {
-      build_setup(c);  // argument errors before any device work
+      check_batch_group(&c);  // argument and support errors of this grid and F before any device work
       g = (int)gcfg.size();
       gcfg.push_back(c);
       members.emplace_back();

@@ -148,3 +148,39 @@ def test_tune_table_import_export(libsbec):
         S.tune_table_import("no tab here\n")
     with pytest.raises(S.ArgumentError):
         S.tune_table_import("shape\tx\n")
+
+
+def test_batch_refuses_unsupported_configs_before_device(libsbec):
+    """sbec_batch_create / _grids / _mixed refuse what the fused passes cannot run (a tensor
+    step, D = 7) with SBEC_ERR_UNSUPPORTED before any device work, on every host; a supported
+    configuration (spin 2 with a nematic c2) gets as far as the device check."""
+    import ctypes as C
+
+    import numpy as np
+
+    import spinorbec as S
+    from spinorbec import _lib, api
+
+    g = S.make_grid(S.GridConfig((32, 32), (16.0, 16.0)))
+    lib = S.load()
+
+    def create(F, c_extra):
+        cfg = api._config(g, F, S.ZeemanParams(), S.SimParams(0.005, 1, True, 1, 1), "fp64",
+                          S.InteractionParams(0.0, 0.0, 0.0, c_extra))
+        psi = np.zeros(2 * 32 * 32 * (2 * F + 1))
+        c0 = np.array([10.0]); c1 = np.array([0.1])
+        V = np.zeros(32 * 32)
+        h = C.c_void_p()
+        st = lib.sbec_batch_create(C.byref(cfg), 1, api.dptr(c0), api.dptr(c1), api.dptr(psi), api.dptr(V),
+                                   C.byref(h))
+        if st == _lib.SBEC_OK:
+            lib.sbec_batch_destroy(h)
+        return st
+
+    assert create(2, (0.5, 0.0, 0.3)) == _lib.SBEC_ERR_UNSUPPORTED  # c4 switches on the tensor step
+    assert create(3, ()) == _lib.SBEC_ERR_UNSUPPORTED               # D = 7 has no fused passes
+    st = create(2, (0.5,))                                           # nematic c2: supported
+    assert st == (_lib.SBEC_ERR_DEVICE if S.device_count() == 0 else _lib.SBEC_OK)
+    with pytest.raises(S.UnsupportedError):
+        S.GroundStateBatch(grids=[g], atoms=[S.AtomSpecies("f3", 3)], c0s=[10.0], c1s=[0.1],
+                           psi_inits=[S.init_psi(g, 3, "polar")], dt=0.005, precision="fp64")
